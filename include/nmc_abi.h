@@ -1,0 +1,318 @@
+/*
+ * nmc_abi.h - C ABI of the GB300 photon-transport engine (mcsub / mcxyz /
+ * mcxyz two-term hop-drop-spin-roulette loop and its tallies).
+ *
+ * The reference drives its GPU kernels through an Objective-C class
+ * (NMC/NMCCode/MetalMC.h:25-31):
+ *
+ *   initWithDevice:kernel_type      -> nmc_create
+ *   prepareData:run_params:tiss:v   -> nmc_prepare
+ *   setNumRunsSeed:                 -> nmc_set_num_runs_seed
+ *   sendComputeCommand              -> nmc_send_compute_command
+ *   getComputeResults: (16 arrays)  -> nmc_get_compute_results
+ *
+ * Everything here is plain C: pointers, sizes and POD structs, no CUDA or
+ * torch types.  Every entry point returns an nmc_status and never exits the
+ * process (the reference calls exit(1) on bad input, mcio.h:163).
+ *
+ * The two configuration PODs are byte-identical to the reference's
+ * `struct RunParams` (172 bytes) and `struct TissueParams` (608 bytes)
+ * (NMC/NMCCode/definitions.h:186-218); they carry an nmc_ prefix so that a
+ * caller may include this header next to the reference's definitions.h and
+ * pass `(const nmc_run_params*)&runParams`.
+ */
+#ifndef NMC_ABI_H
+#define NMC_ABI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NMC_ABI_VERSION 1
+
+/* definitions.h:57-58 (Ntiss, STRLEN) */
+#define NMC_NTISS 19
+#define NMC_STRLEN 32
+
+/* Reference compile-time constants kept as defaults (definitions.h:16-82). */
+#define NMC_PHOTON_TOTAL_DEFAULT 100000u /* PHOTON_TOTAL */
+#define NMC_PHOTON_BATCH_DEFAULT 10000u  /* PHOTON_BATCH */
+#define NMC_MCSUB_BINS_DEFAULT 101       /* BINS (bins 1..BINS, BINS = overflow) */
+#define NMC_MCSUB_DR_DEFAULT 0.0020f     /* dr_mcsub */
+#define NMC_MCSUB_DZ_DEFAULT 0.0020f     /* dz_mcsub */
+
+/* Simulation kinds: same values as enum MC_SIM_TYPE (definitions.h:151-164). */
+typedef enum nmc_sim_type {
+  NMC_SIM_MCSUB = 0,
+  NMC_SIM_MCXYZ = 1,
+  NMC_SIM_MCXYZ_TT = 2,
+  NMC_SIM_POLARIZATION_CBS_ELECTRIC_FIELDS = 3,
+  NMC_SIM_POLARIZATION_MUELLER_STOKES = 4,
+  NMC_SIM_RAMAN = 5
+} nmc_sim_type;
+
+/* Detection side: enum MC_PH_PACKETS_DETECTION_STATE (definitions.h:168-172). */
+enum { NMC_DET_REFLECTANCE = 0, NMC_DET_TRANSMITTANCE = 1 };
+
+/* struct RunParams, definitions.h:186-209.  Enums are 4-byte ints. */
+typedef struct nmc_run_params {
+  char myname[NMC_STRLEN];
+  int32_t mcflag, launchflag, boundaryflag, speckleflag, semiflag;
+  float xfocus, yfocus, zfocus;
+  float ux0, uy0, uz0;
+  float radius, det_radius, xd;
+  float waist;
+  float zsurf;
+  float n1, n2;
+  float na, lambda, lc;
+  int32_t det_state; /* enum MC_PH_PACKETS_DETECTION_STATE */
+  int32_t ph_quant;  /* enum MC_PH_PACKETS_QUANTITY */
+  float dx, dy, dz;
+  int32_t Nx, Ny, Nz, Nt;
+  float xs, ys, zs;
+  float time_min;
+  int32_t mckernelflag; /* enum MC_SIM_TYPE */
+} nmc_run_params;
+
+/* struct TissueParams, definitions.h:211-218.  Index 0 is unused by the
+ * reference's readers (tissue ids are 1..Nt, mcio.h:128). */
+typedef struct nmc_tissue_params {
+  float muav[NMC_NTISS];
+  float musv[NMC_NTISS];
+  float gv[NMC_NTISS];
+  float gf[NMC_NTISS], af[NMC_NTISS], gb[NMC_NTISS], ab[NMC_NTISS], CC[NMC_NTISS];
+} nmc_tissue_params;
+
+#if defined(__cplusplus)
+static_assert(sizeof(nmc_run_params) == 172, "RunParams must stay 172 bytes");
+static_assert(offsetof(nmc_run_params, n1) == 96, "RunParams.n1 offset");
+static_assert(offsetof(nmc_run_params, det_state) == 116, "RunParams.det_state offset");
+static_assert(offsetof(nmc_run_params, dx) == 124, "RunParams.dx offset");
+static_assert(offsetof(nmc_run_params, Nx) == 136, "RunParams.Nx offset");
+static_assert(offsetof(nmc_run_params, xs) == 152, "RunParams.xs offset");
+static_assert(offsetof(nmc_run_params, time_min) == 164, "RunParams.time_min offset");
+static_assert(offsetof(nmc_run_params, mckernelflag) == 168, "RunParams.mckernelflag offset");
+static_assert(sizeof(nmc_tissue_params) == 608, "TissueParams must stay 608 bytes");
+#elif defined(__STDC_VERSION__) && __STDC_VERSION__ >= 201112L
+_Static_assert(sizeof(nmc_run_params) == 172, "RunParams must stay 172 bytes");
+_Static_assert(sizeof(nmc_tissue_params) == 608, "TissueParams must stay 608 bytes");
+#endif
+
+/* ---------------------------------------------------------------- status */
+typedef enum nmc_status {
+  NMC_OK = 0,
+  NMC_EINVAL = 1,      /* bad argument or configuration */
+  NMC_EIO = 2,         /* file missing, short or malformed */
+  NMC_EDEVICE = 3,     /* CUDA error or missing device */
+  NMC_ETIMEOUT = 4,    /* host wait exceeded nmc_ext.timeout_s */
+  NMC_ESTEPCAP = 5,    /* a photon hit the device-side step cap */
+  NMC_ENOMEM = 6,      /* host or device allocation failed */
+  NMC_EUNSUPPORTED = 7,/* kind or option not built */
+  NMC_ESTATE = 8       /* call out of order (e.g. run before prepare) */
+} nmc_status;
+
+/* ---------------------------------------------------------- extensions */
+/* Random number streams. */
+enum {
+  /* Philox4x32-10, key = (seed lo, seed hi), counter = (photon id lo,
+   * photon id hi, block #, 0x4E4D4321).  Each photon owns one stream, so
+   * results do not depend on thread mapping. */
+  NMC_RNG_PHILOX = 0,
+  /* The reference's Tausworthe/xorshift generator with its own per-thread
+   * seeding (helpers.metal:319-371, kernels.metal:91-95,339-343,772); photon
+   * id p maps to (run = p / photons_per_dispatch + 1, index = p %
+   * photons_per_dispatch) exactly as main.m:159-168 dispatches them. */
+  NMC_RNG_TAUS_REF = 1
+};
+
+/* Phase function of the mcsub kernel. */
+enum {
+  NMC_PHASE_HG = 0,            /* Henyey-Greenstein with gv[1] */
+  NMC_PHASE_ISOTROPIC_REF = 1, /* what MCSubKernel actually samples (kernels.metal:252) */
+  NMC_PHASE_TWO_TERM = 2       /* two-term HG with gf/af/gb/ab/CC[1] (kernels.metal:1053-1070) */
+};
+
+/* Reference behaviours that are switchable (default = reference behaviour). */
+enum {
+  /* Two-term kernel: replay the run-1 RNG streams on every dispatch, as the
+   * reference does because its host binds DetPhot2D where the kernel reads
+   * iRunNum (MetalMC.m:462-473 vs kernels.metal:757-768). */
+  NMC_FLAG_TT_REPLAY_RUN1 = 1u << 0,
+  /* Disable the mcxyz MIN_VALUE / MAX_SCATT kill (kernels.metal:747). */
+  NMC_FLAG_NO_HARD_KILL = 1u << 1
+};
+
+typedef struct nmc_ext {
+  uint32_t size;                 /* sizeof(nmc_ext); set by nmc_ext_defaults */
+  uint32_t rng;                  /* NMC_RNG_* */
+  uint64_t seed;                 /* Philox key */
+  uint32_t phase;                /* NMC_PHASE_* (mcsub only) */
+  uint32_t flags;                /* NMC_FLAG_* */
+  uint64_t photons_per_dispatch; /* PHOTON_BATCH */
+  uint64_t photons_total;        /* PHOTON_TOTAL (CLI and normalisation) */
+  /* mcsub geometry and beam: compile-time #defines in the reference
+   * (definitions.h:30-54), run-time here. */
+  int32_t sub_bins;              /* BINS: bins 1..BINS, BINS = overflow */
+  float sub_dr, sub_dz;
+  int32_t sub_mcflag;            /* 0 collimated, 1 Gaussian focus, 2 isotropic point */
+  int32_t sub_boundaryflag;      /* 0 infinite, 1 air/tissue surface */
+  float sub_radius, sub_waist, sub_zfocus, sub_xs, sub_ys, sub_zs;
+  /* launch shape; 0 = chosen by the runtime */
+  int32_t block_size;
+  int32_t blocks_per_sm;
+  double timeout_s;              /* host wait limit per call */
+  uint32_t reserved[8];
+} nmc_ext;
+
+/* Totals since nmc_prepare / nmc_reset.  Sums are un-normalised weights. */
+typedef struct nmc_summary {
+  uint64_t photons;      /* photons completed */
+  uint64_t substeps;     /* mcsub hops / mcxyz voxel sub-steps, counted on the device */
+  uint64_t scatters;     /* SPIN events */
+  double S, A, E;        /* specular, absorbed, escaped weight (SAE of MCSubKernel) */
+  double rd_sum;         /* sum over photons of detected weight */
+  double rd_sumsq;       /* sum over photons of (detected weight)^2 */
+  double kernel_ms;      /* device time of transport launches (CUDA events) */
+  uint32_t launches;     /* transport kernel launches */
+  uint32_t device_flags; /* NMC_DEVFLAG_* raised by kernels */
+} nmc_summary;
+
+enum { NMC_DEVFLAG_STEPCAP = 1u << 0, NMC_DEVFLAG_BADTISSUE = 1u << 1 };
+
+/* FP64 tallies readable with nmc_get_tally_f64. */
+typedef enum nmc_tally {
+  NMC_TALLY_J = 0,        /* mcsub escaping flux J[ir], BINS+1 values (index 0 unused) */
+  NMC_TALLY_F = 1,        /* mcsub F[ir*BINS+iz], (BINS+1)^2 values */
+  NMC_TALLY_F3D = 2,      /* mcxyz deposition, Nx*Ny*Nz, index iz*Ny*Nx + ix*Ny + iy */
+  NMC_TALLY_RD2D = 3,     /* mcxyz detected weight map, Nx*Ny, index ix*Ny + iy */
+  NMC_TALLY_DETPHOT2D = 4,/* mcxyz detected photon counts, Nx*Ny */
+  NMC_TALLY_RD_SLOTS = 5  /* per dispatch slot Rd (kernels.metal:753), photons_per_dispatch */
+} nmc_tally;
+
+/* Per-photon record written by nmc_run_traced (parity tests). */
+typedef struct nmc_photon_record {
+  uint32_t n_scatt;   /* SPIN events */
+  uint32_t n_sub;     /* mcsub hops / mcxyz voxel sub-steps */
+  uint32_t fate;      /* NMC_FATE_* */
+  uint32_t n_detect;  /* detection events */
+  float w_final;      /* weight when the photon died */
+  float absorbed;     /* sum of dropped weight (including outside the grid) */
+  float detected;     /* escaped (mcsub E) or detected (mcxyz Rd_loc) weight */
+  float x, y, z;      /* final position */
+} nmc_photon_record;
+
+enum {
+  NMC_FATE_ALIVE = 0,
+  NMC_FATE_ESCAPED = 1,   /* mcsub escape through the surface */
+  NMC_FATE_ROULETTE = 2,  /* lost the roulette */
+  NMC_FATE_MINWEIGHT = 3, /* W < MIN_VALUE (kernels.metal:747) */
+  NMC_FATE_MAXSCATT = 4,  /* num_scatt > MAX_SCATT (kernels.metal:747) */
+  NMC_FATE_BOUNDARY = 5,  /* left the grid (boundaryflag 1/2) or z < 0 (two-term) */
+  NMC_FATE_STEPCAP = 6    /* device-side step cap (not a reference behaviour) */
+};
+
+/* ------------------------------------------------------------- lifecycle */
+typedef struct nmc_handle nmc_handle;
+
+/* Defaults equal to the reference's compile-time constants. */
+void nmc_ext_defaults(nmc_ext* ext);
+
+/* ABI version of the loaded library (NMC_ABI_VERSION). */
+int32_t nmc_abi_version(void);
+
+/* Replaces -[MetalMC initWithDevice::] (MetalMC.h:26, MetalMC.m:96-177):
+ * selects the transport kernel for `sim_type` (an nmc_sim_type) on CUDA
+ * device `device`.  Kinds whose reference kernel is an empty stub
+ * (kernels.metal:1122-1202) return NMC_EUNSUPPORTED. */
+nmc_status nmc_create(int32_t sim_type, int32_t device, nmc_handle** out);
+
+/* Replaces -[MetalMC prepareData:::] (MetalMC.h:27, MetalMC.m:179-383):
+ * copies the run and tissue parameters and, for the voxel kinds, the
+ * Nx*Ny*Nz uint8 tissue map (index iz*Ny*Nx + ix*Ny + iy) to the device and
+ * clears all tallies.  `v` may be NULL for mcsub. */
+nmc_status nmc_prepare(nmc_handle* h, const nmc_run_params* rp,
+                       const nmc_tissue_params* tp, const uint8_t* v);
+
+/* Extension knobs (RNG, phase function, mcsub bins and beam, launch shape).
+ * Call before nmc_prepare or between runs; defaults from nmc_ext_defaults. */
+nmc_status nmc_set_ext(nmc_handle* h, const nmc_ext* ext);
+
+/* Replaces -[MetalMC setNumRunsSeed::] (MetalMC.h:30, MetalMC.m:498-505).
+ * The next nmc_send_compute_command simulates photons
+ * [(run-1)*photons_per_dispatch, run*photons_per_dispatch).  The reference
+ * never reads time_seed (its kernels seed from run and thread index only);
+ * it is accepted and ignored. */
+nmc_status nmc_set_num_runs_seed(nmc_handle* h, int32_t run, float time_seed);
+
+/* Replaces -[MetalMC sendComputeCommand] (MetalMC.h:28, MetalMC.m:385-496):
+ * one blocking dispatch of photons_per_dispatch photons. */
+nmc_status nmc_send_compute_command(nmc_handle* h);
+
+/* Simulates photons [first_photon, first_photon + n_photons) with one
+ * persistent launch and waits for it.  Tallies accumulate. */
+nmc_status nmc_run(nmc_handle* h, uint64_t first_photon, uint64_t n_photons);
+
+/* Same as nmc_run but returns as soon as the work is queued on the handle's
+ * stream; nmc_synchronize waits for it. */
+nmc_status nmc_run_async(nmc_handle* h, uint64_t first_photon, uint64_t n_photons);
+nmc_status nmc_synchronize(nmc_handle* h);
+
+/* nmc_run that also writes one nmc_photon_record per photon into `recs`
+ * (n_photons entries) and, when `events` is not NULL, the (x, y, z, W)
+ * state after each of the first `k_events` SPIN events of every photon
+ * (n_photons * k_events * 4 floats, unused entries NaN). */
+nmc_status nmc_run_traced(nmc_handle* h, uint64_t first_photon, uint64_t n_photons,
+                          nmc_photon_record* recs, float* events, uint32_t k_events);
+
+/* Replaces -[MetalMC getComputeResults:...] (MetalMC.h:29, MetalMC.m:508-824):
+ * ADDS (+=) the device tallies accumulated since nmc_prepare / nmc_reset into
+ * the caller's arrays, in the reference's layouts:
+ *   J          BINS+1 floats, J[ir], ir = 1..BINS
+ *   F          (BINS+1)*(BINS+1) floats, F[ir*BINS + iz], ir, iz = 1..BINS
+ *              (the reference sizes these BINS and BINS*BINS and writes one
+ *              bin past them, kernels.metal:202-234; here they are sized to
+ *              hold every index the formula produces)
+ *   F3D        Nx*Ny*Nz floats, F3D[iz*Ny*Nx + ix*Ny + iy]
+ *   SAE        3 floats: specular, absorbed, escaped weight (mcsub)
+ *   Rd         photons_per_dispatch floats, per dispatch slot
+ *   Rd2D       Nx*Ny floats, DetPhot2D Nx*Ny ints, index ix*Ny + iy
+ *   Pol*, Phase*, PolVsScatt: outputs of the empty polarisation kernel;
+ *              left untouched.
+ * Any pointer may be NULL; arrays a kind does not produce are left untouched. */
+nmc_status nmc_get_compute_results(nmc_handle* h, float* J, float* F, float* F3D,
+                                   float* SAE, float* Rd, float* Rd2D,
+                                   int32_t* DetPhot2D, float* PolXX, float* PolXY,
+                                   float* PolYX, float* PolYY, float* Phase0,
+                                   float* Phase1, float* Phase2, float* Phase3,
+                                   float* PolVsScatt);
+
+/* Totals, sums and timing since nmc_prepare / nmc_reset. */
+nmc_status nmc_get_summary(nmc_handle* h, nmc_summary* out);
+
+/* Copies one FP64 tally (see nmc_tally for sizes and layouts) into `out`,
+ * which holds `n` doubles; n must equal the tally's size. */
+nmc_status nmc_get_tally_f64(nmc_handle* h, int32_t which, double* out, size_t n);
+
+/* Number of doubles in tally `which` for the prepared configuration. */
+size_t nmc_tally_size(nmc_handle* h, int32_t which);
+
+/* Clears all tallies and counters; keeps the prepared inputs. */
+nmc_status nmc_reset(nmc_handle* h);
+
+/* The cudaStream_t the handle launches on (for timing and overlap). */
+void* nmc_stream(nmc_handle* h);
+
+/* Text of the last error on this handle ("" if none). */
+const char* nmc_last_error(const nmc_handle* h);
+
+/* Frees the handle and its device memory. */
+void nmc_destroy(nmc_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NMC_ABI_H */

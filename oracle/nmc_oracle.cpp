@@ -1,0 +1,1000 @@
+// nmc_oracle.cpp - CPU oracle for the photon-transport engine.
+//
+// TEST INFRASTRUCTURE ONLY: called by tests/, __graft_entry__.smoke() and the
+// CPU baseline of bench.py, never by the product.
+//
+// A line-by-line restatement, in plain C++ templated on the arithmetic type
+// (double for the parity oracle, float to study FP32 rounding) and on the
+// random stream, of the reference's photon kernels:
+//   MCSubKernel    NMC/NMCCode/kernels.metal:59-319
+//   MCXYZKernel    NMC/NMCCode/kernels.metal:321-754
+//   MCXYZKernelTT  NMC/NMCCode/kernels.metal:757-1118
+// and of the helpers they call (NMC/NMCCode/helpers.metal): FltEq :21-25,
+// SameVoxel :27-39, FindVoxelFace2 :85-114, Fresnel::RFresnel :243-291,
+// Fresnel::Snell :293-314, RandomGen :319-371.  Constants are those of
+// NMC/NMCCode/definitions.h.  Per-photon order of random draws is the
+// reference's, so with the reference's own generator (NMC_RNG_TAUS_REF) a
+// photon follows the reference's trajectory, and with Philox it follows the
+// GPU engine's.
+//
+// Departures, each because the reference's behaviour is undefined there:
+//  * the two-term sampler takes the isotropic branch when g_f or g_b is 0
+//    (kernels.metal:1062,1066 divide by 2g);
+//  * the two-term Rd2D index is clamped to the grid (kernels.metal:984 uses
+//    unclamped indices);
+//  * every photon has a step cap (NMC_FATE_STEPCAP) so that no input can
+//    loop forever.
+#include "nmc_oracle.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------- constants
+constexpr double kPI = 3.1415926;               // definitions.h:60 PI
+constexpr double kLS = 10E-8;                   // definitions.h:59 ls
+constexpr double kTHRESHOLD = 0.0001;           // definitions.h:64
+constexpr double kCHANCE = 0.1;                 // definitions.h:65
+constexpr double kMIN_VALUE = 1E-6;             // definitions.h:66
+constexpr int kMAX_SCATT = 10000;               // definitions.h:19
+constexpr int kRAY_DEPTH = 100;                 // definitions.h:21
+constexpr double kCOS90D = 1.0E-6;              // definitions.h:70
+constexpr float kCOSZERO = 1.0F - 1.0E-6F;      // definitions.h:71
+constexpr double kONE_MINUS_COSZERO = 1.0E-12;  // definitions.h:72
+const double kRAD_DEG = 180.0F / kPI;           // definitions.h:77
+constexpr int kMCSUB_LAYER = 1;                 // FIRST_TISSUE_LAYER_MCSUB
+constexpr uint64_t kStepCap = 100000000ull;     // oracle-only safety cap
+constexpr uint32_t kPhiloxTag = 0x4E4D4321u;    // counter word 3
+
+// ------------------------------------------------------------------- RNGs
+void philox10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = lo1;
+    c[2] = n2;
+    c[3] = lo0;
+  }
+}
+
+// What a uniform is used for.  The reference draws sequentially from one
+// stream; the Philox layout below gives every use a fixed slot instead.
+enum Draw { D_LAUNCH, D_STEP, D_COS, D_PSI, D_ROUL, D_FRES, D_CHOICE, D_SAMPLE };
+
+// Philox layout of the GPU engine (same definition as in the CUDA
+// kernels): key = (seed lo, seed hi); counter = (photon lo, photon hi, c2,
+// 0x4E4D4321) with
+//   c2 = 0xFFFFFFFF          launch block, slots used in draw order;
+//   c2 = h                   main block of hop h (h = 0, 1, ...);
+//   c2 = h | 0x40000000      aux block of hop h, generated only when used.
+// Slots:   HG / isotropic     main = (step, cos, psi, roulette), aux = (fresnel)
+//          two-term           main = (step, choice, sample, psi),
+//                             aux  = (fresnel, roulette)
+// u = (2k+1) 2^-24 with k the top 23 bits of the word: 0 < u < 1, exact in
+// float and double, so the reference's `while (rnd <= 0)` loops never repeat.
+struct PhiloxStream {
+  uint32_t k0, k1, id_lo, id_hi;
+  bool tt;
+  uint32_t hop = 0xFFFFFFFFu, nlaunch = 0;
+  uint32_t mb[4], ab[4], lb[4];
+  bool m_ok = false, a_ok = false, l_ok = false;
+  PhiloxStream(uint64_t seed, uint64_t photon, bool two_term)
+      : k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), id_lo((uint32_t)photon),
+        id_hi((uint32_t)(photon >> 32)), tt(two_term) {}
+  void gen(uint32_t c2, uint32_t* out) {
+    uint32_t c[4] = {id_lo, id_hi, c2, kPhiloxTag};
+    philox10(c, k0, k1);
+    std::memcpy(out, c, sizeof c);
+  }
+  void new_hop() {
+    ++hop;
+    m_ok = a_ok = false;
+  }
+  uint32_t main_slot(int k) {
+    if (!m_ok) {
+      gen(hop, mb);
+      m_ok = true;
+    }
+    return mb[k];
+  }
+  uint32_t aux_slot(int k) {
+    if (!a_ok) {
+      gen(hop | 0x40000000u, ab);
+      a_ok = true;
+    }
+    return ab[k];
+  }
+  uint32_t word(Draw d) {
+    switch (d) {
+      case D_LAUNCH:
+        if (!l_ok) {
+          gen(0xFFFFFFFFu, lb);
+          l_ok = true;
+        }
+        return lb[(nlaunch++) & 3];
+      case D_STEP: return main_slot(0);
+      case D_COS: return main_slot(1);
+      case D_CHOICE: return main_slot(1);
+      case D_SAMPLE: return main_slot(2);
+      case D_PSI: return tt ? main_slot(3) : main_slot(2);
+      case D_ROUL: return tt ? aux_slot(1) : main_slot(3);
+      case D_FRES: return aux_slot(0);
+    }
+    return 0;
+  }
+  template <class R>
+  R u(Draw d) {
+    const uint32_t x = word(d);
+    return R(x >> 9) * R(1.0 / 8388608.0) + R(1.0 / 16777216.0);
+  }
+};
+
+// RandomGen, helpers.metal:319-371.
+struct TausStream {
+  uint32_t s1, s2, s3, s4;
+  static uint32_t taus(uint32_t z, int a, int b, int c, uint32_t m) {
+    const uint32_t bb = ((z << a) ^ z) >> b;
+    return ((z & m) << c) ^ bb;
+  }
+  static uint32_t xsh(uint32_t x) {
+    x ^= x << 13;
+    x ^= x >> 17;
+    x ^= x << 5;
+    return x;
+  }
+  TausStream(uint32_t a, uint32_t b, uint32_t c) {
+    a = xsh(a);
+    b = xsh(b);
+    c = xsh(c);
+    s1 = taus(a, 13, 19, 12, 429496729u);
+    s2 = taus(b, 2, 25, 4, 4294967288u);
+    s3 = taus(c, 3, 11, 17, 429496280u);
+    s4 = xsh(a + b + c) ^ 1013904223u;
+    s1 ^= s4;
+    s2 ^= s1;
+    s3 ^= s2;
+  }
+  float next_f() {
+    s1 = taus(s1, 13, 19, 12, 429496729u);
+    s2 = taus(s2, 2, 25, 4, 4294967288u);
+    s3 = taus(s3, 3, 11, 17, 429496280u);
+    s4 = xsh(s4);
+    const uint32_t r = s1 ^ s2 ^ s3 ^ s4;
+    return (float)(r >> 8) * (1.0f / 16777216.0f);
+  }
+  void new_hop() {}
+  template <class R>
+  R u(Draw) {
+    return R(next_f());
+  }
+};
+
+// Seeds of the reference's generator for photon (run, index):
+// kernels.metal:91-95 (mcsub) and :339-343 (mcxyz) use numRuns = run + 1;
+// :772 (two-term) uses (numRuns*index, numRuns*1234, index*1234).
+TausStream taus_for(int sim_type, uint64_t photon, uint64_t batch, bool tt_replay) {
+  const uint32_t run = (uint32_t)(photon / batch) + 1u;  // main.m:159 iRunNum
+  const uint32_t index = (uint32_t)(photon % batch);
+  if (sim_type == NMC_SIM_MCXYZ_TT) {
+    const uint32_t nr = (tt_replay ? 0u : run) + 1u;
+    return TausStream(nr * index, nr * 1234u, index * 1234u);
+  }
+  const uint32_t nr = run + 1u;
+  return TausStream((nr ^ (index * 2654435761u)) + 12345u,
+                    (nr * 1103515245u) ^ (index * 1013904223u),
+                    (index ^ nr) * 1664525u + 1013904223u);
+}
+
+// ----------------------------------------------------------------- helpers
+template <class R>
+bool flt_eq(R a, R b) {  // helpers.metal:21-25 with error = 1
+  const R e = b * R(FLT_EPSILON) * R(2);
+  return (a >= b - e) && (a <= b + e);
+}
+
+template <class R>
+R rfresnel(R n1, R n2, R ca1, R* ca2) {  // helpers.metal:243-291
+  R r = 0;
+  if (flt_eq(n1, n2)) {
+    *ca2 = ca1;
+    r = 0;
+  } else if (ca1 > R(kCOSZERO)) {
+    *ca2 = ca1;
+    r = (n2 - n1) / (n2 + n1);
+    r *= r;
+  } else if (ca1 < R(kCOS90D)) {
+    *ca2 = 0;
+    r = 1;
+  } else {
+    const R sa1 = std::sqrt(R(1) - ca1 * ca1);
+    const R sa2 = n1 * sa1 / n2;
+    if (sa2 >= R(1)) {
+      *ca2 = 0;
+      r = 1;
+    } else {
+      const R c2 = std::sqrt(R(1) - sa2 * sa2);
+      *ca2 = c2;
+      const R cap = ca1 * c2 - sa1 * sa2, cam = ca1 * c2 + sa1 * sa2;
+      const R sap = sa1 * c2 + ca1 * sa2, sam = sa1 * c2 - ca1 * sa2;
+      r = R(0.5) * sam * sam * (cam * cam + cap * cap) / (sap * sap * cam * cam);
+    }
+  }
+  return r;
+}
+
+template <class R>
+void snell(R n1, R n2, R* ux, R* uy, R* uz) {  // helpers.metal:293-314
+  const R x = *ux, y = *uy, z = *uz;
+  const R sc = R(1) - (R(1) - z * z) * n1 * n1 / n2 / n2;
+  if (sc < R(0)) {
+    if (std::fabs(z) > R(1)) *uz = z < R(0) ? R(-1) : R(1);
+    return;
+  }
+  *ux = x * n1 / n2;
+  *uy = y * n1 / n2;
+  *uz = std::sqrt(sc);
+}
+
+template <class R>
+bool same_voxel(R x1, R y1, R z1, R x2, R y2, R z2, R dx, R dy, R dz) {  // :27-39
+  const R xmin = std::min(std::floor(x1 / dx), std::floor(x2 / dx)) * dx;
+  const R ymin = std::min(std::floor(y1 / dy), std::floor(y2 / dy)) * dy;
+  const R zmin = std::min(std::floor(z1 / dz), std::floor(z2 / dz)) * dz;
+  const R xmax = xmin + dx, ymax = ymin + dy, zmax = zmin + dz;
+  return x1 <= xmax && x2 <= xmax && y1 <= ymax && y2 <= ymax && z1 < zmax && z2 <= zmax;
+}
+
+template <class R>
+R find_voxel_face2(R x1, R y1, R z1, R dx, R dy, R dz, R ux, R uy, R uz) {  // :85-114
+  const int ix1 = (int)std::floor(x1 / dx), iy1 = (int)std::floor(y1 / dy),
+            iz1 = (int)std::floor(z1 / dz);
+  const int ix2 = ux >= R(0) ? ix1 + 1 : ix1;
+  const int iy2 = uy >= R(0) ? iy1 + 1 : iy1;
+  const int iz2 = uz >= R(0) ? iz1 + 1 : iz1;
+  const R xs = std::fabs((R(ix2) * dx - x1) / ux);
+  const R ys = std::fabs((R(iy2) * dy - y1) / uy);
+  const R zs = std::fabs((R(iz2) * dz - z1) / uz);
+  return std::min(std::min(xs, ys), zs);
+}
+
+// Henyey-Greenstein sample (kernels.metal:244-251, :696-703).
+template <class R>
+R hg_costheta(R g, R rnd) {
+  if (flt_eq(g, R(0))) return R(2) * rnd - R(1);
+  if (flt_eq(g, R(1))) return R(1);
+  const R temp = (R(1) - g * g) / (R(1) - g + R(2) * g * rnd);
+  return (R(1) + g * g - temp * temp) / (R(2) * g);
+}
+
+// Two-term parameters q1 = 1+g^2, q2 = (1-g)^(2a), q3 = (1+g)^(2a)
+// (kernels.metal:900-905).
+template <class R>
+struct TTq {
+  R q1f, q2f, q3f, q1b, q2b, q3b;
+  void set(R gf, R af, R gb, R ab) {
+    q1f = R(1) + gf * gf;
+    q2f = std::pow(R(1) - gf, R(2) * af);
+    q3f = std::pow(R(1) + gf, R(2) * af);
+    q1b = R(1) + gb * gb;
+    q2b = std::pow(R(1) - gb, R(2) * ab);
+    q3b = std::pow(R(1) + gb, R(2) * ab);
+  }
+};
+
+// One two-term cos(theta) from two draws (kernels.metal:1058-1070).
+template <class R, class G>
+R tt_costheta(G& rng, const TTq<R>& q, R gf, R af, R gb, R ab, R cc) {
+  R rnd = rng.template u<R>(D_CHOICE);
+  R c;
+  if (rnd <= cc) {
+    rnd = rng.template u<R>(D_SAMPLE);
+    if (gf == R(0))
+      c = R(2) * rnd - R(1);
+    else
+      c = (q.q1f / (R(2) * gf)) -
+          std::pow(rnd / q.q2f + (R(1) - rnd) / q.q3f, -R(1) / af) / (R(2) * gf);
+  } else {
+    rnd = rng.template u<R>(D_SAMPLE);
+    if (gb == R(0))
+      c = R(2) * rnd - R(1);
+    else
+      c = (q.q1b / (R(2) * gb)) -
+          std::pow(rnd / q.q2b + (R(1) - rnd) / q.q3b, -R(1) / ab) / (R(2) * gb);
+    c *= R(-1);
+  }
+  if (c >= R(1)) c = R(1.0 - 1e-9);
+  if (c <= R(-1)) c = -R(1.0 - 1e-9);
+  return c;
+}
+
+// psi sample and the new direction (kernels.metal:255-279, :706-730).
+template <class R, class G>
+void spin(G& rng, R costheta, R& ux, R& uy, R& uz) {
+  const R sintheta = std::sqrt(R(1) - costheta * costheta);
+  const R psi = R(2.0 * kPI) * rng.template u<R>(D_PSI);
+  const R cospsi = std::cos(psi);
+  const R sinpsi = psi < R(kPI) ? std::sqrt(R(1) - cospsi * cospsi)
+                                : -std::sqrt(R(1) - cospsi * cospsi);
+  R uxx, uyy, uzz;
+  if (R(1) - std::fabs(uz) <= R(kONE_MINUS_COSZERO)) {
+    uxx = sintheta * cospsi;
+    uyy = sintheta * sinpsi;
+    uzz = costheta * (uz >= R(0) ? R(1) : R(-1));
+  } else {
+    const R temp = std::sqrt(R(1) - uz * uz);
+    uxx = sintheta * (ux * uz * cospsi - uy * sinpsi) / temp + ux * costheta;
+    uyy = sintheta * (uy * uz * cospsi + ux * sinpsi) / temp + uy * costheta;
+    uzz = -sintheta * cospsi * temp + uz * costheta;
+  }
+  ux = uxx;
+  uy = uyy;
+  uz = uzz;
+}
+
+// Replays a fixed list of uniforms (used by the sampler entry points).
+struct FixedDraws {
+  double v[2];
+  int k = 0;
+  template <class R>
+  R u(Draw) {
+    return R(v[k++]);
+  }
+};
+
+// ------------------------------------------------------------ run context
+struct Cfg {
+  int sim;
+  nmc_run_params rp;
+  nmc_tissue_params tp;
+  const uint8_t* v;
+  nmc_ext ext;
+};
+
+struct Tally {
+  std::vector<double> J, F, F3D, Rd2D, Det, slots;
+  double S = 0, A = 0, E = 0, rd = 0, rd2 = 0, ph = 0, sub = 0, sc = 0;
+};
+
+struct Trace {
+  nmc_photon_record* rec;
+  float* ev;
+  uint32_t k;
+  uint32_t nev = 0;
+  void event(double x, double y, double z, double w) {
+    if (!ev || nev >= k) return;
+    float* e = ev + 4 * (size_t)nev;
+    e[0] = (float)x;
+    e[1] = (float)y;
+    e[2] = (float)z;
+    e[3] = (float)w;
+    ++nev;
+  }
+};
+
+// ---------------------------------------------------------------- MCSub
+template <class R, class G>
+void mcsub_photon(const Cfg& c, G& rng, Tally& T, Trace& tr) {
+  const nmc_ext& e = c.ext;
+  const R mua = c.tp.muav[kMCSUB_LAYER], mus = c.tp.musv[kMCSUB_LAYER];
+  const R g = c.tp.gv[kMCSUB_LAYER];
+  const R n1 = c.rp.n1, n2 = c.rp.n2;
+  const int BINS = e.sub_bins;
+  const R dr = e.sub_dr, dz = e.sub_dz, zs = e.sub_zs;
+  TTq<R> q;
+  const R gf = c.tp.gf[kMCSUB_LAYER], af = c.tp.af[kMCSUB_LAYER];
+  const R gb = c.tp.gb[kMCSUB_LAYER], ab = c.tp.ab[kMCSUB_LAYER];
+  const R cc = c.tp.CC[kMCSUB_LAYER];
+  if (e.phase == NMC_PHASE_TWO_TERM) q.set(gf, af, gb, ab);
+
+  R px = 0, py = 0, pz = 0, ux = 0, uy = 0, uz = 0;
+  const R mut = mua + mus, albedo = mus / mut;  // :100-101
+  R Rsptot = 0, Atot = 0, rsp = 0, E = 0, W = 0, rnd, temp;
+  uint32_t nsub = 0, nsc = 0, fate = NMC_FATE_ALIVE, ndet = 0;
+
+  if (e.sub_mcflag == 0) {  // :106-121
+    rnd = rng.template u<R>(D_LAUNCH);
+    px = R(e.sub_radius) * std::sqrt(rnd);
+    py = 0;
+    pz = zs;
+    ux = 0;
+    uy = 0;
+    uz = 1;
+    temp = n1 / n2;
+    temp = (R(1) - temp) / (R(1) + temp);
+    rsp = temp * temp;
+  } else if (e.sub_mcflag == 1) {  // :122-147
+    while ((rnd = rng.template u<R>(D_LAUNCH)) <= R(0)) {
+    }
+    px = R(e.sub_radius) * std::sqrt(-std::log(rnd));
+    py = 0;
+    pz = zs;
+    while ((rnd = rng.template u<R>(D_LAUNCH)) <= R(0)) {
+    }
+    const R xfocus = R(e.sub_waist) * std::sqrt(-std::log(rnd));
+    const R zf = e.sub_zfocus;
+    temp = std::sqrt((px - xfocus) * (px - xfocus) + zf * zf);
+    const R sintheta = -(px - xfocus) / temp, costheta = zf / temp;
+    ux = sintheta;
+    uy = 0;
+    uz = costheta;
+    R uzn = uz;
+    rsp = rfresnel(n2, n1, costheta, &uzn);
+    uz = uzn;
+    ux = std::sqrt(R(1) - uz * uz);
+  } else if (e.sub_mcflag == 2) {  // :148-164
+    px = e.sub_xs;
+    py = e.sub_ys;
+    pz = zs;
+    const R costheta = R(1) - R(2) * rng.template u<R>(D_LAUNCH);
+    const R sintheta = std::sqrt(R(1) - costheta * costheta);
+    const R psi = R(2.0 * kPI) * rng.template u<R>(D_LAUNCH);
+    const R cospsi = std::cos(psi);
+    const R sinpsi = psi < R(kPI) ? std::sqrt(R(1) - cospsi * cospsi)
+                                  : -std::sqrt(R(1) - cospsi * cospsi);
+    ux = sintheta * cospsi;
+    uy = sintheta * sinpsi;
+    uz = costheta;
+    rsp = 0;
+  }
+  W = R(1) - rsp;  // :166-168
+  Rsptot += rsp;
+  bool alive = true;
+
+  do {  // :176-305
+    rng.new_hop();
+    while ((rnd = rng.template u<R>(D_STEP)) <= R(0)) {
+    }
+    R s = -std::log(rnd) / mut;
+    px += s * ux;
+    py += s * uy;
+    pz += s * uz;
+    ++nsub;
+    if (e.sub_boundaryflag == 1 && pz <= zs) {  // :190-214
+      rnd = rng.template u<R>(D_FRES);
+      R uz1;
+      if (rnd > rfresnel(n1, n2, -uz, &uz1)) {
+        px -= s * ux;
+        py -= s * uy;
+        pz -= s * uz;
+        s = std::fabs(pz / uz);
+        px += s * ux;
+        py += s * uy;
+        const R r = std::sqrt(px * px + py * py);
+        long ir = (long)(r / dr) + 1;
+        if (ir > BINS) ir = BINS;
+        if (!T.J.empty()) T.J[ir] += (double)W;
+        E += W;
+        ndet = 1;
+        alive = false;
+        fate = NMC_FATE_ESCAPED;
+      } else {
+        pz = -pz;
+        uz = -uz;
+      }
+    }
+    if (alive) {
+      const R absorb = W * (R(1) - albedo);  // :224-234
+      W -= absorb;
+      Atot += absorb;
+      const R r = std::sqrt(px * px + py * py);
+      long ir = (long)(r / dr) + 1;
+      long iz = (long)(std::fabs(pz) / dz) + 1;
+      if (ir >= BINS) ir = BINS;
+      if (iz >= BINS) iz = BINS;
+      if (!T.F.empty()) T.F[ir * BINS + iz] += (double)absorb;
+
+      R costheta;  // :243-252
+      if (e.phase == NMC_PHASE_TWO_TERM) {
+        costheta = tt_costheta(rng, q, gf, af, gb, ab, cc);
+      } else {
+        rnd = rng.template u<R>(D_COS);
+        costheta = hg_costheta(g, rnd);
+        if (e.phase == NMC_PHASE_ISOTROPIC_REF) costheta = R(2) * rnd - R(1);
+      }
+      spin(rng, costheta, ux, uy, uz);
+      ++nsc;
+      if (W < R(kTHRESHOLD)) {  // :289-294
+        rnd = rng.template u<R>(D_ROUL);
+        if (rnd <= R(kCHANCE))
+          W /= R(kCHANCE);
+        else {
+          alive = false;
+          fate = NMC_FATE_ROULETTE;
+        }
+      }
+      tr.event(px, py, pz, W);
+    }
+    if (alive && nsub >= kStepCap) {
+      alive = false;
+      fate = NMC_FATE_STEPCAP;
+    }
+  } while (alive);
+
+  T.S += (double)Rsptot;
+  T.A += (double)Atot;
+  T.E += (double)E;
+  T.rd += (double)E;
+  T.rd2 += (double)E * (double)E;
+  T.sub += nsub;
+  T.sc += nsc;
+  if (tr.rec) {
+    nmc_photon_record& o = *tr.rec;
+    o.n_scatt = nsc;
+    o.n_sub = nsub;
+    o.fate = fate;
+    o.n_detect = ndet;
+    o.w_final = (float)W;
+    o.absorbed = (float)Atot;
+    o.detected = (float)E;
+    o.x = (float)px;
+    o.y = (float)py;
+    o.z = (float)pz;
+  }
+}
+
+// -------------------------------------------------------------- MCXYZ(TT)
+template <class R>
+struct Voxel {
+  int Nx, Ny, Nz;
+  R dx, dy, dz;
+};
+
+// launch (kernels.metal:366-463; the two-term kernel :796-870 lacks mcflag 1)
+template <class R, class G>
+void xyz_launch(const nmc_run_params& rp, bool tt, G& rng, R& x, R& y, R& z, R& ux, R& uy,
+                R& uz, R& W) {
+  R rnd;
+  x = y = z = ux = uy = uz = 0;  // tagPhoton() zero initialisation, :30-39
+  if (rp.launchflag == 1) {
+    x = rp.xs;
+    y = rp.ys;
+    z = rp.zs;
+    ux = rp.ux0;
+    uy = rp.uy0;
+    uz = rp.uz0;
+    return;
+  }
+  if (rp.mcflag == 0 || (rp.mcflag == 1 && !tt)) {
+    const bool gauss = rp.mcflag == 1;
+    while ((rnd = rng.template u<R>(D_LAUNCH)) <= R(0)) {
+    }
+    R r = gauss ? R(rp.radius) * std::sqrt(-std::log(rnd)) : R(rp.radius) * std::sqrt(rnd);
+    while ((rnd = rng.template u<R>(D_LAUNCH)) <= R(0)) {
+    }
+    R phi = rnd * R(2.0) * R(kPI);
+    x = R(rp.xs) + r * std::cos(phi);
+    y = R(rp.ys) + r * std::sin(phi);
+    z = rp.zs;
+    while ((rnd = rng.template u<R>(D_LAUNCH)) <= R(0)) {
+    }
+    r = R(rp.waist) * std::sqrt(rnd);
+    while ((rnd = rng.template u<R>(D_LAUNCH)) <= R(0)) {
+    }
+    phi = rnd * R(2.0) * R(kPI);
+    const R xfocus = r * std::cos(phi), yfocus = r * std::sin(phi);
+    const R zf = rp.zfocus;
+    const R temp = std::sqrt((x - xfocus) * (x - xfocus) + (y - yfocus) * (y - yfocus) + zf * zf);
+    ux = -(x - xfocus) / temp;
+    uy = -(y - yfocus) / temp;
+    uz = std::sqrt(R(1) - ux * ux - uy * uy);
+    if (gauss) {  // :423-427
+      R uz_new = uz;
+      const R int_rsp = rfresnel(R(rp.n2), R(rp.n1), std::fabs(uz), &uz_new);
+      W = W * (R(1) - int_rsp);
+      snell(R(rp.n2), R(rp.n1), &ux, &uy, &uz);
+    }
+  } else if (rp.mcflag == 2) {
+    const R costheta = R(1) - R(2) * rng.template u<R>(D_LAUNCH);
+    const R sintheta = std::sqrt(R(1) - costheta * costheta);
+    const R psi = R(2.0 * kPI) * rng.template u<R>(D_LAUNCH);
+    const R cospsi = std::cos(psi);
+    const R sinpsi = psi < R(kPI) ? std::sqrt(R(1) - cospsi * cospsi)
+                                  : -std::sqrt(R(1) - cospsi * cospsi);
+    x = rp.xs;
+    y = rp.ys;
+    z = rp.zs;
+    ux = sintheta * cospsi;
+    uy = sintheta * sinpsi;
+    uz = costheta;
+  } else if (rp.mcflag == 3) {
+    while ((rnd = rng.template u<R>(D_LAUNCH)) <= R(0)) {
+    }
+    x = R(rp.radius) * (rnd * R(2.0) - R(1.0));
+    while ((rnd = rng.template u<R>(D_LAUNCH)) <= R(0)) {
+    }
+    y = R(rp.radius) * (rnd * R(2.0) - R(1.0));
+    z = rp.zs;
+    ux = 0;
+    uy = 0;
+    uz = 1;
+  } else if (rp.mcflag == 4) {
+    x = 0;
+    y = 0;
+    z = rp.zs;
+    ux = 0;
+    uy = 0;
+    uz = 1;
+  }
+}
+
+template <class R, class G>
+void mcxyz_photon(const Cfg& c, bool tt, G& rng, Tally& T, Trace& tr, uint64_t slot) {
+  const nmc_run_params& rp = c.rp;
+  const nmc_tissue_params& tp = c.tp;
+  const int Nx = rp.Nx, Ny = rp.Ny, Nz = rp.Nz;
+  const R dx = rp.dx, dy = rp.dy, dz = rp.dz, zsurf = rp.zsurf;
+  const bool hard_kill = !(c.ext.flags & NMC_FLAG_NO_HARD_KILL);
+  R x, y, z, ux, uy, uz, W = 1;
+  xyz_launch(rp, tt, rng, x, y, z, ux, uy, uz, W);
+  // launch voxel (kernels.metal:472-487): integer Nx/2 here, Nx/2.0 later
+  int ix = (int)(Nx / 2 + x / dx);
+  int iy = (int)(Ny / 2 + y / dy);
+  int iz = (int)(z / dz);
+  if (ix >= Nx) ix = Nx - 1;
+  if (iy >= Ny) iy = Ny - 1;
+  if (iz >= Nz) iz = Nz - 1;
+  if (ix < 0) ix = 0;
+  if (iy < 0) iy = 0;
+  if (iz < 0) iz = 0;
+  long i = (long)iz * Ny * Nx + (long)ix * Ny + iy;
+  int tiss = c.v[i];
+  R mua = tp.muav[tiss], mus = tp.musv[tiss], g = tp.gv[tiss];
+  TTq<R> q;
+  if (tt) q.set(R(tp.gf[tiss]), R(tp.af[tiss]), R(tp.gb[tiss]), R(tp.ab[tiss]));
+  int bflag = 1, surfflag = 1;
+  bool alive = true;
+  R Rd_loc = 0, Atot = 0, rnd;
+  uint32_t nsub = 0, nsc = 0, fate = NMC_FATE_ALIVE, ndet = 0;
+  auto kill = [&](uint32_t why) {
+    if (alive) fate = why;
+    alive = false;
+  };
+
+  do {  // :493-750
+    rng.new_hop();
+    while ((rnd = rng.template u<R>(D_STEP)) <= R(0)) {
+    }
+    R sleft = -std::log(rnd);
+    int depth = 0;
+    do {  // :505-685
+      R s = sleft / mus;
+      const R tx = x + s * ux, ty = y + s * uy, tz = z + s * uz;
+      ++nsub;
+      if (same_voxel(x, y, z, tx, ty, tz, dx, dy, dz)) {
+        x = tx;
+        y = ty;
+        z = tz;
+        const R absorb = W * (R(1) - std::exp(-mua * s));
+        W -= absorb;
+        Atot += absorb;
+        if (bflag && !T.F3D.empty()) T.F3D[i] += (double)absorb;
+        sleft = 0;
+      } else {
+        s = R(kLS) + find_voxel_face2(x, y, z, dx, dy, dz, ux, uy, uz);
+        const R absorb = W * (R(1) - std::exp(-mua * s));
+        W -= absorb;
+        Atot += absorb;
+        if (bflag && !T.F3D.empty()) T.F3D[i] += (double)absorb;
+        sleft -= s * mus;
+        if (sleft <= R(kLS)) sleft = 0;
+        if (!tt) {
+          // surface detection (kernels.metal:560-637)
+          const R z_new = z + s * uz;
+          bool cross = false;
+          if (rp.det_state == NMC_DET_REFLECTANCE && z_new <= zsurf && uz < R(0))
+            cross = true;
+          else if (rp.det_state == NMC_DET_TRANSMITTANCE && z_new >= zsurf && uz > R(0))
+            cross = true;
+          if (cross) {
+            const R dl_b = (zsurf - z) / uz;
+            sleft = (s - dl_b) * mus;
+            if (sleft <= R(kLS)) sleft = 0;
+            s = dl_b;
+            x += s * ux;
+            y += s * uy;
+            z += s * uz;
+            R uz_temp = 0;
+            const R rsp = rfresnel(R(rp.n1), R(rp.n2), std::fabs(uz), &uz_temp);
+            if (rsp < R(1)) {
+              R th_exit = 0;
+              if (!flt_eq(uz_temp, R(1))) th_exit = R(kRAD_DEG) * std::acos(uz_temp);
+              const R ro = std::sqrt(x * x + y * y);
+              R r_min, r_max;
+              if (flt_eq(R(rp.xd), R(0))) {
+                r_min = 0;
+                r_max = rp.det_radius;
+              } else {
+                r_min = R(rp.xd) - R(rp.det_radius);
+                r_max = r_min + R(2) * R(rp.det_radius);
+              }
+              if (ro >= r_min && ro <= r_max && th_exit <= R(rp.na)) {
+                int jx = (int)(Nx / 2.0 + x / dx), jy = (int)(Ny / 2.0 + y / dy);
+                if (jx >= Nx) jx = Nx - 1;
+                if (jy >= Ny) jy = Ny - 1;
+                if (jx < 0) jx = 0;
+                if (jy < 0) jy = 0;
+                const R dw = W * (R(1) - rsp);
+                Rd_loc += dw;
+                const long i2d = (long)jx * Ny + jy;
+                if (!T.Rd2D.empty()) T.Rd2D[i2d] += (double)dw;
+                if (!T.Det.empty()) T.Det[i2d] += 1.0;
+                ++ndet;
+                uz = -uz;
+                W = W * rsp;
+              }
+            } else {
+              uz = -uz;
+              W = W * rsp;
+            }
+          } else {
+            x += s * ux;
+            y += s * uy;
+            z += s * uz;
+          }
+          ix = (int)(Nx / 2.0 + x / dx);
+          iy = (int)(Ny / 2.0 + y / dy);
+          iz = (int)(z / dz);
+        } else {
+          // two-term kernel: move, first crossing above zsurf counts as Rd
+          // (kernels.metal:972-993)
+          x += s * ux;
+          y += s * uy;
+          z += s * uz;
+          ix = (int)(Nx / 2.0 + x / dx);
+          iy = (int)(Ny / 2.0 + y / dy);
+          iz = (int)(z / dz);
+          if (z < zsurf && surfflag == 1) {
+            surfflag = 0;
+            Rd_loc += W;
+            ++ndet;
+            const int jx = std::min(std::max(ix, 0), Nx - 1);
+            const int jy = std::min(std::max(iy, 0), Ny - 1);
+            if (!T.Rd2D.empty()) T.Rd2D[(long)jx * Ny + jy] += (double)W;
+          }
+          if (z < R(0)) {
+            kill(NMC_FATE_BOUNDARY);
+            sleft = 0;
+          }
+          bflag = 1;
+        }
+        if (rp.boundaryflag == 0) {  // :646-672
+          if (iz >= Nz) { iz = Nz - 1; bflag = 0; }
+          if (ix >= Nx) { ix = Nx - 1; bflag = 0; }
+          if (iy >= Ny) { iy = Ny - 1; bflag = 0; }
+          if (iz < 0) { iz = 0; bflag = 0; }
+          if (ix < 0) { ix = 0; bflag = 0; }
+          if (iy < 0) { iy = 0; bflag = 0; }
+        } else if (rp.boundaryflag == 1) {
+          if (iz >= Nz) { iz = Nz - 1; kill(NMC_FATE_BOUNDARY); sleft = 0; }
+          if (ix >= Nx) { ix = Nx - 1; kill(NMC_FATE_BOUNDARY); sleft = 0; }
+          if (iy >= Ny) { iy = Ny - 1; kill(NMC_FATE_BOUNDARY); sleft = 0; }
+          if (iz < 0) { iz = 0; kill(NMC_FATE_BOUNDARY); sleft = 0; }
+          if (ix < 0) { ix = 0; kill(NMC_FATE_BOUNDARY); sleft = 0; }
+          if (iy < 0) { iy = 0; kill(NMC_FATE_BOUNDARY); sleft = 0; }
+        } else if (rp.boundaryflag == 2) {
+          if (iz >= Nz) { iz = Nz - 1; bflag = 0; }
+          if (ix >= Nx) { ix = Nx - 1; bflag = 0; }
+          if (iy >= Ny) { iy = Ny - 1; bflag = 0; }
+          if (iz < 0) { iz = 0; kill(NMC_FATE_BOUNDARY); sleft = 0; }
+          if (ix < 0) { ix = 0; bflag = 0; }
+          if (iy < 0) { iy = 0; bflag = 0; }
+        }
+        i = (long)iz * Ny * Nx + (long)ix * Ny + iy;  // :675-679
+        tiss = c.v[i];
+        mua = tp.muav[tiss];
+        mus = tp.musv[tiss];
+        g = tp.gv[tiss];
+        if (tt) q.set(R(tp.gf[tiss]), R(tp.af[tiss]), R(tp.gb[tiss]), R(tp.ab[tiss]));
+      }
+      ++depth;
+      if (nsub >= kStepCap) {
+        kill(NMC_FATE_STEPCAP);
+        break;
+      }
+    } while (depth <= kRAY_DEPTH && sleft > R(0));
+    if (fate == NMC_FATE_STEPCAP) break;
+
+    R costheta;  // SPIN, :695-731 / :1053-1071
+    if (tt) {
+      costheta = tt_costheta(rng, q, R(tp.gf[tiss]), R(tp.af[tiss]), R(tp.gb[tiss]),
+                             R(tp.ab[tiss]), R(tp.CC[tiss]));
+    } else {
+      rnd = rng.template u<R>(D_COS);
+      costheta = hg_costheta(g, rnd);
+    }
+    spin(rng, costheta, ux, uy, uz);
+    ++nsc;
+    if (W < R(kTHRESHOLD)) {  // :740-744
+      if (rng.template u<R>(D_ROUL) <= R(kCHANCE))
+        W /= R(kCHANCE);
+      else
+        kill(NMC_FATE_ROULETTE);
+    }
+    if (hard_kill && (W < R(kMIN_VALUE) || (int)nsc > kMAX_SCATT))  // :747-748
+      kill(W < R(kMIN_VALUE) ? NMC_FATE_MINWEIGHT : NMC_FATE_MAXSCATT);
+    tr.event(x, y, z, W);
+  } while (alive);
+
+  if (!T.slots.empty()) T.slots[slot] += (double)Rd_loc;  // :753
+  T.A += (double)Atot;
+  T.rd += (double)Rd_loc;
+  T.rd2 += (double)Rd_loc * (double)Rd_loc;
+  T.sub += nsub;
+  T.sc += nsc;
+  if (tr.rec) {
+    nmc_photon_record& o = *tr.rec;
+    o.n_scatt = nsc;
+    o.n_sub = nsub;
+    o.fate = fate;
+    o.n_detect = ndet;
+    o.w_final = (float)W;
+    o.absorbed = (float)Atot;
+    o.detected = (float)Rd_loc;
+    o.x = (float)x;
+    o.y = (float)y;
+    o.z = (float)z;
+  }
+}
+
+template <class R, class G>
+void run_photon(const Cfg& c, G& rng, Tally& T, Trace& tr, uint64_t photon) {
+  if (c.sim == NMC_SIM_MCSUB)
+    mcsub_photon<R>(c, rng, T, tr);
+  else
+    mcxyz_photon<R>(c, c.sim == NMC_SIM_MCXYZ_TT, rng, T, tr,
+                    photon % c.ext.photons_per_dispatch);
+}
+
+bool two_term_family(const Cfg& c) {
+  return c.sim == NMC_SIM_MCXYZ_TT || (c.sim == NMC_SIM_MCSUB && c.ext.phase == NMC_PHASE_TWO_TERM);
+}
+
+template <class R>
+void run_range(const Cfg& c, uint64_t first, uint64_t lo, uint64_t hi, Tally& T,
+               nmc_photon_record* recs, float* events, uint32_t k) {
+  const bool replay = (c.ext.flags & NMC_FLAG_TT_REPLAY_RUN1) != 0;
+  for (uint64_t j = lo; j < hi; ++j) {
+    const uint64_t p = first + j;
+    Trace tr{recs ? recs + j : nullptr, events ? events + (size_t)j * k * 4 : nullptr, k};
+    if (tr.ev)
+      for (size_t m = 0; m < (size_t)k * 4; ++m) tr.ev[m] = NAN;
+    if (c.ext.rng == NMC_RNG_TAUS_REF) {
+      TausStream g = taus_for(c.sim, p, c.ext.photons_per_dispatch, replay);
+      run_photon<R>(c, g, T, tr, p);
+    } else {
+      PhiloxStream g(c.ext.seed, p, two_term_family(c));
+      run_photon<R>(c, g, T, tr, p);
+    }
+    T.ph += 1;
+  }
+}
+
+bool valid_inputs(const Cfg& c) {
+  if (c.sim == NMC_SIM_MCSUB) {
+    const int b = c.ext.sub_bins;
+    return b >= 2 && c.ext.sub_dr > 0 && c.ext.sub_dz > 0 &&
+           c.tp.muav[kMCSUB_LAYER] + c.tp.musv[kMCSUB_LAYER] > 0;
+  }
+  if (c.sim != NMC_SIM_MCXYZ && c.sim != NMC_SIM_MCXYZ_TT) return false;
+  const nmc_run_params& rp = c.rp;
+  if (!c.v || rp.Nx <= 0 || rp.Ny <= 0 || rp.Nz <= 0 || !(rp.dx > 0) || !(rp.dy > 0) ||
+      !(rp.dz > 0))
+    return false;
+  const long n = (long)rp.Nx * rp.Ny * rp.Nz;
+  for (long k = 0; k < n; ++k)
+    if (c.v[k] >= NMC_NTISS || !(c.tp.musv[c.v[k]] > 0)) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_run(int sim_type, int real_bits, const nmc_run_params* rp, const nmc_tissue_params* tp,
+            const uint8_t* v, const nmc_ext* ext, uint64_t first, uint64_t n, int nthreads,
+            orc_out* out, nmc_photon_record* recs, float* events, uint32_t k_events) {
+  if (!rp || !tp || !ext || !out || (real_bits != 32 && real_bits != 64)) return NMC_EINVAL;
+  Cfg c;
+  c.sim = sim_type;
+  c.rp = *rp;
+  c.tp = *tp;
+  c.v = v;
+  c.ext = *ext;
+  if (c.ext.photons_per_dispatch == 0) return NMC_EINVAL;
+  if (!valid_inputs(c)) return NMC_EINVAL;
+  if (nthreads < 1) nthreads = 1;
+  if ((uint64_t)nthreads > n) nthreads = n ? (int)n : 1;
+  const size_t nJ = (size_t)c.ext.sub_bins + 1, nF = nJ * nJ;
+  const size_t nvox = (size_t)rp->Nx * rp->Ny * rp->Nz, n2d = (size_t)rp->Nx * rp->Ny;
+  const bool xyz = sim_type != NMC_SIM_MCSUB;
+  std::vector<Tally> T(nthreads);
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; ++t) {
+    const uint64_t lo = n * t / nthreads, hi = n * (t + 1) / nthreads;
+    th.emplace_back([&, t, lo, hi] {
+      Tally& tl = T[t];
+      if (!xyz) {
+        if (out->J) tl.J.assign(nJ, 0.0);
+        if (out->F) tl.F.assign(nF, 0.0);
+      } else {
+        if (out->F3D) tl.F3D.assign(nvox, 0.0);
+        if (out->Rd2D) tl.Rd2D.assign(n2d, 0.0);
+        if (out->DetPhot2D) tl.Det.assign(n2d, 0.0);
+        if (out->rd_slots) tl.slots.assign(c.ext.photons_per_dispatch, 0.0);
+      }
+      if (real_bits == 64)
+        run_range<double>(c, first, lo, hi, tl, recs, events, k_events);
+      else
+        run_range<float>(c, first, lo, hi, tl, recs, events, k_events);
+    });
+  }
+  for (auto& x : th) x.join();
+  for (int t = 0; t < nthreads; ++t) {
+    const Tally& tl = T[t];
+    for (size_t k = 0; k < tl.J.size(); ++k) out->J[k] += tl.J[k];
+    for (size_t k = 0; k < tl.F.size(); ++k) out->F[k] += tl.F[k];
+    for (size_t k = 0; k < tl.F3D.size(); ++k) out->F3D[k] += tl.F3D[k];
+    for (size_t k = 0; k < tl.Rd2D.size(); ++k) out->Rd2D[k] += tl.Rd2D[k];
+    for (size_t k = 0; k < tl.Det.size(); ++k) out->DetPhot2D[k] += tl.Det[k];
+    for (size_t k = 0; k < tl.slots.size(); ++k) out->rd_slots[k] += tl.slots[k];
+    out->S += tl.S;
+    out->A += tl.A;
+    out->E += tl.E;
+    out->rd_sum += tl.rd;
+    out->rd_sumsq += tl.rd2;
+    out->photons += tl.ph;
+    out->substeps += tl.sub;
+    out->scatters += tl.sc;
+  }
+  return 0;
+}
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+  philox10(c, key[0], key[1]);
+  for (int k = 0; k < 4; ++k) out[k] = c[k];
+}
+
+void orc_uniforms(const nmc_ext* ext, int sim_type, uint64_t photon_id, int n, double* out) {
+  if (ext->rng == NMC_RNG_TAUS_REF) {
+    TausStream g = taus_for(sim_type, photon_id, ext->photons_per_dispatch,
+                            (ext->flags & NMC_FLAG_TT_REPLAY_RUN1) != 0);
+    for (int k = 0; k < n; ++k) out[k] = g.u<double>(D_STEP);
+  } else {
+    // Philox: the n uniforms are hop 0's main block, then hop 1's, ...
+    PhiloxStream g(ext->seed, photon_id, false);
+    for (int k = 0; k < n; ++k) {
+      if (k % 4 == 0) g.new_hop();
+      out[k] = g.u<double>((Draw)(k % 4 == 0 ? D_STEP : k % 4 == 1 ? D_COS : k % 4 == 2 ? D_PSI : D_ROUL));
+    }
+  }
+}
+
+double orc_rfresnel(double n1, double n2, double ca1, double* ca2) {
+  return rfresnel<double>(n1, n2, ca1, ca2);
+}
+
+double orc_tt_costheta(double gf, double af, double gb, double ab, double cc, double u_choice,
+                       double u_sample) {
+  FixedDraws g{{u_choice, u_sample}};
+  TTq<double> q;
+  q.set(gf, af, gb, ab);
+  return tt_costheta<double>(g, q, gf, af, gb, ab, cc);
+}
+
+double orc_hg_costheta(double g, double u) { return hg_costheta<double>(g, u); }
+
+}  // extern "C"
