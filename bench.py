@@ -1,0 +1,283 @@
+"""Benchmark: photons/s of the voxel photon-transport path on the 200^3
+skin-vessel workload (mcxyz kernel, 1e8 photons per step).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one pass of the transport over the workload's photon budget
+(1e8 photons per GPU) with inputs resident in HBM.  Prints one JSON line.
+
+  value     photons/s over all ranks, device time (CUDA events) of K steps
+  e2e       photons/s through the C ABI with host buffers: nmc_prepare (H2D of
+            the tissue map), nmc_run, nmc_get_compute_results (D2H of F3D,
+            Rd slots, Rd2D, DetPhot2D) inside the timed region
+  roofline  the transport kernel against the measured FP32-issue ceiling
+  cpu_baseline  the reference algorithm restated on the host cores (FP32,
+            the reference's own generator), a bounded sample of the workload
+
+--impl reference times that CPU restatement alone on the same workload (the
+reference runs only on Apple Metal; its kernels cannot execute on this machine).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+METRIC = "photons/s at 1% Rd std-err, batched+adjoint vs plain kernel, 1×GB300"
+PHOTONS_PER_STEP = 100_000_000
+WORKLOAD = "mcxyz skin-vessel 200^3 @0.005 cm, 1e8 photons per GPU per step"
+
+# Algorithmic work of one voxel sub-step (the kernel's loop trip), counted
+# from the source of the transport loop: FP32/INT lane operations issued on
+# the FMA/ALU pipes for the sub-step proper (position update, same-voxel
+# test, face distances, absorption, voxel index and tissue lookup) and the
+# per-hop SPIN/roulette share.  Fixed once; see the design doc.
+OPS_PER_SUBSTEP = 64.0
+MUFU_PER_SUBSTEP = 3.0
+
+
+def _clock_sampler(stop: threading.Event, out: list, dev: int):
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    try:
+        p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                              "-i", str(dev), "-lms", "200"], stdout=subprocess.PIPE, text=True)
+    except Exception:
+        return
+    try:
+        while not stop.is_set():
+            line = p.stdout.readline()
+            if not line:
+                break
+            out.append(line.strip())
+    finally:
+        p.terminate()
+
+
+def _clocks_summary(lines: list) -> dict:
+    import statistics
+
+    sm, mx, reasons = [], 0.0, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for ln in lines:
+        f = [x.strip() for x in ln.split(",")]
+        if len(f) < 9:
+            continue
+        try:
+            sm.append(float(f[1]))
+            mx = max(mx, float(f[2]))
+        except ValueError:
+            continue
+        for n, v in zip(names, f[5:9]):
+            if v.lower() == "active":
+                reasons.add(n)
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+            "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(seconds: float = 12.0, threads: int | None = None) -> dict:
+    """The reference algorithm on the host cores: the oracle's FP32 restatement
+    with the reference's Tausworthe generator (which reproduces the
+    reference's FP32 voxel walk), on a bounded sample of the workload."""
+    import nmc_cases as cases
+    from nmc_gb300 import abi
+    from oracle import bindings
+
+    bindings.build(ref=False)
+    threads = threads or os.cpu_count() or 1
+    rp, tp, v, ext = cases.skin_vessel_case(N=200, rng=abi.RNG_TAUS_REF)
+    n = 64 * threads
+    t0 = time.perf_counter()
+    r = bindings.run(abi.SIM_MCXYZ, rp, tp, v, ext=ext, n=n, nthreads=threads, real_bits=32, tallies=False)
+    dt = time.perf_counter() - t0
+    n2 = max(threads, int(n * max(seconds - dt, 1.0) / max(dt, 1e-3)))
+    t0 = time.perf_counter()
+    r2 = bindings.run(abi.SIM_MCXYZ, rp, tp, v, ext=ext, first=n, n=n2, nthreads=threads, real_bits=32,
+                      tallies=False)
+    dt2 = time.perf_counter() - t0
+    return {"photons": n2, "seconds": dt2, "photons_per_s": n2 / dt2, "threads": threads,
+            "substeps_per_photon": r2["substeps"] / n2}
+
+
+def run_reference(args) -> dict:
+    """--impl reference: the reference's photon-step algorithm on host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return {}
+    threads = os.cpu_count() or 1
+    per_step_s = 6.0
+    samples = []
+    for i in range(args.warmup + args.steps):
+        s = cpu_sample(per_step_s if i >= args.warmup else 2.0, threads)
+        if i >= args.warmup:
+            samples.append(s)
+    ph = sum(s["photons"] for s in samples)
+    sec = sum(s["seconds"] for s in samples)
+    v = ph / sec
+    desc = (f"{ph} photons of the 200^3 skin-vessel workload in {args.steps} samples, FP32 restatement with "
+            f"the reference's generator, {threads} threads")
+    return {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "photons/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "photons_per_step_sampled": ph // args.steps},
+        "cpu_baseline": {"value": v, "unit": "photons/s", "cores": threads, "kind": "port", "sample": desc},
+        "e2e": {"value": v, "unit": "photons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def run_ours(args) -> dict:
+    import numpy as np
+    import torch
+
+    import nmc_cases as cases
+    from nmc_gb300 import abi, build, engine
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    if rank == 0 or world == 1:
+        build.build()
+    if dist:
+        dist.barrier()
+
+    P = args.photons
+    rp, tp, v, ext = cases.skin_vessel_case(N=200)
+    e = engine.Engine(abi.SIM_MCXYZ, local, ext)
+    e.prepare_data(rp, tp, v)
+    stream = torch.cuda.ExternalStream(e.stream)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")  # > L2 (129 MB)
+    base = rank * 10 ** 12  # disjoint photon ids per rank
+
+    def step(i):
+        e.run_async(base + i * P, P)
+
+    for i in range(args.warmup):
+        step(i)
+        e.synchronize()
+    e.reset()
+    s0 = e.summary()
+
+    # -- timed region: device time of K steps (L2 flushed before each step)
+    clock_lines, stop = [], threading.Event()
+    th = threading.Thread(target=_clock_sampler, args=(stop, clock_lines, local), daemon=True)
+    th.start()
+    times = []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step(args.warmup + i)
+        b.record(stream)
+        e.synchronize()
+        times.append(a.elapsed_time(b))
+    torch.cuda.synchronize()
+    stop.set()
+    th.join(timeout=2)
+    s1 = e.summary()
+    total_ms = float(sum(times))
+    if dist:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    photons_all = P * args.steps * world
+    value = photons_all / (total_ms * 1e-3)
+    launches = s1["launches"] - s0["launches"]
+    kernel_ms = s1["kernel_ms"] - s0["kernel_ms"]
+    substeps = s1["substeps"] - s0["substeps"]
+    rd_mean = s1["rd_sum"] / max(s1["photons"], 1)
+    rd_var = s1["rd_sumsq"] / max(s1["photons"], 1) - rd_mean ** 2
+    rd_se = (rd_var / max(s1["photons"], 1)) ** 0.5
+    e.close()
+
+    # -- e2e through the C ABI with host buffers (prepare H2D + run + results D2H)
+    e2 = engine.Engine(abi.SIM_MCXYZ, local, ext)
+    e2_times = []
+    h2d = v.nbytes + 172 + 608
+    n2d = rp.Nx * rp.Ny
+    d2h = rp.Nx * rp.Ny * rp.Nz * 4 + ext.photons_per_dispatch * 4 + 2 * n2d * 4
+    for i in range(1 + min(args.steps, 3)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2.prepare_data(rp, tp, v)
+        e2.run(base + (10 ** 9) + i * P, P)
+        res = e2.get_compute_results()
+        dt = time.perf_counter() - t0
+        if i > 0:
+            e2_times.append(dt)
+    assert np.isfinite(res["F3D"]).all()
+    e2.close()
+    e2e_value = P * world / (sum(e2_times) / len(e2_times))
+
+    # -- roofline: transport kernel against the measured FP32 issue ceiling
+    ffma, mufu = engine.probe_issue_peaks(local)
+    kernel_s = kernel_ms * 1e-3
+    achieved = substeps * OPS_PER_SUBSTEP / kernel_s / 1e12 if kernel_s > 0 else None
+    peak = ffma / 1e12
+    out = {
+        "metric": METRIC, "value": value, "unit": "photons/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "photons_per_step": P, "grid": [200, 200, 200], "voxel_cm": 0.005,
+                   "l2": "256 MB buffer written before each timed step", "rng": "philox4x32-10",
+                   "rd": rd_mean, "rd_rel_se": rd_se / rd_mean if rd_mean else None,
+                   "substeps_per_photon": substeps / max(P * args.steps, 1),
+                   "parallelism": f"replicas{world}"},
+        "e2e": {"value": e2e_value, "unit": "photons/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "fp32_issue", "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "kernel": "mcxyz_kernel", "ops_per_substep": OPS_PER_SUBSTEP,
+                     "substeps_per_s": substeps / kernel_s if kernel_s > 0 else None,
+                     "mufu_peak_tlanes": mufu / 1e12, "peak_source": "measured live (nmc_probe_issue_peaks)"},
+        "gpu_launches": launches,
+        "clocks": _clocks_summary(clock_lines),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cs = cpu_sample(12.0)
+        out["cpu_baseline"] = {"value": cs["photons_per_s"], "unit": "photons/s", "cores": cs["threads"],
+                               "kind": "port",
+                               "sample": f"{cs['photons']} photons of the same workload, FP32 restatement with the "
+                                         f"reference's generator ({cs['substeps_per_photon']:.0f} sub-steps/photon), "
+                                         f"{cs['seconds']:.1f} s"}
+    if dist:
+        dist.destroy_process_group()
+    return out if rank == 0 else {}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--photons", type=int, default=PHOTONS_PER_STEP)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    out = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if out:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

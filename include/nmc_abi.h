@@ -311,6 +311,12 @@ const char* nmc_last_error(const nmc_handle* h);
 /* Frees the handle and its device memory. */
 void nmc_destroy(nmc_handle* h);
 
+/* Measurement support (no counterpart in the reference): FP32 FMA lanes per
+ * second and MUFU (ex2) lanes per second sustained on `device`, the issue
+ * ceilings that bound the transport kernels. */
+nmc_status nmc_probe_issue_peaks(int32_t device, double* ffma_lanes_per_s,
+                                 double* mufu_lanes_per_s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,79 @@
+// engine.h - parameter blocks and launch entry points of the transport
+// kernels, shared by the kernel translation units and the C-ABI runtime.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "nmc_abi.h"
+#include "nmc_device.cuh"
+
+namespace nmc {
+
+// Voxel kernels (MCXYZKernel kernels.metal:321-754 and MCXYZKernelTT
+// :757-1118).  Photon positions are kept as an integer voxel-lattice cell
+// (k = floor(x / d), unbounded) plus an FP32 offset inside the cell.
+struct XyzParams {
+  int Nx, Ny, Nz;
+  float dx, dy, dz, idx, idy, idz;
+  float dxmax, dymax, dzmax;  // largest float below dx, dy, dz
+  int ksurf;                  // zsurf = ksurf * dz + fsurf
+  float fsurf;
+  int boundaryflag, det_state;
+  int launchflag, mcflag;
+  float xs, ys, zs, ux0, uy0, uz0, radius, waist, zfocus, n1, n2;
+  float r_min, r_max, na;
+  int det_everything;         // detector accepts every exit (skips the geometry test)
+  const uint8_t* V;
+  float4 core[NMC_NTISS];     // mua, mus, 1/mus, g
+  PhaseConst phase[NMC_NTISS];
+  uint32_t flags;
+  uint32_t step_cap;
+  unsigned long long* F3D;
+  unsigned long long* Rd2D;
+  unsigned int* Det2D;
+  unsigned long long* rd_slots;
+  unsigned long long nslots;
+  DevSums* sums;
+  unsigned long long first, n;
+  RngParams rng;
+  TraceParams trace;
+};
+
+// Layered semi-infinite kernel (MCSubKernel kernels.metal:59-319).
+struct SubParams {
+  float mua, mus, mut, albedo, n1, n2;
+  float dr, dz, idr, idz;
+  int bins;
+  int mcflag, boundaryflag;
+  float radius, waist, zfocus, xs, ys, zs;
+  PhaseConst phase;  // tissue 1
+  int phase_kind;    // SubPhase
+  unsigned long long* J;  // fixed point 2^-32, BINS+1
+  unsigned long long* F;  // (BINS+1)^2
+  DevSums* sums;
+  unsigned long long first, n;
+  RngParams rng;
+  TraceParams trace;
+  uint32_t step_cap;
+};
+
+enum SubPhase { kPhaseHG = 0, kPhaseIsoRef = 1, kPhaseTT = 2 };
+
+// Launchers (blocking is up to the caller; all work goes on `stream`).
+cudaError_t launch_mcxyz(const XyzParams& p, bool two_term, bool trace, int grid, int block,
+                         cudaStream_t stream);
+cudaError_t mcxyz_occupancy(bool two_term, bool trace, int block, int* blocks_per_sm);
+
+cudaError_t launch_mcsub(const SubParams& p, bool trace, int grid, int block, cudaStream_t stream);
+cudaError_t mcsub_occupancy(const SubParams& p, bool trace, int block, int* blocks_per_sm);
+size_t mcsub_smem_bytes(int bins);
+
+// u64 fixed point (2^-32) -> float / double, element-wise.
+cudaError_t launch_unfix_f32(const unsigned long long* src, float* dst, size_t n, double scale,
+                             cudaStream_t stream);
+cudaError_t launch_unfix_f64(const unsigned long long* src, double* dst, size_t n, double scale,
+                             cudaStream_t stream);
+
+}  // namespace nmc

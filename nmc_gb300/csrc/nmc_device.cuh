@@ -1,0 +1,332 @@
+// nmc_device.cuh - device building blocks shared by the transport kernels.
+//
+// Random streams, the optical helpers of the photon step (Fresnel, phase
+// function samplers, SPIN), fixed-point tally arithmetic and the parameter
+// blocks the kernels receive.  Physics follows NMC/NMCCode/helpers.metal and
+// NMC/NMCCode/kernels.metal; line references are given per function.
+#pragma once
+
+#include <cooperative_groups.h>
+#include <cstdint>
+
+#include "nmc_abi.h"
+
+namespace nmc {
+
+namespace cg = cooperative_groups;
+
+// ------------------------------------------------------------ constants
+// definitions.h:16-82
+constexpr float kLS = 10E-8f;             // ls
+constexpr float kPIref = 3.1415926f;      // PI as the reference defines it
+constexpr float kTHRESHOLD = 0.0001f;
+constexpr float kCHANCE = 0.1f;
+constexpr float kMIN_VALUE = 1E-6f;
+constexpr int kMAX_SCATT = 10000;
+constexpr int kRAY_DEPTH = 100;
+constexpr float kCOS90D = 1.0E-6f;
+constexpr float kCOSZERO = 1.0F - 1.0E-6F;
+constexpr float kRAD_DEG = (float)(180.0F / 3.1415926);
+constexpr uint32_t kPhiloxTag = 0x4E4D4321u;
+
+// Tallies are accumulated as unsigned 64-bit fixed point with 32 fractional
+// bits: integer addition is associative, so every tally is bit-reproducible
+// whatever the order in which threads deposit.
+constexpr float kFix = 4294967296.0f;     // 2^32
+constexpr double kUnfix = 1.0 / 4294967296.0;
+
+__device__ __forceinline__ unsigned long long to_fix(float v) {
+  return v > 0.f ? __float2ull_rn(v * kFix) : 0ull;
+}
+
+// ----------------------------------------------------------------- Philox
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+    const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// 0 < u < 1, u = (2k+1) 2^-24 from the top 23 bits (exact in float).
+__device__ __forceinline__ float u01(uint32_t x) {
+  return fmaf((float)(x >> 9), 0x1p-23f, 0x1p-24f);
+}
+
+// Per-photon Philox layout (identical in the oracle):
+//   key     = (seed lo, seed hi)
+//   counter = (photon lo, photon hi, c2, 0x4E4D4321)
+//   c2 = 0xFFFFFFFF launch block; c2 = h main block of hop h;
+//   c2 = h | 0x40000000 aux block of hop h.
+//   HG family: main = (step, cos, psi, roulette), aux = (fresnel)
+//   two-term:  main = (step, choice, sample, psi), aux = (fresnel, roulette)
+// The main block of a hop is generated once at the hop's start, so every
+// thread of a warp refills at the same point of the loop.
+template <bool TT>
+struct PhiloxRng {
+  uint32_t k0, k1, plo, phi, hop, nl;
+  uint4 m, l;
+  __device__ __forceinline__ void init(uint32_t key0, uint32_t key1, uint64_t photon) {
+    k0 = key0;
+    k1 = key1;
+    plo = (uint32_t)photon;
+    phi = (uint32_t)(photon >> 32);
+    hop = 0xFFFFFFFFu;
+    nl = 0;
+    l = philox4x32_10(make_uint4(plo, phi, 0xFFFFFFFFu, kPhiloxTag), k0, k1);
+  }
+  __device__ __forceinline__ float launch_u() {
+    const uint32_t k = nl++;
+    return u01(k == 0 ? l.x : k == 1 ? l.y : k == 2 ? l.z : l.w);
+  }
+  __device__ __forceinline__ void new_hop() {
+    ++hop;
+    m = philox4x32_10(make_uint4(plo, phi, hop, kPhiloxTag), k0, k1);
+  }
+  __device__ __forceinline__ uint4 aux() const {
+    return philox4x32_10(make_uint4(plo, phi, hop | 0x40000000u, kPhiloxTag), k0, k1);
+  }
+  __device__ __forceinline__ float step_u() { return u01(m.x); }
+  __device__ __forceinline__ float cos_u() { return u01(m.y); }
+  __device__ __forceinline__ float choice_u() { return u01(m.y); }
+  __device__ __forceinline__ float sample_u() { return u01(m.z); }
+  __device__ __forceinline__ float psi_u() { return u01(TT ? m.w : m.z); }
+  __device__ __forceinline__ float roul_u() { return TT ? u01(aux().y) : u01(m.w); }
+  __device__ __forceinline__ float fres_u() { return u01(aux().x); }
+};
+
+// The reference's generator (helpers.metal:319-371), drawn sequentially in
+// the reference's order.  Used to replay the reference's own photon streams.
+struct TausRng {
+  uint32_t s1, s2, s3, s4;
+  __device__ __forceinline__ static uint32_t taus(uint32_t z, int a, int b, int c, uint32_t m) {
+    const uint32_t bb = ((z << a) ^ z) >> b;
+    return ((z & m) << c) ^ bb;
+  }
+  __device__ __forceinline__ static uint32_t xsh(uint32_t x) {
+    x ^= x << 13;
+    x ^= x >> 17;
+    x ^= x << 5;
+    return x;
+  }
+  __device__ __forceinline__ void seed(uint32_t a, uint32_t b, uint32_t c) {
+    a = xsh(a);
+    b = xsh(b);
+    c = xsh(c);
+    s1 = taus(a, 13, 19, 12, 429496729u);
+    s2 = taus(b, 2, 25, 4, 4294967288u);
+    s3 = taus(c, 3, 11, 17, 429496280u);
+    s4 = xsh(a + b + c) ^ 1013904223u;
+    s1 ^= s4;
+    s2 ^= s1;
+    s3 ^= s2;
+  }
+  // Seeding per photon (run, index) as kernels.metal:91-95 / :339-343 / :772.
+  __device__ __forceinline__ void init_photon(uint64_t photon, uint64_t batch, bool tt,
+                                              bool tt_replay) {
+    const uint32_t run = (uint32_t)(photon / batch) + 1u;
+    const uint32_t index = (uint32_t)(photon % batch);
+    if (tt) {
+      const uint32_t nr = (tt_replay ? 0u : run) + 1u;
+      seed(nr * index, nr * 1234u, index * 1234u);
+    } else {
+      const uint32_t nr = run + 1u;
+      seed((nr ^ (index * 2654435761u)) + 12345u, (nr * 1103515245u) ^ (index * 1013904223u),
+           (index ^ nr) * 1664525u + 1013904223u);
+    }
+  }
+  __device__ __forceinline__ float next() {
+    s1 = taus(s1, 13, 19, 12, 429496729u);
+    s2 = taus(s2, 2, 25, 4, 4294967288u);
+    s3 = taus(s3, 3, 11, 17, 429496280u);
+    s4 = xsh(s4);
+    return (float)((s1 ^ s2 ^ s3 ^ s4) >> 8) * (1.0f / 16777216.0f);
+  }
+  __device__ __forceinline__ float launch_u() { return next(); }
+  __device__ __forceinline__ void new_hop() {}
+  __device__ __forceinline__ float step_u() { return next(); }
+  __device__ __forceinline__ float cos_u() { return next(); }
+  __device__ __forceinline__ float choice_u() { return next(); }
+  __device__ __forceinline__ float sample_u() { return next(); }
+  __device__ __forceinline__ float psi_u() { return next(); }
+  __device__ __forceinline__ float roul_u() { return next(); }
+  __device__ __forceinline__ float fres_u() { return next(); }
+};
+
+// ---------------------------------------------------------------- optics
+// FltEq (helpers.metal:21-25) with error = 1.
+__device__ __forceinline__ bool flt_eq(float a, float b) {
+  const float e = b * 1.1920928955078125e-7f * 2.f;
+  return (a >= b - e) && (a <= b + e);
+}
+
+// Fresnel::RFresnel (helpers.metal:243-291): unpolarised reflectance from
+// medium n1 into n2 at incidence cosine ca1; *ca2 = transmitted cosine.
+__device__ __forceinline__ float rfresnel(float n1, float n2, float ca1, float* ca2) {
+  if (flt_eq(n1, n2)) {
+    *ca2 = ca1;
+    return 0.f;
+  }
+  if (ca1 > kCOSZERO) {
+    *ca2 = ca1;
+    const float r = (n2 - n1) / (n2 + n1);
+    return r * r;
+  }
+  if (ca1 < kCOS90D) {
+    *ca2 = 0.f;
+    return 1.f;
+  }
+  const float sa1 = sqrtf(fmaf(-ca1, ca1, 1.f));
+  const float sa2 = n1 * sa1 / n2;
+  if (sa2 >= 1.f) {
+    *ca2 = 0.f;
+    return 1.f;
+  }
+  const float c2 = sqrtf(fmaf(-sa2, sa2, 1.f));
+  *ca2 = c2;
+  const float cap = ca1 * c2 - sa1 * sa2, cam = ca1 * c2 + sa1 * sa2;
+  const float sap = sa1 * c2 + ca1 * sa2, sam = sa1 * c2 - ca1 * sa2;
+  return 0.5f * sam * sam * (cam * cam + cap * cap) / (sap * sap * cam * cam);
+}
+
+// Fresnel::Snell (helpers.metal:293-314).
+__device__ __forceinline__ void snell(float n1, float n2, float& ux, float& uy, float& uz) {
+  const float sc = 1.f - (1.f - uz * uz) * n1 * n1 / n2 / n2;
+  if (sc < 0.f) {
+    if (fabsf(uz) > 1.f) uz = uz < 0.f ? -1.f : 1.f;
+    return;
+  }
+  ux = ux * n1 / n2;
+  uy = uy * n1 / n2;
+  uz = sqrtf(sc);
+}
+
+// Per-tissue phase-function constants, precomputed on the host in double.
+// HG (kernels.metal:696-703): cos = (d - (a / (b + c u))^2) * e with
+// a = 1-g^2, b = 1-g, c = 2g, d = 1+g^2, e = 1/(2g); mode 1 = isotropic
+// (g == 0), mode 2 = straight ahead (g == 1).
+// Two-term (kernels.metal:1060-1070): per branch q1/(2g), 1/q2, 1/q3,
+// -1/alpha, 1/(2g); iso flag when g == 0.
+struct PhaseConst {
+  float hg_a, hg_b, hg_c, hg_d, hg_e;
+  int hg_mode;
+  float cc;
+  float f_q1e, f_iq2, f_iq3, f_ninva, f_e;
+  float b_q1e, b_iq2, b_iq3, b_ninva, b_e;
+  int f_iso, b_iso;
+};
+
+__device__ __forceinline__ float hg_sample(const PhaseConst& p, float u) {
+  if (p.hg_mode == 1) return 2.f * u - 1.f;
+  if (p.hg_mode == 2) return 1.f;
+  const float t = p.hg_a / fmaf(p.hg_c, u, p.hg_b);
+  return fmaf(-t, t, p.hg_d) * p.hg_e;
+}
+
+template <class RNG>
+__device__ __forceinline__ float tt_sample(const PhaseConst& p, RNG& rng) {
+  const float uc = rng.choice_u();
+  float c;
+  if (uc <= p.cc) {
+    const float u = rng.sample_u();
+    c = p.f_iso ? 2.f * u - 1.f
+                : p.f_q1e - powf(fmaf(u, p.f_iq2, (1.f - u) * p.f_iq3), p.f_ninva) * p.f_e;
+  } else {
+    const float u = rng.sample_u();
+    c = p.b_iso ? 2.f * u - 1.f
+                : p.b_q1e - powf(fmaf(u, p.b_iq2, (1.f - u) * p.b_iq3), p.b_ninva) * p.b_e;
+    c = -c;
+  }
+  if (c >= 1.f) c = 1.0f - 1e-9f;
+  if (c <= -1.f) c = -(1.0f - 1e-9f);
+  return c;
+}
+
+// SPIN (kernels.metal:253-279, :704-730): rotate (ux, uy, uz) by polar
+// cos(theta) and azimuth psi = 2 pi u.  Near |uz| -> 1 the rotation and a
+// renormalisation run in FP64 (1 - uz^2 loses all FP32 bits there).
+__device__ __forceinline__ void spin(float costheta, float upsi, float& ux, float& uy,
+                                     float& uz) {
+  const float sintheta = sqrtf(fmaxf(fmaf(-costheta, costheta, 1.f), 0.f));
+  float sinpsi, cospsi;
+  sincospif(2.f * upsi, &sinpsi, &cospsi);
+  const float auz = fabsf(uz);
+  if (auz >= 1.f) {  // 1 - |uz| <= 1e-12 in FP32
+    ux = sintheta * cospsi;
+    uy = sintheta * sinpsi;
+    uz = uz >= 0.f ? costheta : -costheta;
+  } else if (1.f - auz < 1e-5f) {
+    const double dz = uz, temp = sqrt(1.0 - dz * dz);
+    const double st = sintheta, ct = costheta, cp = cospsi, sp = sinpsi;
+    double nx = st * (ux * dz * cp - uy * sp) / temp + ux * ct;
+    double ny = st * (uy * dz * cp + ux * sp) / temp + uy * ct;
+    double nz = -st * cp * temp + dz * ct;
+    const double inv = 1.0 / sqrt(nx * nx + ny * ny + nz * nz);
+    ux = (float)(nx * inv);
+    uy = (float)(ny * inv);
+    uz = (float)(nz * inv);
+  } else {
+    const float temp2 = fmaf(-uz, uz, 1.f);
+    const float itemp = rsqrtf(temp2);
+    const float temp = temp2 * itemp;
+    const float nx = fmaf(sintheta * (ux * uz * cospsi - uy * sinpsi), itemp, ux * costheta);
+    const float ny = fmaf(sintheta * (uy * uz * cospsi + ux * sinpsi), itemp, uy * costheta);
+    const float nz = fmaf(-sintheta * cospsi, temp, uz * costheta);
+    ux = nx;
+    uy = ny;
+    uz = nz;
+  }
+}
+
+// ----------------------------------------------------------- work queue
+// Hands out photon indices in warp-aggregated chunks: one atomic per group
+// of threads that need a photon at the same time.
+__device__ __forceinline__ unsigned long long next_photon(unsigned long long* counter) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned long long base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(counter, (unsigned long long)g.size());
+  base = g.shfl(base, 0);
+  return base + g.thread_rank();
+}
+
+// Sums a per-thread u64 over the warp, then one atomic per warp.
+__device__ __forceinline__ void warp_add_u64(unsigned long long* dst, unsigned long long v) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  for (int o = 16; o > 0; o >>= 1) v += g.shfl_down(v, o);
+  if (g.thread_rank() == 0 && v) atomicAdd(dst, v);
+}
+__device__ __forceinline__ void warp_add_f64(double* dst, double v) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  for (int o = 16; o > 0; o >>= 1) v += g.shfl_down(v, o);
+  if (g.thread_rank() == 0 && v != 0.0) atomicAdd(dst, v);
+}
+
+// ------------------------------------------------------------ parameters
+// Totals every launch adds into (device memory, one per handle).
+struct DevSums {
+  unsigned long long photons, substeps, scatters;
+  unsigned long long S, A, E, rd;  // fixed point 2^-32
+  double rd_sumsq;
+  unsigned int flags, pad;
+  unsigned long long work;         // photon counter of the running launch
+};
+
+struct RngParams {
+  uint32_t kind;  // NMC_RNG_*
+  uint32_t k0, k1;
+  uint32_t tt_replay;
+  uint64_t batch;  // photons_per_dispatch (Taus run/index mapping)
+};
+
+struct TraceParams {
+  nmc_photon_record* recs;
+  float4* events;
+  uint32_t k_events;
+};
+
+}  // namespace nmc

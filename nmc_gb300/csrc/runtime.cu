@@ -1,0 +1,761 @@
+// runtime.cu - the C ABI of include/nmc_abi.h.
+//
+// Replaces the reference's Objective-C host runtime (NMC/NMCCode/MetalMC.m):
+// kernel selection (MetalMC.m:115-149), buffer set-up (:179-383), dispatch
+// (:385-496) and the host-side tally reduction (:508-824).  Differences by
+// design:
+//  * one persistent launch simulates any number of photons (the reference
+//    dispatches PHOTON_BATCH threads per blocking command buffer);
+//  * tallies are device-resident u64 fixed point (no per-thread slabs: the
+//    reference's mcxyz Rd2D/DetPhot2D slabs are PHOTON_BATCH*Nx*Ny each);
+//  * every call returns a status; waits are bounded by nmc_ext.timeout_s.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "engine.h"
+#include "nmc_abi.h"
+
+using nmc::DevSums;
+
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+};
+
+struct nmc_handle {
+  int sim = 0;
+  int device = 0;
+  nmc_ext ext{};
+  nmc_run_params rp{};
+  nmc_tissue_params tp{};
+  bool prepared = false;
+  std::string err;
+  int32_t run = 1;
+  cudaStream_t stream = nullptr;
+  int nsm = 0;
+  DevSums* d_sums = nullptr;
+  uint8_t* d_V = nullptr;
+  unsigned long long* d_F3D = nullptr;
+  unsigned long long* d_Rd2D = nullptr;
+  unsigned int* d_Det = nullptr;
+  unsigned long long* d_slots = nullptr;
+  unsigned long long* d_J = nullptr;
+  unsigned long long* d_F = nullptr;
+  size_t nvox = 0, n2d = 0, nslots = 0, nJ = 0, nF = 0;
+  float* d_stage = nullptr;  // conversion buffer for results (floats)
+  float* h_stage = nullptr;  // pinned host copy
+  size_t stage_elems = 0;
+  std::vector<EventPair> pending;
+  std::vector<EventPair> pool;
+  double kernel_ms = 0.0;
+  uint32_t launches = 0;
+  uint32_t seen_flags = 0;
+  nmc::XyzParams xp{};
+  nmc::SubParams sp{};
+};
+
+namespace {
+
+nmc_status fail(nmc_handle* h, nmc_status st, const std::string& msg) {
+  if (h) h->err = msg;
+  return st;
+}
+
+nmc_status cuda_fail(nmc_handle* h, cudaError_t e, const char* what) {
+  return fail(h, NMC_EDEVICE, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define NMC_CUDA(h, call)                                 \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+template <class T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+void free_buffers(nmc_handle* h) {
+  dfree(h->d_V);
+  dfree(h->d_F3D);
+  dfree(h->d_Rd2D);
+  dfree(h->d_Det);
+  dfree(h->d_slots);
+  dfree(h->d_J);
+  dfree(h->d_F);
+  dfree(h->d_stage);
+  if (h->h_stage) cudaFreeHost(h->h_stage);
+  h->h_stage = nullptr;
+  h->nvox = h->n2d = h->nslots = h->nJ = h->nF = h->stage_elems = 0;
+}
+
+bool finite_nonneg(float v) { return std::isfinite(v) && v >= 0.f; }
+
+bool flt_eq_host(float a, float b) {
+  const float e = b * 1.1920928955078125e-7f * 2.f;
+  return (a >= b - e) && (a <= b + e);
+}
+
+// Phase-function constants for one tissue, computed in double.
+nmc::PhaseConst phase_const(const nmc_tissue_params& tp, int t) {
+  nmc::PhaseConst p{};
+  const double g = tp.gv[t];
+  p.hg_mode = (tp.gv[t] == 0.f) ? 1 : (flt_eq_host(tp.gv[t], 1.f) ? 2 : 0);
+  if (p.hg_mode == 0) {
+    p.hg_a = (float)(1.0 - g * g);
+    p.hg_b = (float)(1.0 - g);
+    p.hg_c = (float)(2.0 * g);
+    p.hg_d = (float)(1.0 + g * g);
+    p.hg_e = (float)(1.0 / (2.0 * g));
+  }
+  const double gf = tp.gf[t], af = tp.af[t], gb = tp.gb[t], ab = tp.ab[t];
+  p.cc = tp.CC[t];
+  p.f_iso = gf == 0.0;
+  p.b_iso = gb == 0.0;
+  if (!p.f_iso) {
+    const double q1 = 1.0 + gf * gf, q2 = std::pow(1.0 - gf, 2.0 * af), q3 = std::pow(1.0 + gf, 2.0 * af);
+    p.f_q1e = (float)(q1 / (2.0 * gf));
+    p.f_iq2 = (float)(1.0 / q2);
+    p.f_iq3 = (float)(1.0 / q3);
+    p.f_ninva = (float)(-1.0 / af);
+    p.f_e = (float)(1.0 / (2.0 * gf));
+  }
+  if (!p.b_iso) {
+    const double q1 = 1.0 + gb * gb, q2 = std::pow(1.0 - gb, 2.0 * ab), q3 = std::pow(1.0 + gb, 2.0 * ab);
+    p.b_q1e = (float)(q1 / (2.0 * gb));
+    p.b_iq2 = (float)(1.0 / q2);
+    p.b_iq3 = (float)(1.0 / q3);
+    p.b_ninva = (float)(-1.0 / ab);
+    p.b_e = (float)(1.0 / (2.0 * gb));
+  }
+  return p;
+}
+
+nmc::RngParams rng_params(const nmc_ext& e, int sim) {
+  nmc::RngParams r{};
+  r.kind = e.rng;
+  r.k0 = (uint32_t)e.seed;
+  r.k1 = (uint32_t)(e.seed >> 32);
+  r.tt_replay = (sim == NMC_SIM_MCXYZ_TT && (e.flags & NMC_FLAG_TT_REPLAY_RUN1)) ? 1u : 0u;
+  r.batch = e.photons_per_dispatch;
+  return r;
+}
+
+void lattice_split(float zsurf, float dz, int* k, float* f) {
+  const double q = std::floor((double)zsurf / (double)dz);
+  double rem = (double)zsurf - q * (double)dz;
+  int kk = (int)q;
+  if (rem < 0) {
+    rem += dz;
+    --kk;
+  }
+  if (rem >= dz) {
+    rem -= dz;
+    ++kk;
+  }
+  *k = kk;
+  *f = (float)rem;
+  if (*f >= dz) *f = std::nextafter(dz, 0.f);
+}
+
+nmc_status build_xyz(nmc_handle* h) {
+  const nmc_run_params& rp = h->rp;
+  nmc::XyzParams& p = h->xp;
+  p = nmc::XyzParams{};
+  p.Nx = rp.Nx;
+  p.Ny = rp.Ny;
+  p.Nz = rp.Nz;
+  p.dx = rp.dx;
+  p.dy = rp.dy;
+  p.dz = rp.dz;
+  p.idx = (float)(1.0 / rp.dx);
+  p.idy = (float)(1.0 / rp.dy);
+  p.idz = (float)(1.0 / rp.dz);
+  p.dxmax = std::nextafter(rp.dx, 0.f);
+  p.dymax = std::nextafter(rp.dy, 0.f);
+  p.dzmax = std::nextafter(rp.dz, 0.f);
+  lattice_split(rp.zsurf, rp.dz, &p.ksurf, &p.fsurf);
+  p.boundaryflag = rp.boundaryflag;
+  p.det_state = rp.det_state;
+  p.launchflag = rp.launchflag;
+  p.mcflag = rp.mcflag;
+  p.xs = rp.xs;
+  p.ys = rp.ys;
+  p.zs = rp.zs;
+  p.ux0 = rp.ux0;
+  p.uy0 = rp.uy0;
+  p.uz0 = rp.uz0;
+  p.radius = rp.radius;
+  p.waist = rp.waist;
+  p.zfocus = rp.zfocus;
+  p.n1 = rp.n1;
+  p.n2 = rp.n2;
+  if (flt_eq_host(rp.xd, 0.f)) {  // kernels.metal:590-599
+    p.r_min = 0.f;
+    p.r_max = rp.det_radius;
+  } else {
+    p.r_min = rp.xd - rp.det_radius;
+    p.r_max = p.r_min + 2.f * rp.det_radius;
+  }
+  p.na = rp.na;
+  p.det_everything = (p.r_min <= 0.f && std::isinf(p.r_max) && rp.na >= 90.f) ? 1 : 0;
+  p.V = h->d_V;
+  for (int t = 0; t < NMC_NTISS; ++t) {
+    const float mus = h->tp.musv[t];
+    p.core[t] = make_float4(h->tp.muav[t], mus, mus > 0.f ? (float)(1.0 / mus) : 0.f, h->tp.gv[t]);
+    p.phase[t] = phase_const(h->tp, t);
+  }
+  p.flags = h->ext.flags;
+  p.step_cap = 4000000u;
+  p.F3D = h->d_F3D;
+  p.Rd2D = h->d_Rd2D;
+  p.Det2D = h->d_Det;
+  p.rd_slots = h->d_slots;
+  p.nslots = h->nslots;
+  p.sums = h->d_sums;
+  p.rng = rng_params(h->ext, h->sim);
+  return NMC_OK;
+}
+
+nmc_status build_sub(nmc_handle* h) {
+  const nmc_ext& e = h->ext;
+  nmc::SubParams& p = h->sp;
+  p = nmc::SubParams{};
+  const int L = 1;  // FIRST_TISSUE_LAYER_MCSUB
+  p.mua = h->tp.muav[L];
+  p.mus = h->tp.musv[L];
+  p.mut = p.mua + p.mus;
+  p.albedo = p.mus / p.mut;
+  p.n1 = h->rp.n1;
+  p.n2 = h->rp.n2;
+  p.dr = e.sub_dr;
+  p.dz = e.sub_dz;
+  p.idr = (float)(1.0 / e.sub_dr);
+  p.idz = (float)(1.0 / e.sub_dz);
+  p.bins = e.sub_bins;
+  p.mcflag = e.sub_mcflag;
+  p.boundaryflag = e.sub_boundaryflag;
+  p.radius = e.sub_radius;
+  p.waist = e.sub_waist;
+  p.zfocus = e.sub_zfocus;
+  p.xs = e.sub_xs;
+  p.ys = e.sub_ys;
+  p.zs = e.sub_zs;
+  p.phase = phase_const(h->tp, L);
+  p.phase_kind = e.phase == NMC_PHASE_TWO_TERM ? nmc::kPhaseTT
+                 : e.phase == NMC_PHASE_ISOTROPIC_REF ? nmc::kPhaseIsoRef
+                                                      : nmc::kPhaseHG;
+  p.J = h->d_J;
+  p.F = h->d_F;
+  p.sums = h->d_sums;
+  p.rng = rng_params(e, h->sim);
+  p.step_cap = 10000000u;
+  return NMC_OK;
+}
+
+nmc_status validate(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue_params* tp,
+                    const uint8_t* v) {
+  const nmc_ext& e = h->ext;
+  if (e.photons_per_dispatch == 0) return fail(h, NMC_EINVAL, "photons_per_dispatch must be > 0");
+  if (e.rng != NMC_RNG_PHILOX && e.rng != NMC_RNG_TAUS_REF) return fail(h, NMC_EINVAL, "unknown rng");
+  if (h->sim == NMC_SIM_MCSUB) {
+    if (e.sub_bins < 2 || e.sub_bins > 4096) return fail(h, NMC_EINVAL, "sub_bins out of range [2, 4096]");
+    if (!(e.sub_dr > 0.f) || !(e.sub_dz > 0.f)) return fail(h, NMC_EINVAL, "sub_dr / sub_dz must be > 0");
+    if (e.phase > NMC_PHASE_TWO_TERM) return fail(h, NMC_EINVAL, "unknown phase function");
+    const float mua = tp->muav[1], mus = tp->musv[1];
+    if (!finite_nonneg(mua) || !finite_nonneg(mus) || !(mua + mus > 0.f))
+      return fail(h, NMC_EINVAL, "tissue 1 needs finite mua, mus >= 0 with mua + mus > 0");
+    if (!(rp->n1 > 0.f) || !(rp->n2 > 0.f)) return fail(h, NMC_EINVAL, "n1, n2 must be > 0");
+    return NMC_OK;
+  }
+  if (!v) return fail(h, NMC_EINVAL, "voxel kinds need a tissue map");
+  if (rp->Nx <= 0 || rp->Ny <= 0 || rp->Nz <= 0) return fail(h, NMC_EINVAL, "Nx, Ny, Nz must be > 0");
+  if ((double)rp->Nx * rp->Ny * rp->Nz >= 2147483647.0) return fail(h, NMC_EINVAL, "grid too large (>= 2^31 voxels)");
+  if (!(rp->dx > 0.f) || !(rp->dy > 0.f) || !(rp->dz > 0.f) || !std::isfinite(rp->dx) ||
+      !std::isfinite(rp->dy) || !std::isfinite(rp->dz))
+    return fail(h, NMC_EINVAL, "dx, dy, dz must be finite and > 0");
+  if (rp->boundaryflag < 0 || rp->boundaryflag > 2) return fail(h, NMC_EINVAL, "boundaryflag must be 0, 1 or 2");
+  if (rp->det_state != 0 && rp->det_state != 1) return fail(h, NMC_EINVAL, "det_state must be 0 or 1");
+  if (!(rp->n1 > 0.f) || !(rp->n2 > 0.f)) return fail(h, NMC_EINVAL, "n1, n2 must be > 0");
+  bool used[NMC_NTISS] = {false};
+  const size_t n = (size_t)rp->Nx * rp->Ny * rp->Nz;
+  for (size_t k = 0; k < n; ++k) {
+    if (v[k] >= NMC_NTISS) {
+      char msg[96];
+      std::snprintf(msg, sizeof msg, "tissue id %u at voxel %zu exceeds %d", (unsigned)v[k], k, NMC_NTISS - 1);
+      return fail(h, NMC_EINVAL, msg);
+    }
+    used[v[k]] = true;
+  }
+  for (int t = 0; t < NMC_NTISS; ++t) {
+    if (!used[t]) continue;
+    if (!finite_nonneg(tp->muav[t]) || !(tp->musv[t] > 0.f) || !std::isfinite(tp->musv[t]) ||
+        !std::isfinite(tp->gv[t])) {
+      char msg[96];
+      std::snprintf(msg, sizeof msg, "tissue %d needs finite mua >= 0, mus > 0 and g", t);
+      return fail(h, NMC_EINVAL, msg);
+    }
+  }
+  return NMC_OK;
+}
+
+nmc_status wait_event(nmc_handle* h, cudaEvent_t ev) {
+  const auto t0 = std::chrono::steady_clock::now();
+  const double limit = h->ext.timeout_s > 0 ? h->ext.timeout_s : 1e30;
+  while (true) {
+    const cudaError_t q = cudaEventQuery(ev);
+    if (q == cudaSuccess) return NMC_OK;
+    if (q != cudaErrorNotReady) return cuda_fail(h, q, "kernel execution");
+    const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (el > limit) return fail(h, NMC_ETIMEOUT, "device work did not finish within timeout_s");
+    std::this_thread::sleep_for(std::chrono::microseconds(el < 0.01 ? 20 : 500));
+  }
+}
+
+// Waits (bounded by timeout_s) for everything queued on the handle's stream.
+nmc_status wait_stream(nmc_handle* h) {
+  cudaEvent_t ev;
+  NMC_CUDA(h, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  cudaError_t e = cudaEventRecord(ev, h->stream);
+  nmc_status st = e == cudaSuccess ? wait_event(h, ev) : cuda_fail(h, e, "cudaEventRecord");
+  cudaEventDestroy(ev);
+  return st;
+}
+
+EventPair get_pair(nmc_handle* h) {
+  if (!h->pool.empty()) {
+    EventPair p = h->pool.back();
+    h->pool.pop_back();
+    return p;
+  }
+  EventPair p;
+  cudaEventCreate(&p.a);
+  cudaEventCreate(&p.b);
+  return p;
+}
+
+nmc_status launch(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_record* d_recs,
+                  float4* d_events, uint32_t k_events) {
+  if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
+  if (n == 0) return NMC_OK;
+  NMC_CUDA(h, cudaSetDevice(h->device));
+  NMC_CUDA(h, cudaMemsetAsync(&h->d_sums->work, 0, sizeof(unsigned long long), h->stream));
+  const bool trace = d_recs != nullptr;
+  nmc::TraceParams tr{d_recs, d_events, d_events ? k_events : 0u};
+  int block, per_sm = 0;
+  EventPair ev = get_pair(h);
+  NMC_CUDA(h, cudaEventRecord(ev.a, h->stream));
+  if (h->sim == NMC_SIM_MCSUB) {
+    nmc::SubParams p = h->sp;
+    p.first = first;
+    p.n = n;
+    p.trace = tr;
+    block = h->ext.block_size > 0 ? h->ext.block_size : 512;
+    NMC_CUDA(h, nmc::mcsub_occupancy(p, trace, block, &per_sm));
+    if (h->ext.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)h->ext.blocks_per_sm);
+    if (per_sm < 1) return fail(h, NMC_EDEVICE, "mcsub kernel does not fit on an SM with this block size");
+    uint64_t grid = (uint64_t)h->nsm * per_sm;
+    grid = std::min<uint64_t>(grid, (n + block - 1) / block);
+    NMC_CUDA(h, nmc::launch_mcsub(p, trace, (int)grid, block, h->stream));
+  } else {
+    nmc::XyzParams p = h->xp;
+    p.first = first;
+    p.n = n;
+    p.trace = tr;
+    block = h->ext.block_size > 0 ? h->ext.block_size : 256;
+    const bool tt = h->sim == NMC_SIM_MCXYZ_TT;
+    NMC_CUDA(h, nmc::mcxyz_occupancy(tt, trace, block, &per_sm));
+    if (h->ext.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)h->ext.blocks_per_sm);
+    if (per_sm < 1) return fail(h, NMC_EDEVICE, "mcxyz kernel does not fit on an SM with this block size");
+    uint64_t grid = (uint64_t)h->nsm * per_sm;
+    grid = std::min<uint64_t>(grid, (n + block - 1) / block);
+    NMC_CUDA(h, nmc::launch_mcxyz(p, tt, trace, (int)grid, block, h->stream));
+  }
+  NMC_CUDA(h, cudaEventRecord(ev.b, h->stream));
+  h->pending.push_back(ev);
+  ++h->launches;
+  return NMC_OK;
+}
+
+nmc_status sync_all(nmc_handle* h) {
+  if (h->pending.empty()) {
+    NMC_CUDA(h, cudaStreamSynchronize(h->stream));
+    return NMC_OK;
+  }
+  nmc_status st = wait_event(h, h->pending.back().b);
+  if (st != NMC_OK) return st;
+  for (EventPair& p : h->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) h->kernel_ms += ms;
+    h->pool.push_back(p);
+  }
+  h->pending.clear();
+  NMC_CUDA(h, cudaStreamSynchronize(h->stream));
+  unsigned int flags = 0;
+  NMC_CUDA(h, cudaMemcpy(&flags, &h->d_sums->flags, sizeof flags, cudaMemcpyDeviceToHost));
+  const unsigned int fresh = flags & ~h->seen_flags;
+  h->seen_flags = flags;
+  if (fresh & NMC_DEVFLAG_STEPCAP)
+    return fail(h, NMC_ESTEPCAP, "a photon reached the device step cap and was terminated");
+  return NMC_OK;
+}
+
+__global__ void unfix_f32(const unsigned long long* __restrict__ s, float* __restrict__ d, size_t n,
+                          double scale) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    d[k] = (float)((double)s[k] * scale);
+}
+__global__ void unfix_f64(const unsigned long long* __restrict__ s, double* __restrict__ d, size_t n,
+                          double scale) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    d[k] = (double)s[k] * scale;
+}
+__global__ void u32_to_f32(const unsigned int* __restrict__ s, float* __restrict__ d, size_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    d[k] = __uint_as_float(s[k]);
+}
+
+// Converts a device tally into h->h_stage as floats (u32 counts are passed
+// through bit-exactly and reinterpreted by the caller).
+nmc_status stage_tally(nmc_handle* h, const void* dsrc, size_t n, bool counts) {
+  if (n > h->stage_elems) return fail(h, NMC_EINVAL, "staging buffer too small");
+  const int block = 256;
+  const int grid = (int)std::min<size_t>((n + block - 1) / block, (size_t)h->nsm * 8);
+  if (counts)
+    u32_to_f32<<<grid, block, 0, h->stream>>>((const unsigned int*)dsrc, h->d_stage, n);
+  else
+    unfix_f32<<<grid, block, 0, h->stream>>>((const unsigned long long*)dsrc, h->d_stage, n,
+                                             nmc::kUnfix);
+  NMC_CUDA(h, cudaGetLastError());
+  NMC_CUDA(h, cudaMemcpyAsync(h->h_stage, h->d_stage, n * sizeof(float), cudaMemcpyDeviceToHost,
+                              h->stream));
+  return wait_stream(h);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- C entry points
+extern "C" {
+
+void nmc_ext_defaults(nmc_ext* e) {
+  if (!e) return;
+  std::memset(e, 0, sizeof *e);
+  e->size = sizeof(nmc_ext);
+  e->rng = NMC_RNG_PHILOX;
+  e->seed = 0;
+  e->phase = NMC_PHASE_HG;
+  e->flags = 0;
+  e->photons_per_dispatch = NMC_PHOTON_BATCH_DEFAULT;
+  e->photons_total = NMC_PHOTON_TOTAL_DEFAULT;
+  e->sub_bins = NMC_MCSUB_BINS_DEFAULT;
+  e->sub_dr = NMC_MCSUB_DR_DEFAULT;
+  e->sub_dz = NMC_MCSUB_DZ_DEFAULT;
+  e->sub_mcflag = 0;          // mcflag_mcsub (definitions.h:38)
+  e->sub_boundaryflag = 1;    // boundaryflag_mcsub (definitions.h:48)
+  e->sub_radius = 0.0f;       // radius_mcsub
+  e->sub_waist = 0.10f;       // waist_mcsub
+  e->sub_zfocus = 1.0f;       // zfocus_mcsub
+  e->sub_xs = e->sub_ys = e->sub_zs = 0.0f;
+  e->block_size = 0;
+  e->blocks_per_sm = 0;
+  e->timeout_s = 600.0;
+}
+
+int32_t nmc_abi_version(void) { return NMC_ABI_VERSION; }
+
+nmc_status nmc_create(int32_t sim_type, int32_t device, nmc_handle** out) {
+  if (!out) return NMC_EINVAL;
+  *out = nullptr;
+  if (sim_type == NMC_SIM_POLARIZATION_CBS_ELECTRIC_FIELDS || sim_type == NMC_SIM_RAMAN ||
+      sim_type == NMC_SIM_POLARIZATION_MUELLER_STOKES)
+    return NMC_EUNSUPPORTED;
+  if (sim_type != NMC_SIM_MCSUB && sim_type != NMC_SIM_MCXYZ && sim_type != NMC_SIM_MCXYZ_TT)
+    return NMC_EINVAL;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return NMC_EDEVICE;
+  nmc_handle* h = new (std::nothrow) nmc_handle();
+  if (!h) return NMC_ENOMEM;
+  h->sim = sim_type;
+  h->device = device;
+  nmc_ext_defaults(&h->ext);
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaMalloc((void**)&h->d_sums, sizeof(DevSums)) != cudaSuccess ||
+      cudaMemset(h->d_sums, 0, sizeof(DevSums)) != cudaSuccess) {
+    if (h->d_sums) cudaFree(h->d_sums);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return NMC_EDEVICE;
+  }
+  *out = h;
+  return NMC_OK;
+}
+
+nmc_status nmc_set_ext(nmc_handle* h, const nmc_ext* ext) {
+  if (!h || !ext) return NMC_EINVAL;
+  if (ext->size != sizeof(nmc_ext)) return fail(h, NMC_EINVAL, "nmc_ext.size does not match this library");
+  const bool reprepare = h->prepared;
+  h->ext = *ext;
+  if (reprepare) {
+    if (h->sim == NMC_SIM_MCSUB && (size_t)h->ext.sub_bins + 1 != h->nJ)
+      return fail(h, NMC_ESTATE, "sub_bins changed: call nmc_prepare again");
+    if (h->sim != NMC_SIM_MCSUB && h->ext.photons_per_dispatch != h->nslots)
+      return fail(h, NMC_ESTATE, "photons_per_dispatch changed: call nmc_prepare again");
+    return h->sim == NMC_SIM_MCSUB ? build_sub(h) : build_xyz(h);
+  }
+  return NMC_OK;
+}
+
+nmc_status nmc_prepare(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue_params* tp,
+                       const uint8_t* v) {
+  if (!h || !rp || !tp) return fail(h, NMC_EINVAL, "null argument");
+  nmc_status st = validate(h, rp, tp, v);
+  if (st != NMC_OK) return st;
+  NMC_CUDA(h, cudaSetDevice(h->device));
+  st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  free_buffers(h);
+  h->prepared = false;
+  h->rp = *rp;
+  h->tp = *tp;
+  size_t stage = 4096;
+  if (h->sim == NMC_SIM_MCSUB) {
+    h->nJ = (size_t)h->ext.sub_bins + 1;
+    h->nF = h->nJ * h->nJ;
+    NMC_CUDA(h, cudaMalloc((void**)&h->d_J, h->nJ * 8));
+    NMC_CUDA(h, cudaMalloc((void**)&h->d_F, h->nF * 8));
+    stage = std::max(stage, h->nF);
+  } else {
+    h->nvox = (size_t)rp->Nx * rp->Ny * rp->Nz;
+    h->n2d = (size_t)rp->Nx * rp->Ny;
+    h->nslots = h->ext.photons_per_dispatch;
+    NMC_CUDA(h, cudaMalloc((void**)&h->d_V, h->nvox));
+    NMC_CUDA(h, cudaMemcpyAsync(h->d_V, v, h->nvox, cudaMemcpyHostToDevice, h->stream));
+    NMC_CUDA(h, cudaMalloc((void**)&h->d_F3D, h->nvox * 8));
+    NMC_CUDA(h, cudaMalloc((void**)&h->d_Rd2D, h->n2d * 8));
+    NMC_CUDA(h, cudaMalloc((void**)&h->d_Det, h->n2d * 4));
+    NMC_CUDA(h, cudaMalloc((void**)&h->d_slots, h->nslots * 8));
+    stage = std::max({stage, h->nvox, h->n2d, h->nslots});
+  }
+  h->stage_elems = stage;
+  NMC_CUDA(h, cudaMalloc((void**)&h->d_stage, stage * sizeof(float)));
+  NMC_CUDA(h, cudaMallocHost((void**)&h->h_stage, stage * sizeof(float)));
+  h->prepared = true;
+  st = nmc_reset(h);
+  if (st != NMC_OK) return st;
+  return h->sim == NMC_SIM_MCSUB ? build_sub(h) : build_xyz(h);
+}
+
+nmc_status nmc_reset(nmc_handle* h) {
+  if (!h) return NMC_EINVAL;
+  if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
+  nmc_status st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  NMC_CUDA(h, cudaMemsetAsync(h->d_sums, 0, sizeof(DevSums), h->stream));
+  if (h->d_J) NMC_CUDA(h, cudaMemsetAsync(h->d_J, 0, h->nJ * 8, h->stream));
+  if (h->d_F) NMC_CUDA(h, cudaMemsetAsync(h->d_F, 0, h->nF * 8, h->stream));
+  if (h->d_F3D) NMC_CUDA(h, cudaMemsetAsync(h->d_F3D, 0, h->nvox * 8, h->stream));
+  if (h->d_Rd2D) NMC_CUDA(h, cudaMemsetAsync(h->d_Rd2D, 0, h->n2d * 8, h->stream));
+  if (h->d_Det) NMC_CUDA(h, cudaMemsetAsync(h->d_Det, 0, h->n2d * 4, h->stream));
+  if (h->d_slots) NMC_CUDA(h, cudaMemsetAsync(h->d_slots, 0, h->nslots * 8, h->stream));
+  h->kernel_ms = 0.0;
+  h->launches = 0;
+  h->seen_flags = 0;
+  return wait_stream(h);
+}
+
+nmc_status nmc_set_num_runs_seed(nmc_handle* h, int32_t run, float time_seed) {
+  (void)time_seed;  // never read by the reference kernels (kernels.metal:330 is unused)
+  if (!h) return NMC_EINVAL;
+  if (run < 1) return fail(h, NMC_EINVAL, "run numbers start at 1 (main.m:159)");
+  h->run = run;
+  return NMC_OK;
+}
+
+nmc_status nmc_send_compute_command(nmc_handle* h) {
+  if (!h) return NMC_EINVAL;
+  const uint64_t b = h->ext.photons_per_dispatch;
+  return nmc_run(h, (uint64_t)(h->run - 1) * b, b);
+}
+
+nmc_status nmc_run_async(nmc_handle* h, uint64_t first, uint64_t n) {
+  if (!h) return NMC_EINVAL;
+  return launch(h, first, n, nullptr, nullptr, 0);
+}
+
+nmc_status nmc_synchronize(nmc_handle* h) {
+  if (!h) return NMC_EINVAL;
+  return sync_all(h);
+}
+
+nmc_status nmc_run(nmc_handle* h, uint64_t first, uint64_t n) {
+  nmc_status st = nmc_run_async(h, first, n);
+  if (st != NMC_OK) return st;
+  return sync_all(h);
+}
+
+nmc_status nmc_run_traced(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_record* recs,
+                          float* events, uint32_t k_events) {
+  if (!h || !recs) return fail(h, NMC_EINVAL, "null argument");
+  if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
+  nmc_photon_record* d_recs = nullptr;
+  float4* d_ev = nullptr;
+  NMC_CUDA(h, cudaSetDevice(h->device));
+  NMC_CUDA(h, cudaMalloc((void**)&d_recs, n * sizeof(nmc_photon_record)));
+  const size_t nev = events ? (size_t)n * k_events : 0;
+  if (nev) {
+    if (cudaMalloc((void**)&d_ev, nev * sizeof(float4)) != cudaSuccess) {
+      cudaFree(d_recs);
+      return fail(h, NMC_ENOMEM, "trace event buffer");
+    }
+    std::vector<float> nanv(nev * 4, NAN);
+    cudaMemcpy(d_ev, nanv.data(), nev * sizeof(float4), cudaMemcpyHostToDevice);
+  }
+  nmc_status st = launch(h, first, n, d_recs, d_ev, nev ? k_events : 0);
+  if (st == NMC_OK) st = sync_all(h);
+  if (st == NMC_OK || st == NMC_ESTEPCAP) {
+    if (cudaMemcpy(recs, d_recs, n * sizeof(nmc_photon_record), cudaMemcpyDeviceToHost) != cudaSuccess)
+      st = fail(h, NMC_EDEVICE, "copying trace records");
+    if (nev && cudaMemcpy(events, d_ev, nev * sizeof(float4), cudaMemcpyDeviceToHost) != cudaSuccess)
+      st = fail(h, NMC_EDEVICE, "copying trace events");
+  }
+  cudaFree(d_recs);
+  if (d_ev) cudaFree(d_ev);
+  return st;
+}
+
+size_t nmc_tally_size(nmc_handle* h, int32_t which) {
+  if (!h || !h->prepared) return 0;
+  switch (which) {
+    case NMC_TALLY_J: return h->nJ;
+    case NMC_TALLY_F: return h->nF;
+    case NMC_TALLY_F3D: return h->nvox;
+    case NMC_TALLY_RD2D: return h->n2d;
+    case NMC_TALLY_DETPHOT2D: return h->n2d;
+    case NMC_TALLY_RD_SLOTS: return h->nslots;
+    default: return 0;
+  }
+}
+
+nmc_status nmc_get_tally_f64(nmc_handle* h, int32_t which, double* out, size_t n) {
+  if (!h || !out) return fail(h, NMC_EINVAL, "null argument");
+  if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
+  const size_t want = nmc_tally_size(h, which);
+  if (want == 0 || n != want) return fail(h, NMC_EINVAL, "tally not produced by this kind, or wrong size");
+  nmc_status st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  if (which == NMC_TALLY_DETPHOT2D) {
+    std::vector<unsigned int> tmp(n);
+    NMC_CUDA(h, cudaMemcpy(tmp.data(), h->d_Det, n * 4, cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < n; ++k) out[k] = tmp[k];
+    return NMC_OK;
+  }
+  const unsigned long long* src = which == NMC_TALLY_J ? h->d_J
+                                  : which == NMC_TALLY_F ? h->d_F
+                                  : which == NMC_TALLY_F3D ? h->d_F3D
+                                  : which == NMC_TALLY_RD2D ? h->d_Rd2D
+                                                           : h->d_slots;
+  std::vector<unsigned long long> tmp(n);
+  NMC_CUDA(h, cudaMemcpy(tmp.data(), src, n * 8, cudaMemcpyDeviceToHost));
+  for (size_t k = 0; k < n; ++k) out[k] = (double)tmp[k] * nmc::kUnfix;
+  return NMC_OK;
+}
+
+nmc_status nmc_get_compute_results(nmc_handle* h, float* J, float* F, float* F3D, float* SAE,
+                                   float* Rd, float* Rd2D, int32_t* DetPhot2D, float* PolXX,
+                                   float* PolXY, float* PolYX, float* PolYY, float* Phase0,
+                                   float* Phase1, float* Phase2, float* Phase3, float* PolVsScatt) {
+  (void)PolXX, (void)PolXY, (void)PolYX, (void)PolYY, (void)Phase0, (void)Phase1, (void)Phase2,
+      (void)Phase3, (void)PolVsScatt;
+  if (!h) return NMC_EINVAL;
+  if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
+  nmc_status st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  auto add_f = [&](float* dst, const void* src, size_t n, bool counts) -> nmc_status {
+    if (!dst || !src || n == 0) return NMC_OK;
+    nmc_status s = stage_tally(h, src, n, counts);
+    if (s != NMC_OK) return s;
+    if (counts) {
+      const unsigned int* c = reinterpret_cast<const unsigned int*>(h->h_stage);
+      for (size_t k = 0; k < n; ++k) reinterpret_cast<int32_t*>(dst)[k] += (int32_t)c[k];
+    } else {
+      for (size_t k = 0; k < n; ++k) dst[k] += h->h_stage[k];
+    }
+    return NMC_OK;
+  };
+  if (h->sim == NMC_SIM_MCSUB) {
+    if ((st = add_f(J, h->d_J, h->nJ, false)) != NMC_OK) return st;
+    if ((st = add_f(F, h->d_F, h->nF, false)) != NMC_OK) return st;
+    if (SAE) {
+      DevSums s;
+      NMC_CUDA(h, cudaMemcpy(&s, h->d_sums, sizeof s, cudaMemcpyDeviceToHost));
+      SAE[0] += (float)(s.S * nmc::kUnfix);
+      SAE[1] += (float)(s.A * nmc::kUnfix);
+      SAE[2] += (float)(s.E * nmc::kUnfix);
+    }
+    return NMC_OK;
+  }
+  if ((st = add_f(F3D, h->d_F3D, h->nvox, false)) != NMC_OK) return st;
+  if ((st = add_f(Rd, h->d_slots, h->nslots, false)) != NMC_OK) return st;
+  if ((st = add_f(Rd2D, h->d_Rd2D, h->n2d, false)) != NMC_OK) return st;
+  if (h->sim == NMC_SIM_MCXYZ)
+    if ((st = add_f(reinterpret_cast<float*>(DetPhot2D), h->d_Det, h->n2d, true)) != NMC_OK) return st;
+  return NMC_OK;
+}
+
+nmc_status nmc_get_summary(nmc_handle* h, nmc_summary* out) {
+  if (!h || !out) return fail(h, NMC_EINVAL, "null argument");
+  std::memset(out, 0, sizeof *out);
+  if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
+  nmc_status st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  DevSums s;
+  NMC_CUDA(h, cudaMemcpy(&s, h->d_sums, sizeof s, cudaMemcpyDeviceToHost));
+  out->photons = s.photons;
+  out->substeps = s.substeps;
+  out->scatters = s.scatters;
+  out->S = s.S * nmc::kUnfix;
+  out->A = s.A * nmc::kUnfix;
+  out->E = s.E * nmc::kUnfix;
+  out->rd_sum = s.rd * nmc::kUnfix;
+  out->rd_sumsq = s.rd_sumsq;
+  out->kernel_ms = h->kernel_ms;
+  out->launches = h->launches;
+  out->device_flags = s.flags;
+  return NMC_OK;
+}
+
+void* nmc_stream(nmc_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+const char* nmc_last_error(const nmc_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+void nmc_destroy(nmc_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_buffers(h);
+  if (h->d_sums) cudaFree(h->d_sums);
+  for (EventPair& p : h->pool) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (EventPair& p : h->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+}  // extern "C"

@@ -1,0 +1,195 @@
+"""Python face of the engine: a ctypes wrapper over include/nmc_abi.h.
+
+``Engine`` mirrors the reference's host class (NMC/NMCCode/MetalMC.h:25-31):
+
+    MetalMC initWithDevice:kernel_type  -> Engine(sim_type, device)
+    prepareData: run_params tiss v      -> Engine.prepare_data(rp, tp, v)
+    setNumRunsSeed:                     -> Engine.set_num_runs_seed(run, seed)
+    sendComputeCommand                  -> Engine.send_compute_command()
+    getComputeResults: (16 arrays)      -> Engine.get_compute_results(...)
+
+plus whole-job calls (``run``, ``summary``, ``tally``).  There is no CPU
+fallback: constructing an Engine without the built library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "libnmc_gb300.so")
+
+_lib = None
+_P = C.c_void_p
+
+
+class NMCError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{abi.STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def lib() -> C.CDLL:
+    """The loaded engine library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FileNotFoundError(
+                f"engine library {LIB_PATH} is missing; build it with `python -m nmc_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        H = C.c_void_p
+        L.nmc_ext_defaults.argtypes = [C.POINTER(abi.Ext)]
+        L.nmc_abi_version.restype = C.c_int32
+        L.nmc_create.argtypes = [C.c_int32, C.c_int32, C.POINTER(H)]
+        L.nmc_prepare.argtypes = [H, C.POINTER(abi.RunParams), C.POINTER(abi.TissueParams), _P]
+        L.nmc_set_ext.argtypes = [H, C.POINTER(abi.Ext)]
+        L.nmc_set_num_runs_seed.argtypes = [H, C.c_int32, C.c_float]
+        L.nmc_send_compute_command.argtypes = [H]
+        L.nmc_run.argtypes = [H, C.c_uint64, C.c_uint64]
+        L.nmc_run_async.argtypes = [H, C.c_uint64, C.c_uint64]
+        L.nmc_synchronize.argtypes = [H]
+        L.nmc_run_traced.argtypes = [H, C.c_uint64, C.c_uint64, _P, _P, C.c_uint32]
+        L.nmc_get_compute_results.argtypes = [H] + [_P] * 16
+        L.nmc_get_summary.argtypes = [H, C.POINTER(abi.Summary)]
+        L.nmc_get_tally_f64.argtypes = [H, C.c_int32, _P, C.c_size_t]
+        L.nmc_tally_size.argtypes = [H, C.c_int32]
+        L.nmc_tally_size.restype = C.c_size_t
+        L.nmc_reset.argtypes = [H]
+        L.nmc_stream.argtypes = [H]
+        L.nmc_stream.restype = C.c_void_p
+        L.nmc_last_error.argtypes = [H]
+        L.nmc_last_error.restype = C.c_char_p
+        L.nmc_destroy.argtypes = [H]
+        L.nmc_probe_issue_peaks.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        for name in ("nmc_create", "nmc_prepare", "nmc_set_ext", "nmc_set_num_runs_seed",
+                     "nmc_send_compute_command", "nmc_run", "nmc_run_async", "nmc_synchronize",
+                     "nmc_run_traced", "nmc_get_compute_results", "nmc_get_summary",
+                     "nmc_get_tally_f64", "nmc_reset"):
+            getattr(L, name).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+def probe_issue_peaks(device: int = 0) -> tuple[float, float]:
+    """Measured FP32 FMA lanes/s and MUFU lanes/s of `device`."""
+    f, m = C.c_double(), C.c_double()
+    st = lib().nmc_probe_issue_peaks(int(device), C.byref(f), C.byref(m))
+    if st != 0:
+        raise NMCError(st, "nmc_probe_issue_peaks")
+    return f.value, m.value
+
+
+class Engine:
+    """One simulation handle on one GPU (not thread-safe; one per host thread)."""
+
+    def __init__(self, sim_type: int, device: int = 0, ext: abi.Ext | None = None):
+        self._L = lib()
+        self._h = C.c_void_p()
+        st = self._L.nmc_create(int(sim_type), int(device), C.byref(self._h))
+        if st != 0:
+            raise NMCError(st, f"nmc_create(sim_type={sim_type}, device={device})")
+        self.sim_type = int(sim_type)
+        self.ext = ext or abi.ext_defaults()
+        self._check(self._L.nmc_set_ext(self._h, C.byref(self.ext)), "nmc_set_ext")
+        self.rp: abi.RunParams | None = None
+
+    # -- plumbing
+    def _check(self, st: int, what: str):
+        if st != 0:
+            msg = self._L.nmc_last_error(self._h) if self._h else b""
+            raise NMCError(st, f"{what}: {msg.decode(errors='replace') if msg else ''}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.nmc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- reference lifecycle
+    def set_ext(self, ext: abi.Ext):
+        self.ext = ext
+        self._check(self._L.nmc_set_ext(self._h, C.byref(ext)), "nmc_set_ext")
+
+    def prepare_data(self, rp: abi.RunParams, tp: abi.TissueParams, v=None):
+        self.rp = rp
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.uint8).ravel()
+        self._check(self._L.nmc_prepare(self._h, C.byref(rp), C.byref(tp), _ptr(vv)), "nmc_prepare")
+
+    def set_num_runs_seed(self, run: int, time_seed: float = 0.0):
+        self._check(self._L.nmc_set_num_runs_seed(self._h, int(run), float(time_seed)), "nmc_set_num_runs_seed")
+
+    def send_compute_command(self):
+        self._check(self._L.nmc_send_compute_command(self._h), "nmc_send_compute_command")
+
+    def get_compute_results(self) -> dict:
+        """Reference-layout float arrays (getComputeResults, MetalMC.m:508-824)."""
+        out: dict = {}
+        J = F = F3D = SAE = Rd = Rd2D = Det = None
+        if self.sim_type == abi.SIM_MCSUB:
+            b = self.ext.sub_bins
+            J = out["J"] = np.zeros(b + 1, np.float32)
+            F = out["F"] = np.zeros((b + 1) * (b + 1), np.float32)
+            SAE = out["SAE"] = np.zeros(3, np.float32)
+        else:
+            rp = self.rp
+            F3D = out["F3D"] = np.zeros(rp.Nx * rp.Ny * rp.Nz, np.float32)
+            Rd = out["Rd"] = np.zeros(self.ext.photons_per_dispatch, np.float32)
+            Rd2D = out["Rd2D"] = np.zeros(rp.Nx * rp.Ny, np.float32)
+            Det = out["DetPhot2D"] = np.zeros(rp.Nx * rp.Ny, np.int32)
+        args = [J, F, F3D, SAE, Rd, Rd2D, Det] + [None] * 9
+        self._check(self._L.nmc_get_compute_results(self._h, *[_ptr(a) for a in args]),
+                    "nmc_get_compute_results")
+        return out
+
+    # -- whole-job calls
+    def run(self, first: int, n: int):
+        self._check(self._L.nmc_run(self._h, int(first), int(n)), "nmc_run")
+
+    def run_async(self, first: int, n: int):
+        self._check(self._L.nmc_run_async(self._h, int(first), int(n)), "nmc_run_async")
+
+    def synchronize(self):
+        self._check(self._L.nmc_synchronize(self._h), "nmc_synchronize")
+
+    def run_traced(self, first: int, n: int, k_events: int = 0):
+        recs = np.zeros(n, abi.PHOTON_RECORD_DTYPE)
+        ev = np.zeros((n, k_events, 4), np.float32) if k_events else None
+        self._check(self._L.nmc_run_traced(self._h, int(first), int(n), _ptr(recs), _ptr(ev), int(k_events)),
+                    "nmc_run_traced")
+        return recs, ev
+
+    def summary(self) -> dict:
+        s = abi.Summary()
+        self._check(self._L.nmc_get_summary(self._h, C.byref(s)), "nmc_get_summary")
+        return {k: getattr(s, k) for k, _ in abi.Summary._fields_}
+
+    def tally(self, which: int) -> np.ndarray:
+        n = self._L.nmc_tally_size(self._h, int(which))
+        out = np.zeros(n, np.float64)
+        self._check(self._L.nmc_get_tally_f64(self._h, int(which), _ptr(out), n), "nmc_get_tally_f64")
+        return out
+
+    def reset(self):
+        self._check(self._L.nmc_reset(self._h), "nmc_reset")
+
+    @property
+    def stream(self) -> int:
+        return self._L.nmc_stream(self._h) or 0

@@ -1,0 +1,101 @@
+"""Shared simulation set-ups for the tests and the benchmark.
+
+Geometries follow the reference's sample notebooks (NMC-samples/example0.ipynb
+cells 2-4: homogeneous cube; example2.ipynb cells 3-4: skin with a blood
+vessel) and the workload list the benchmark quotes (mcsub semi-infinite
+medium; 200^3 skin-vessel voxel grid).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from nmc_gb300 import abi
+
+# Tissue ids of the skin-vessel map (index 0 unused, mcio.h:128)
+AIR, EPIDERMIS, DERMIS, BLOOD = 1, 2, 3, 4
+
+
+def mcsub_case(g: float = 0.9, phase: int = abi.PHASE_HG, rng: int = abi.RNG_PHILOX, seed: int = 0,
+               bins: int = 101, dr: float = 0.01, dz: float = 0.01, mua: float = 1.0, mus: float = 100.0,
+               n1: float = 1.37, n2: float = 1.0, tt=None):
+    """Semi-infinite medium, normal pencil beam: mua=1, mus=100 /cm, g=0.9,
+    n 1.37/1.0, Rd(r) 100 bins + overflow of 0.01 cm, F(r,z) 100x100 of 0.01 cm."""
+    rp = abi.run_params(myname="mcsub", n1=n1, n2=n2, mckernelflag=abi.SIM_MCSUB, Nt=1)
+    kw = {}
+    if tt is not None:
+        gf, af, gb, ab, cc = tt
+        kw = dict(gf=[gf], af=[af], gb=[gb], ab=[ab], cc=[cc])
+    tp = abi.tissue_params(mua=[mua], mus=[mus], g=[g], **kw)
+    ext = abi.ext_defaults(rng=rng, seed=seed, phase=phase, sub_bins=bins, sub_dr=dr, sub_dz=dz)
+    return rp, tp, ext
+
+
+def homogeneous_case(N: int = 200, d: float = 0.02, rng: int = abi.RNG_PHILOX, seed: int = 0):
+    """example0.ipynb cells 2-4: homogeneous cube, uniform beam r=1.2,
+    mua=1, mus=100, g=0.9, n 1.4/1.001, boundaryflag 2, zsurf=0."""
+    rp = abi.run_params(myname="test", Nx=N, Ny=N, Nz=N, dx=d, dy=d, dz=d, mcflag=0, launchflag=0,
+                        boundaryflag=2, xs=0.0, ys=0.0, zs=0.0, xfocus=0.0, yfocus=0.0, zfocus=1e12,
+                        ux0=0.7, uy0=0.4, uz0=math.sqrt(1 - 0.49 - 0.16), radius=1.2, waist=1.2,
+                        zsurf=0.0, det_radius=5.0, xd=0.0, n1=1.4, n2=1.001, na=90.0, det_state=0,
+                        mckernelflag=abi.SIM_MCXYZ, Nt=1)
+    tp = abi.tissue_params(mua=[1.0], mus=[100.0], g=[0.9])
+    v = np.ones(N * N * N, np.uint8)
+    ext = abi.ext_defaults(rng=rng, seed=seed)
+    return rp, tp, v, ext
+
+
+def skin_vessel_map(N: int = 200, d: float = 0.005, zsurf: float = 0.01, epi: float = 0.006,
+                    vessel_z: float = 0.05, vessel_r: float = 0.01, Ny: int | None = None,
+                    Nz: int | None = None) -> np.ndarray:
+    """uint8 tissue map, index iz*Ny*Nx + ix*Ny + iy (kernels.metal:482).
+    Air above zsurf, one epidermis layer of thickness `epi` below it (rounded
+    to voxels as example2.ipynb cell 4 does), dermis below, and a blood
+    vessel cylinder along x of radius vessel_r centred at depth vessel_z."""
+    Nx = N
+    Ny = Ny or N
+    Nz = Nz or N
+    T = np.full((Nz, Nx, Ny), DERMIS, np.uint8)  # [iz, ix, iy]
+    n_air = int(round(zsurf / d))
+    T[:n_air] = AIR
+    e1 = int(round(zsurf / d)) + 1
+    e2 = min(int(round((zsurf + epi) / d)), Nz)
+    if e2 >= e1:
+        T[e1 - 1:e2] = EPIDERMIS
+    yc = (np.arange(Ny) + 0.5 - Ny / 2.0) * d
+    zc = (np.arange(Nz) + 0.5) * d
+    inside = (yc[None, :] ** 2 + (zc[:, None] - vessel_z) ** 2) <= vessel_r ** 2  # [iz, iy]
+    for iz in range(Nz):
+        T[iz][:, inside[iz]] = BLOOD
+    return T.reshape(-1)
+
+
+def skin_vessel_case(N: int = 200, d: float = 0.005, rng: int = abi.RNG_PHILOX, seed: int = 0,
+                     n2: float = 1.0, tissue_n: float = 1.37):
+    """Skin-vessel workload: 200^3 @ 0.005 cm, air 0.01 cm, epidermis 0.006 cm
+    (mua 20, mus 300, g 0.9), dermis (mua 0.5, mus 200, g 0.9), vessel along x
+    r 0.01 cm at depth 0.05 cm (mua 230, mus 200, g 0.9), n = 1.37; uniform
+    collimated beam r = 0.03 cm launched just below zsurf (example2.ipynb
+    cell 3: zs = zsurf + 1e-4), boundaryflag 2, detector accepting all exits."""
+    zsurf = 0.01
+    rp = abi.run_params(myname="skinvessel", Nx=N, Ny=N, Nz=N, dx=d, dy=d, dz=d, mcflag=0, launchflag=0,
+                        boundaryflag=2, xs=0.0, ys=0.0, zs=zsurf + 0.0001, xfocus=0.0, yfocus=0.0,
+                        zfocus=float("inf"), ux0=0.7, uy0=0.4, uz0=math.sqrt(1 - 0.49 - 0.16),
+                        radius=0.03, waist=0.03, zsurf=zsurf, det_radius=15.0, xd=0.0,
+                        n1=tissue_n, n2=n2, na=90.0, det_state=0, mckernelflag=abi.SIM_MCXYZ, Nt=4)
+    tp = abi.tissue_params(mua=[0.0001, 20.0, 0.5, 230.0], mus=[1.0, 300.0, 200.0, 200.0],
+                           g=[1.0, 0.9, 0.9, 0.9])
+    v = skin_vessel_map(N, d, zsurf)
+    ext = abi.ext_defaults(rng=rng, seed=seed)
+    return rp, tp, v, ext
+
+
+def match_fraction(a, b, rel=1e-3, abs_=1e-6, fields=("detected", "absorbed")):
+    """Fraction of photons whose fate, SPIN count and weight fields agree."""
+    ok = (a["fate"] == b["fate"]) & (a["n_scatt"] == b["n_scatt"])
+    for f in fields:
+        x = a[f].astype(np.float64)
+        y = b[f].astype(np.float64)
+        ok &= np.abs(x - y) <= abs_ + rel * np.maximum(np.abs(x), np.abs(y))
+    return float(np.mean(ok)), ok

@@ -1,0 +1,78 @@
+"""The C ABI without a GPU: struct layouts, exported symbols, error paths."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from nmc_gb300 import abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_functions():
+    src = open(os.path.join(ROOT, "include", "nmc_abi.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(nmc_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_struct_layouts_match_reference_sizes():
+    assert C.sizeof(abi.RunParams) == 172
+    assert C.sizeof(abi.TissueParams) == 608
+    assert abi.RunParams.myname.offset == 0
+    assert abi.RunParams.n1.offset == 96
+    assert abi.RunParams.det_state.offset == 116
+    assert abi.RunParams.Nx.offset == 136
+    assert abi.RunParams.mckernelflag.offset == 168
+
+
+def test_struct_layouts_match_reference_compiler_layout(oracle):
+    if not oracle.ref_available():
+        pytest.skip("reference sources not present on this machine")
+    lib = oracle.ref_lib()
+    assert lib.ref_sizeof_runparams() == C.sizeof(abi.RunParams)
+    assert lib.ref_sizeof_tissueparams() == C.sizeof(abi.TissueParams)
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    L = engine_lib.lib()
+    names = _declared_functions()
+    assert "nmc_create" in names and "nmc_get_compute_results" in names
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    assert L.nmc_abi_version() == 1
+
+
+def test_ext_defaults_match_reference_constants(engine_lib):
+    L = engine_lib.lib()
+    e = abi.Ext()
+    L.nmc_ext_defaults(C.byref(e))
+    assert e.size == C.sizeof(abi.Ext)
+    assert e.photons_per_dispatch == 10000 and e.photons_total == 100000  # definitions.h:16-17
+    assert e.sub_bins == 101 and abs(e.sub_dr - 0.002) < 1e-9  # definitions.h:31,52
+    assert e.sub_boundaryflag == 1 and e.sub_mcflag == 0
+    py = abi.ext_defaults()
+    for name, _ in abi.Ext._fields_:
+        if name in ("reserved",):
+            continue
+        assert getattr(e, name) == pytest.approx(getattr(py, name)), name
+
+
+def test_create_reports_missing_device_or_unsupported_kind(engine_lib):
+    L = engine_lib.lib()
+    h = C.c_void_p()
+    # empty reference kernels (kernels.metal:1122-1202) are not offered
+    assert L.nmc_create(abi.SIM_POLARIZATION_CBS_ELECTRIC_FIELDS, 0, C.byref(h)) == 7
+    assert L.nmc_create(abi.SIM_RAMAN, 0, C.byref(h)) == 7
+    assert L.nmc_create(42, 0, C.byref(h)) == 1
+    st = L.nmc_create(abi.SIM_MCXYZ, 10_000, C.byref(h))
+    assert st == 3  # NMC_EDEVICE: no such device
+    assert not h.value
+
+
+def test_null_handle_calls_do_not_crash(engine_lib):
+    L = engine_lib.lib()
+    assert L.nmc_run(None, 0, 1) == 1
+    assert L.nmc_reset(None) == 1
+    assert L.nmc_last_error(None) == b"null handle"
+    L.nmc_destroy(None)

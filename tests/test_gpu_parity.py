@@ -1,0 +1,134 @@
+"""GPU parity: the CUDA kernels against the FP64 oracle on the same photon
+streams (per photon and per tally), through the C ABI.
+
+Tolerances:
+ * per-photon match = same fate and SPIN count, detected and absorbed weight
+   within 1e-3 relative (+1e-6 absolute); FP32 stepping against FP64
+   arithmetic flips a boundary decision now and then, so a stated fraction
+   of photons must match, not all;
+ * tallies agree within 3 combined standard errors (batch means).
+"""
+import numpy as np
+import pytest
+
+from nmc_gb300 import abi
+import nmc_cases as cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine(gpu, sim, rp, tp, v, ext):
+    e = gpu.Engine(sim, 0, ext)
+    e.prepare_data(rp, tp, v)
+    return e
+
+
+def test_mcsub_reference_rng_per_photon(gpu, oracle):
+    """Reference generator and isotropic sampling (kernels.metal:252): the GPU
+    replays the reference's own photon streams."""
+    rp, tp, ext = cases.mcsub_case(phase=abi.PHASE_ISOTROPIC_REF, rng=abi.RNG_TAUS_REF, dr=0.002, dz=0.002)
+    n = 20000
+    e = _engine(gpu, abi.SIM_MCSUB, rp, tp, None, ext)
+    recs, _ = e.run_traced(0, n)
+    o = oracle.run(abi.SIM_MCSUB, rp, tp, ext=ext, n=n, trace=True)
+    frac, _ = cases.match_fraction(recs, o["recs"], fields=("detected", "absorbed"))
+    print(f"mcsub taus per-photon match {frac:.5f}")
+    assert frac >= 0.99
+    s = e.summary()
+    assert s["photons"] == n
+    assert abs(s["S"] + s["A"] + s["E"] - n) / n < 1e-4  # weight conservation (roulette: in expectation)
+
+
+def test_mcsub_hg_philox_per_photon_and_tallies(gpu, oracle):
+    rp, tp, ext = cases.mcsub_case()
+    n = 20000
+    e = _engine(gpu, abi.SIM_MCSUB, rp, tp, None, ext)
+    recs, ev = e.run_traced(0, n, k_events=8)
+    o = oracle.run(abi.SIM_MCSUB, rp, tp, ext=ext, n=n, trace=True, k_events=8)
+    frac, _ = cases.match_fraction(recs, o["recs"])
+    d = np.abs(ev - o["events"])
+    ev_ok = np.nanmax(d[..., :3], axis=(1, 2)) <= 1e-4
+    print(f"mcsub HG philox per-photon match {frac:.5f}; first-8-events match {np.mean(ev_ok):.5f}")
+    assert frac >= 0.98
+    assert np.mean(ev_ok) >= 0.99
+    J = e.tally(abi.TALLY_J)
+    F = e.tally(abi.TALLY_F)
+    assert abs(J.sum() - o["J"].sum()) <= 1e-3 * o["J"].sum()
+    assert abs(F.sum() - o["F"].sum()) <= 1e-3 * o["F"].sum()
+
+
+def test_mcsub_tallies_within_3_sigma(gpu, oracle):
+    rp, tp, ext = cases.mcsub_case()
+    n_gpu, n_cpu = 1_000_000, 200_000
+    e = _engine(gpu, abi.SIM_MCSUB, rp, tp, None, ext)
+    e.run(10_000_000, n_gpu)
+    s = e.summary()
+    o = oracle.run(abi.SIM_MCSUB, rp, tp, ext=ext, first=0, n=n_cpu)
+    for key, g, c, gs, cs in (("Rd", s["rd_sum"], o["rd_sum"], s["rd_sumsq"], o["rd_sumsq"]),):
+        mg, mc = g / n_gpu, c / n_cpu
+        se = np.sqrt((gs / n_gpu - mg ** 2) / n_gpu + (cs / n_cpu - mc ** 2) / n_cpu)
+        print(f"{key}: gpu {mg:.6f} oracle {mc:.6f} z={(mg - mc) / se:.2f}")
+        assert abs(mg - mc) <= 3 * se
+    assert abs(s["S"] + s["A"] + s["E"] - n_gpu) / n_gpu < 1e-4
+
+
+def test_mcxyz_skin_vessel_per_photon(gpu, oracle):
+    rp, tp, v, ext = cases.skin_vessel_case(N=48)
+    n = 4000
+    e = _engine(gpu, abi.SIM_MCXYZ, rp, tp, v, ext)
+    recs, ev = e.run_traced(0, n, k_events=16)
+    o = oracle.run(abi.SIM_MCXYZ, rp, tp, v, ext=ext, n=n, trace=True, k_events=16)
+    frac, _ = cases.match_fraction(recs, o["recs"])
+    d = np.abs(ev - o["events"])[..., :3]
+    prefix_ok = np.all(np.where(np.isnan(d), True, d <= 1e-4), axis=2)
+    first16 = np.mean(np.all(prefix_ok, axis=1))
+    print(f"mcxyz skin-vessel per-photon match {frac:.4f}; first-16-events match {first16:.4f}; "
+          f"substeps/photon gpu {recs['n_sub'].mean():.1f} oracle {o['recs']['n_sub'].mean():.1f}")
+    assert frac >= 0.80
+    assert first16 >= 0.90
+
+
+def test_mcxyz_skin_vessel_tallies_3_sigma(gpu, oracle):
+    rp, tp, v, ext = cases.skin_vessel_case(N=64)
+    n_gpu, n_cpu = 200_000, 40_000
+    e = _engine(gpu, abi.SIM_MCXYZ, rp, tp, v, ext)
+    e.run(1_000_000, n_gpu)
+    s = e.summary()
+    o = oracle.run(abi.SIM_MCXYZ, rp, tp, v, ext=ext, first=0, n=n_cpu)
+    mg, mc = s["rd_sum"] / n_gpu, o["rd_sum"] / n_cpu
+    se = np.sqrt((s["rd_sumsq"] / n_gpu - mg ** 2) / n_gpu + (o["rd_sumsq"] / n_cpu - mc ** 2) / n_cpu)
+    print(f"Rd gpu {mg:.6f} oracle {mc:.6f} z={(mg - mc) / se:.2f}; substeps/photon gpu "
+          f"{s['substeps'] / n_gpu:.1f} oracle {o['substeps'] / n_cpu:.1f}")
+    assert abs(mg - mc) <= 3 * se
+    F = e.tally(abi.TALLY_F3D)
+    ag, ac = F.sum() / n_gpu, o["F3D"].sum() / n_cpu
+    assert abs(ag - ac) <= 0.02 * ac
+    assert abs(s["A"] / n_gpu - o["A"] / n_cpu) <= 0.02 * (o["A"] / n_cpu)
+
+
+def test_mcxyz_two_term_per_photon(gpu, oracle):
+    rp, tp, v, ext = cases.skin_vessel_case(N=40)
+    rp.mckernelflag = abi.SIM_MCXYZ_TT
+    rp.boundaryflag = 1
+    for t in range(1, 5):
+        tp.gf[t], tp.af[t], tp.gb[t], tp.ab[t], tp.CC[t] = 0.9, 0.5, 0.3, 0.5, 0.9
+    n = 3000
+    e = _engine(gpu, abi.SIM_MCXYZ_TT, rp, tp, v, ext)
+    recs, _ = e.run_traced(0, n)
+    o = oracle.run(abi.SIM_MCXYZ_TT, rp, tp, v, ext=ext, n=n, trace=True)
+    frac, _ = cases.match_fraction(recs, o["recs"])
+    print(f"mcxyz two-term per-photon match {frac:.4f}")
+    assert frac >= 0.75
+
+
+def test_tallies_bit_reproducible(gpu):
+    rp, tp, v, ext = cases.skin_vessel_case(N=48)
+    out = []
+    for _ in range(2):
+        e = _engine(gpu, abi.SIM_MCXYZ, rp, tp, v, ext)
+        e.run(0, 50_000)
+        out.append((e.tally(abi.TALLY_F3D), e.tally(abi.TALLY_RD2D), e.summary()["rd_sum"]))
+        e.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
