@@ -7,6 +7,7 @@
 #pragma once
 
 #include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
 #include <cstdint>
 
 #include "nmc_abi.h"
@@ -294,15 +295,16 @@ __device__ __forceinline__ unsigned long long next_photon(unsigned long long* co
   return base + g.thread_rank();
 }
 
-// Sums a per-thread u64 over the warp, then one atomic per warp.
+// Sums a per-thread value over the threads of the warp that are here
+// together (any subset), then one atomic per group.
 __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, unsigned long long v) {
   cg::coalesced_group g = cg::coalesced_threads();
-  for (int o = 16; o > 0; o >>= 1) v += g.shfl_down(v, o);
+  v = cg::reduce(g, v, cg::plus<unsigned long long>());
   if (g.thread_rank() == 0 && v) atomicAdd(dst, v);
 }
 __device__ __forceinline__ void warp_add_f64(double* dst, double v) {
   cg::coalesced_group g = cg::coalesced_threads();
-  for (int o = 16; o > 0; o >>= 1) v += g.shfl_down(v, o);
+  v = cg::reduce(g, v, cg::plus<double>());
   if (g.thread_rank() == 0 && v != 0.0) atomicAdd(dst, v);
 }
 
