@@ -317,6 +317,45 @@ void nmc_destroy(nmc_handle* h);
 nmc_status nmc_probe_issue_peaks(int32_t device, double* ffma_lanes_per_s,
                                  double* mufu_lanes_per_s);
 
+/* Largest grid nmc_mcxyz_run_noalloc accepts. */
+#define NMC_NOALLOC_MAX_VOXELS 2097152u /* Nx*Ny*Nz, e.g. 128^3 */
+#define NMC_NOALLOC_MAX_MAP 65536u      /* Nx*Ny, e.g. 256^2 */
+
+/* Voxel transport that allocates no memory.  No counterpart in the
+ * reference.
+ *
+ * For callers that cannot let a library call cudaMalloc: an application
+ * that hands out device memory only from its own pool, a plugin living
+ * inside another runtime's fixed memory budget, or a real-time loop where an
+ * allocation may neither stall nor fail.  The caller owns every buffer it
+ * passes, all on the current device: the uint8 tissue map `d_v`
+ * (Nx*Ny*Nz, index iz*Ny*Nx + ix*Ny + iy) and the outputs `d_F3D`
+ * (Nx*Ny*Nz floats), `d_Rd2D` (Nx*Ny floats, may be NULL), `d_DetPhot2D`
+ * (Nx*Ny counts, may be NULL) and `d_totals` (8 doubles, may be NULL:
+ * photons, sub-steps, SPIN events, absorbed weight, detected weight, sum of
+ * squared detected weight per photon, device flags, 0).  Outputs are
+ * overwritten with the tallies of photons [first_photon, first_photon +
+ * n_photons), unnormalised, exactly as nmc_run followed by
+ * nmc_get_tally_f64 would give them for a fresh handle.  rp->mckernelflag
+ * selects MCXYZ or MCXYZ_TT; `ext` gives the RNG, seed and flags.
+ *
+ * The library's working memory for this call (u64 tallies, photon counter,
+ * totals; about 17 MB) is one fixed array in device memory that every GPU
+ * loading the library holds until the process exits; grids beyond
+ * NMC_NOALLOC_MAX_VOXELS voxels or NMC_NOALLOC_MAX_MAP columns are rejected
+ * with NMC_EINVAL.  Every call reuses that array and clears it first, so
+ * calls whose GPU work overlaps (two streams, two host threads) race and
+ * must be serialised by the caller.  The first call on a device looks up the
+ * array's device address (once per device, with that device current); make
+ * that first call before any stream capture.  The call checks the tissue
+ * map on the GPU and waits on `stream` for that check once, then queues the
+ * transport and the output conversion on `stream` and returns. */
+nmc_status nmc_mcxyz_run_noalloc(const nmc_run_params* rp, const nmc_tissue_params* tp,
+                                 const nmc_ext* ext, const uint8_t* d_v,
+                                 uint64_t first_photon, uint64_t n_photons, float* d_F3D,
+                                 float* d_Rd2D, uint32_t* d_DetPhot2D, double* d_totals,
+                                 void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,262 @@
+// noalloc.cu - voxel transport for callers that cannot allocate device memory.
+//
+// Some hosts own every byte of device memory themselves: an application
+// that sub-allocates from its own memory pool, a plugin process inside a
+// larger runtime with a fixed memory budget, or a real-time loop where an
+// allocation's latency or failure is not allowed.  Such a caller hands over
+// its own device buffers for the inputs and outputs and cannot let the
+// library call cudaMalloc.  nmc_mcxyz_run_noalloc serves it: the working
+// memory the transport needs beyond the caller's buffers (the u64
+// fixed-point tallies, the photon counter and the totals) is one file-scope
+// __device__ array of fixed size, so the call allocates nothing.
+//
+// Costs of that choice, all documented in nmc_abi.h:
+//  * the array (about 17 MB) exists on every GPU that loads this library,
+//    for as long as the process lives;
+//  * grids are limited to NMC_NOALLOC_MAX_VOXELS voxels and
+//    NMC_NOALLOC_MAX_MAP columns (Nx*Ny);
+//  * every call uses the same array: the call clears what must start at
+//    zero, and calls whose GPU work overlaps (e.g. on two streams) race.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "engine.h"
+#include "nmc_abi.h"
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+
+struct NoAllocScratch {
+  unsigned long long F3D[NMC_NOALLOC_MAX_VOXELS];
+  unsigned long long Rd2D[NMC_NOALLOC_MAX_MAP];
+  unsigned int Det[NMC_NOALLOC_MAX_MAP];
+  unsigned long long slot[1];
+  nmc::DevSums sums;
+  unsigned int tissue_mask;
+  unsigned int pad;
+};
+
+static __device__ __align__(256) NoAllocScratch g_scratch;
+
+// Device address of g_scratch, looked up once per device (host code may not
+// use the symbol's name as an address).
+NoAllocScratch* g_scratch_addr[kMaxDevices];
+std::mutex g_scratch_mu;
+
+nmc_status scratch_on(int dev, NoAllocScratch** out) {
+  if (dev < 0 || dev >= kMaxDevices) return NMC_EDEVICE;
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return NMC_EDEVICE;
+    g_scratch_addr[dev] = static_cast<NoAllocScratch*>(p);
+  }
+  *out = g_scratch_addr[dev];
+  return NMC_OK;
+}
+
+// Bit t set for every tissue id t present in the map (ids >= 31 set bit 31).
+__global__ void tissue_mask_kernel(const uint8_t* __restrict__ v, size_t n, unsigned int* mask) {
+  unsigned int m = 0;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const unsigned int t = v[k];
+    m |= t < 31 ? (1u << t) : 0x80000000u;
+  }
+  m = __reduce_or_sync(0xFFFFFFFFu, m);
+  if ((threadIdx.x & 31) == 0 && m) atomicOr(mask, m);
+}
+
+__global__ void finish_kernel(const NoAllocScratch* __restrict__ s, size_t nvox, size_t n2d, float* F3D,
+                              float* Rd2D, uint32_t* Det, double* totals) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  for (size_t k = t0; k < nvox; k += stride) F3D[k] = (float)((double)s->F3D[k] * nmc::kUnfix);
+  for (size_t k = t0; k < n2d; k += stride) {
+    if (Rd2D) Rd2D[k] = (float)((double)s->Rd2D[k] * nmc::kUnfix);
+    if (Det) Det[k] = s->Det[k];
+  }
+  if (t0 == 0 && totals) {
+    totals[0] = (double)s->sums.photons;
+    totals[1] = (double)s->sums.substeps;
+    totals[2] = (double)s->sums.scatters;
+    totals[3] = (double)s->sums.A * nmc::kUnfix;
+    totals[4] = (double)s->sums.rd * nmc::kUnfix;
+    totals[5] = s->sums.rd_sumsq;
+    totals[6] = (double)s->sums.flags;
+    totals[7] = 0.0;
+  }
+}
+
+bool feq(float a, float b) {
+  const float e = b * 1.1920928955078125e-7f * 2.f;
+  return (a >= b - e) && (a <= b + e);
+}
+
+nmc::PhaseConst phase_of(const nmc_tissue_params& tp, int t) {
+  nmc::PhaseConst p{};
+  const double g = tp.gv[t];
+  p.hg_mode = (tp.gv[t] == 0.f) ? 1 : (feq(tp.gv[t], 1.f) ? 2 : 0);
+  if (p.hg_mode == 0) {
+    p.hg_a = (float)(1.0 - g * g);
+    p.hg_b = (float)(1.0 - g);
+    p.hg_c = (float)(2.0 * g);
+    p.hg_d = (float)(1.0 + g * g);
+    p.hg_e = (float)(1.0 / (2.0 * g));
+  }
+  const double gf = tp.gf[t], af = tp.af[t], gb = tp.gb[t], ab = tp.ab[t];
+  p.cc = tp.CC[t];
+  p.f_iso = gf == 0.0;
+  p.b_iso = gb == 0.0;
+  if (!p.f_iso) {
+    p.f_q1e = (float)((1.0 + gf * gf) / (2.0 * gf));
+    p.f_iq2 = (float)(1.0 / std::pow(1.0 - gf, 2.0 * af));
+    p.f_iq3 = (float)(1.0 / std::pow(1.0 + gf, 2.0 * af));
+    p.f_ninva = (float)(-1.0 / af);
+    p.f_e = (float)(1.0 / (2.0 * gf));
+  }
+  if (!p.b_iso) {
+    p.b_q1e = (float)((1.0 + gb * gb) / (2.0 * gb));
+    p.b_iq2 = (float)(1.0 / std::pow(1.0 - gb, 2.0 * ab));
+    p.b_iq3 = (float)(1.0 / std::pow(1.0 + gb, 2.0 * ab));
+    p.b_ninva = (float)(-1.0 / ab);
+    p.b_e = (float)(1.0 / (2.0 * gb));
+  }
+  return p;
+}
+
+}  // namespace
+
+extern "C" nmc_status nmc_mcxyz_run_noalloc(const nmc_run_params* rp, const nmc_tissue_params* tp,
+                                            const nmc_ext* ext, const uint8_t* d_v, uint64_t first_photon,
+                                            uint64_t n_photons, float* d_F3D, float* d_Rd2D,
+                                            uint32_t* d_DetPhot2D, double* d_totals, void* stream) {
+  if (!rp || !tp || !ext || !d_v || !d_F3D) return NMC_EINVAL;
+  if (ext->size != sizeof(nmc_ext) || ext->photons_per_dispatch == 0) return NMC_EINVAL;
+  if (ext->rng != NMC_RNG_PHILOX && ext->rng != NMC_RNG_TAUS_REF) return NMC_EINVAL;
+  if (rp->mckernelflag != NMC_SIM_MCXYZ && rp->mckernelflag != NMC_SIM_MCXYZ_TT) return NMC_EINVAL;
+  if (rp->Nx <= 0 || rp->Ny <= 0 || rp->Nz <= 0) return NMC_EINVAL;
+  const size_t nvox = (size_t)rp->Nx * rp->Ny * rp->Nz, n2d = (size_t)rp->Nx * rp->Ny;
+  if (nvox > NMC_NOALLOC_MAX_VOXELS || n2d > NMC_NOALLOC_MAX_MAP) return NMC_EINVAL;  // grid too large
+  if (!(rp->dx > 0.f) || !(rp->dy > 0.f) || !(rp->dz > 0.f) || !std::isfinite(rp->dx) ||
+      !std::isfinite(rp->dy) || !std::isfinite(rp->dz))
+    return NMC_EINVAL;
+  if (rp->boundaryflag < 0 || rp->boundaryflag > 2 || (rp->det_state != 0 && rp->det_state != 1))
+    return NMC_EINVAL;
+  if (!(rp->n1 > 0.f) || !(rp->n2 > 0.f)) return NMC_EINVAL;
+
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return NMC_EDEVICE;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return NMC_EDEVICE;
+  NoAllocScratch* S = nullptr;
+  nmc_status st = scratch_on(dev, &S);
+  if (st != NMC_OK) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+  // tissue ids must index the 19-entry table and name usable tissues
+  unsigned int mask = 0;
+  if (cudaMemsetAsync(&S->tissue_mask, 0, sizeof(unsigned int), s) != cudaSuccess) return NMC_EDEVICE;
+  tissue_mask_kernel<<<nsm * 4, 256, 0, s>>>(d_v, nvox, &S->tissue_mask);
+  if (cudaMemcpyAsync(&mask, &S->tissue_mask, sizeof mask, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return NMC_EDEVICE;
+  for (int t = 0; t < 32; ++t) {
+    if (!(mask & (1u << t))) continue;
+    if (t >= NMC_NTISS) return NMC_EINVAL;
+    if (!std::isfinite(tp->muav[t]) || tp->muav[t] < 0.f || !(tp->musv[t] > 0.f) ||
+        !std::isfinite(tp->musv[t]) || !std::isfinite(tp->gv[t]))
+      return NMC_EINVAL;
+  }
+
+  // the working memory starts at zero on every call
+  if (cudaMemsetAsync(S->F3D, 0, nvox * sizeof(unsigned long long), s) != cudaSuccess ||
+      cudaMemsetAsync(S->Rd2D, 0, n2d * sizeof(unsigned long long), s) != cudaSuccess ||
+      cudaMemsetAsync(S->Det, 0, n2d * sizeof(unsigned int), s) != cudaSuccess ||
+      cudaMemsetAsync(S->slot, 0, sizeof S->slot, s) != cudaSuccess ||
+      cudaMemsetAsync(&S->sums, 0, sizeof(nmc::DevSums), s) != cudaSuccess)
+    return NMC_EDEVICE;
+
+  if (n_photons > 0) {
+    nmc::XyzParams p{};
+    p.Nx = rp->Nx;
+    p.Ny = rp->Ny;
+    p.Nz = rp->Nz;
+    p.dx = rp->dx;
+    p.dy = rp->dy;
+    p.dz = rp->dz;
+    p.idx = (float)(1.0 / rp->dx);
+    p.idy = (float)(1.0 / rp->dy);
+    p.idz = (float)(1.0 / rp->dz);
+    p.dxmax = std::nextafter(rp->dx, 0.f);
+    p.dymax = std::nextafter(rp->dy, 0.f);
+    p.dzmax = std::nextafter(rp->dz, 0.f);
+    {
+      const double q = std::floor((double)rp->zsurf / (double)rp->dz);
+      double rem = (double)rp->zsurf - q * (double)rp->dz;
+      int k = (int)q;
+      if (rem < 0) { rem += rp->dz; --k; }
+      if (rem >= rp->dz) { rem -= rp->dz; ++k; }
+      p.ksurf = k;
+      p.fsurf = (float)rem >= rp->dz ? p.dzmax : (float)rem;
+    }
+    p.boundaryflag = rp->boundaryflag;
+    p.det_state = rp->det_state;
+    p.launchflag = rp->launchflag;
+    p.mcflag = rp->mcflag;
+    p.xs = rp->xs;
+    p.ys = rp->ys;
+    p.zs = rp->zs;
+    p.ux0 = rp->ux0;
+    p.uy0 = rp->uy0;
+    p.uz0 = rp->uz0;
+    p.radius = rp->radius;
+    p.waist = rp->waist;
+    p.zfocus = rp->zfocus;
+    p.n1 = rp->n1;
+    p.n2 = rp->n2;
+    if (feq(rp->xd, 0.f)) {
+      p.r_min = 0.f;
+      p.r_max = rp->det_radius;
+    } else {
+      p.r_min = rp->xd - rp->det_radius;
+      p.r_max = p.r_min + 2.f * rp->det_radius;
+    }
+    p.na = rp->na;
+    p.det_everything = (p.r_min <= 0.f && std::isinf(p.r_max) && rp->na >= 90.f) ? 1 : 0;
+    p.V = d_v;
+    for (int t = 0; t < NMC_NTISS; ++t) {
+      const float mus = tp->musv[t];
+      p.core[t] = make_float4(tp->muav[t], mus, mus > 0.f ? (float)(1.0 / mus) : 0.f, tp->gv[t]);
+      p.phase[t] = phase_of(*tp, t);
+    }
+    p.flags = ext->flags;
+    p.step_cap = 4000000u;
+    p.F3D = S->F3D;
+    p.Rd2D = S->Rd2D;
+    p.Det2D = S->Det;
+    p.rd_slots = S->slot;
+    p.nslots = 1;
+    p.sums = &S->sums;
+    p.first = first_photon;
+    p.n = n_photons;
+    p.rng.kind = ext->rng;
+    p.rng.k0 = (uint32_t)ext->seed;
+    p.rng.k1 = (uint32_t)(ext->seed >> 32);
+    p.rng.tt_replay =
+        (rp->mckernelflag == NMC_SIM_MCXYZ_TT && (ext->flags & NMC_FLAG_TT_REPLAY_RUN1)) ? 1u : 0u;
+    p.rng.batch = ext->photons_per_dispatch;
+    p.trace = nmc::TraceParams{nullptr, nullptr, 0};
+    const bool tt = rp->mckernelflag == NMC_SIM_MCXYZ_TT;
+    const int block = 256;
+    int per_sm = 0;
+    if (nmc::mcxyz_occupancy(tt, false, block, &per_sm) != cudaSuccess || per_sm < 1) return NMC_EDEVICE;
+    uint64_t grid = (uint64_t)nsm * per_sm;
+    if (grid > (n_photons + block - 1) / block) grid = (n_photons + block - 1) / block;
+    if (nmc::launch_mcxyz(p, tt, false, (int)grid, block, s) != cudaSuccess) return NMC_EDEVICE;
+  }
+  finish_kernel<<<nsm * 4, 256, 0, s>>>(S, nvox, n2d, d_F3D, d_Rd2D, d_DetPhot2D, d_totals);
+  return cudaGetLastError() == cudaSuccess ? NMC_OK : NMC_EDEVICE;
+}

@@ -1,0 +1,76 @@
+"""nmc_mcxyz_run_noalloc: the voxel transport for callers that cannot let a
+library allocate device memory (they own a memory pool or a fixed budget).
+The test plays such a caller: it owns the device buffers and passes them in,
+then checks two calls in a row against the regular entry point (nmc_prepare
++ nmc_run on a fresh handle) for the same photons.
+
+This file is collected last on purpose (test_zz_*).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from nmc_gb300 import abi
+import nmc_cases as cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _bind(lib):
+    f = lib.nmc_mcxyz_run_noalloc
+    f.restype = C.c_int
+    f.argtypes = [C.POINTER(abi.RunParams), C.POINTER(abi.TissueParams), C.POINTER(abi.Ext), C.c_void_p,
+                  C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    return f
+
+
+def test_noalloc_matches_regular_entry_point_twice(gpu):
+    import torch
+
+    run_noalloc = _bind(gpu.lib())
+    rp, tp, v, ext = cases.skin_vessel_case(N=48)
+    nvox, n2d = rp.Nx * rp.Ny * rp.Nz, rp.Nx * rp.Ny
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(0)
+    d_v = torch.from_numpy(v).to(dev)
+    d_F3D = torch.full((nvox,), -1.0, dtype=torch.float32, device=dev)
+    d_Rd2D = torch.full((n2d,), -1.0, dtype=torch.float32, device=dev)
+    d_Det = torch.full((n2d,), -1, dtype=torch.int32, device=dev)
+    d_tot = torch.zeros(8, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    for first, n in ((0, 40_000), (40_000, 25_000)):
+        st = run_noalloc(C.byref(rp), C.byref(tp), C.byref(ext), d_v.data_ptr(), first, n, d_F3D.data_ptr(),
+                         d_Rd2D.data_ptr(), d_Det.data_ptr(), d_tot.data_ptr(), stream.cuda_stream)
+        assert st == 0, abi.STATUS.get(st, st)
+        torch.cuda.synchronize()
+        with gpu.Engine(abi.SIM_MCXYZ, 0, ext) as e:
+            e.prepare_data(rp, tp, v)
+            e.run(first, n)
+            F = e.tally(abi.TALLY_F3D)
+            R = e.tally(abi.TALLY_RD2D)
+            D = e.tally(abi.TALLY_DETPHOT2D)
+            s = e.summary()
+        # same photon streams, same integer tallies: equal up to float rounding
+        np.testing.assert_allclose(d_F3D.cpu().numpy(), F, rtol=1e-6, atol=1e-12)
+        np.testing.assert_allclose(d_Rd2D.cpu().numpy(), R, rtol=1e-6, atol=1e-12)
+        assert np.array_equal(d_Det.cpu().numpy().astype(np.float64), D)
+        tot = d_tot.cpu().numpy()
+        assert tot[0] == n == s["photons"]
+        assert tot[1] == s["substeps"]
+        assert tot[4] == pytest.approx(s["rd_sum"], rel=1e-12)
+        assert tot[3] == pytest.approx(s["A"], rel=1e-12)
+
+
+def test_noalloc_rejects_grids_beyond_its_limit(gpu):
+    import torch
+
+    run_noalloc = _bind(gpu.lib())
+    rp, tp, v, ext = cases.skin_vessel_case(N=8)
+    rp.Nx = rp.Ny = 256
+    rp.Nz = 64  # 256*256*64 = 4,194,304 voxels > NMC_NOALLOC_MAX_VOXELS
+    d = torch.zeros(16, dtype=torch.float32, device="cuda:0")
+    st = run_noalloc(C.byref(rp), C.byref(tp), C.byref(ext), d.data_ptr(), 0, 10, d.data_ptr(), None, None,
+                     None, torch.cuda.current_stream().cuda_stream)
+    assert st == 1  # NMC_EINVAL, before any device work
