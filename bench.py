@@ -170,6 +170,15 @@ def run_ours(args) -> dict:
     for i in range(args.warmup):
         step(i)
         e.synchronize()
+    if args.profile_only:  # the transport launches alone, for ncu captures
+        for i in range(args.steps):
+            step(args.warmup + i)
+            e.synchronize()
+        s = e.summary()
+        e.close()
+        print(json.dumps({"profile_only": True, "photons": s["photons"], "kernel_ms": s["kernel_ms"],
+                          "launches": s["launches"]}))
+        return {}
     e.reset()
     s0 = e.summary()
 
@@ -273,6 +282,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--photons", type=int, default=PHOTONS_PER_STEP)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run only the warm-up and timed transport launches (for ncu)")
     args = ap.parse_args()
     out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if out:

@@ -142,7 +142,10 @@ enum {
    * iRunNum (MetalMC.m:462-473 vs kernels.metal:757-768). */
   NMC_FLAG_TT_REPLAY_RUN1 = 1u << 0,
   /* Disable the mcxyz MIN_VALUE / MAX_SCATT kill (kernels.metal:747). */
-  NMC_FLAG_NO_HARD_KILL = 1u << 1
+  NMC_FLAG_NO_HARD_KILL = 1u << 1,
+  /* Use CUDA's correctly rounded / 1-ulp log, exp, sin/cos, reciprocal and
+   * pow in the photon step instead of the SFU approximations. */
+  NMC_FLAG_PRECISE_MATH = 1u << 2
 };
 
 typedef struct nmc_ext {

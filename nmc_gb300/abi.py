@@ -39,6 +39,7 @@ PHASE_TWO_TERM = 2
 
 FLAG_TT_REPLAY_RUN1 = 1 << 0
 FLAG_NO_HARD_KILL = 1 << 1
+FLAG_PRECISE_MATH = 1 << 2
 
 FATE_ALIVE, FATE_ESCAPED, FATE_ROULETTE, FATE_MINWEIGHT, FATE_MAXSCATT, FATE_BOUNDARY, FATE_STEPCAP = range(7)
 

@@ -18,6 +18,8 @@ struct XyzParams {
   int Nx, Ny, Nz;
   float dx, dy, dz, idx, idy, idz;
   float dxmax, dymax, dzmax;  // largest float below dx, dy, dz
+  int hx, hy, ox, oy;         // Nx/2, Ny/2 rounded down; Nx, Ny odd
+  float hdx, hdy;             // dx/2, dy/2
   int ksurf;                  // zsurf = ksurf * dz + fsurf
   float fsurf;
   int boundaryflag, det_state;
@@ -29,6 +31,7 @@ struct XyzParams {
   float4 core[NMC_NTISS];     // mua, mus, 1/mus, g
   PhaseConst phase[NMC_NTISS];
   uint32_t flags;
+  int fast_math;              // SFU approximations (Math<true>)
   uint32_t step_cap;
   unsigned long long* F3D;
   unsigned long long* Rd2D;
@@ -50,6 +53,7 @@ struct SubParams {
   float radius, waist, zfocus, xs, ys, zs;
   PhaseConst phase;  // tissue 1
   int phase_kind;    // SubPhase
+  int fast_math;
   unsigned long long* J;  // fixed point 2^-32, BINS+1
   unsigned long long* F;  // (BINS+1)^2
   DevSums* sums;
@@ -60,6 +64,14 @@ struct SubParams {
 };
 
 enum SubPhase { kPhaseHG = 0, kPhaseIsoRef = 1, kPhaseTT = 2 };
+
+// Parameter blocks from the reference's configuration (params.cu); device
+// pointers are left for the caller to set.
+PhaseConst phase_const(const nmc_tissue_params& tp, int t);
+RngParams rng_params(const nmc_ext& e, int sim);
+void fill_xyz(XyzParams& p, const nmc_run_params& rp, const nmc_tissue_params& tp, const nmc_ext& e,
+              int sim);
+void fill_sub(SubParams& p, const nmc_run_params& rp, const nmc_tissue_params& tp, const nmc_ext& e);
 
 // Launchers (blocking is up to the caller; all work goes on `stream`).
 cudaError_t launch_mcxyz(const XyzParams& p, bool two_term, bool trace, int grid, int block,

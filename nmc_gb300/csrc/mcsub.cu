@@ -1,8 +1,9 @@
 // mcsub.cu - semi-infinite medium photon transport (MCSubKernel,
 // kernels.metal:59-319) as a persistent CUDA kernel for sm_103a.
 //
-// One loop trip is one HOP-ESCAPE-DROP-SPIN-ROULETTE cycle of one photon.
-// The cylindrical tallies F(r,z) and J(r) are privatised per block in shared
+// One loop trip is one HOP-ESCAPE-DROP-SPIN-ROULETTE cycle of one photon;
+// the SPIN draws and the next hop's step come from one Philox block.  The
+// cylindrical tallies F(r,z) and J(r) are privatised per block in shared
 // memory as 64-bit fixed point held in two 32-bit words (low word atomicAdd,
 // carry into the high word when the add wraps), so every deposit is a
 // shared-memory atomic and the block's copy is folded into the global u64
@@ -25,25 +26,74 @@ __device__ __forceinline__ void smem_add(uint32_t* lo, uint32_t* hi, int k, floa
   if (old + a < old) atomicAdd(hi + k, 1u);
 }
 
-template <int PHASE, class RNG, bool TRACE, bool SMEM>
+template <bool FAST, class D>
+__device__ __forceinline__ void launch_photon(const SubParams& P, D& d, float& x, float& y, float& z,
+                                              float& ux, float& uy, float& uz, float& rsp) {
+  using M = Math<FAST>;
+  rsp = 0.f;
+  x = y = z = 0.f;
+  ux = uy = uz = 0.f;
+  if (P.mcflag == 0) {  // kernels.metal:106-121
+    const float r = d.next();
+    x = P.radius * sqrtf(r);
+    z = P.zs;
+    uz = 1.f;
+    float t = P.n1 / P.n2;
+    t = (1.f - t) / (1.f + t);
+    rsp = t * t;
+  } else if (P.mcflag == 1) {  // :122-147
+    float r;
+    while ((r = d.next()) <= 0.f) {
+    }
+    x = P.radius * sqrtf(-logf(r));
+    z = P.zs;
+    while ((r = d.next()) <= 0.f) {
+    }
+    const float xf = P.waist * sqrtf(-logf(r));
+    const float temp = sqrtf((x - xf) * (x - xf) + P.zfocus * P.zfocus);
+    const float costheta = P.zfocus / temp;
+    ux = -(x - xf) / temp;
+    uz = costheta;
+    float uzn = uz;
+    rsp = rfresnel(P.n2, P.n1, costheta, &uzn);
+    uz = uzn;
+    ux = sqrtf(fmaxf(1.f - uz * uz, 0.f));
+  } else if (P.mcflag == 2) {  // :148-164
+    x = P.xs;
+    y = P.ys;
+    z = P.zs;
+    const float costheta = 1.f - 2.f * d.next();
+    const float sintheta = sqrtf(fmaxf(1.f - costheta * costheta, 0.f));
+    float sp, cp;
+    M::sincos2pi(d.next(), &sp, &cp);
+    ux = sintheta * cp;
+    uy = sintheta * sp;
+    uz = costheta;
+  }
+}
+
+template <int PHASE, class RNG, bool TRACE, bool SMEM, bool FAST>
 __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
+  using M = Math<FAST>;
+  constexpr bool TT = PHASE == kPhaseTT;
   extern __shared__ uint32_t smem[];
+  __shared__ unsigned long long s_tot[6];  // photons, hops, scatters, S, A, E
+  __shared__ double s_rd2;
   const int BINS = P.bins;
   const int nJ = BINS + 1, nF = nJ * nJ;
   uint32_t* Flo = smem;
   uint32_t* Fhi = Flo + nF;
   uint32_t* Jlo = Fhi + nF;
   uint32_t* Jhi = Jlo + nJ;
-  if (SMEM) {
+  if (SMEM)
     for (int k = threadIdx.x; k < 2 * (nF + nJ); k += blockDim.x) smem[k] = 0u;
-    __syncthreads();
-  }
-
-  unsigned long long t_ph = 0, t_sub = 0, t_sc = 0, t_S = 0, t_A = 0, t_E = 0;
-  double t_rd2 = 0.0;
+  if (threadIdx.x < 6) s_tot[threadIdx.x] = 0ull;
+  if (threadIdx.x == 0) s_rd2 = 0.0;
+  __syncthreads();
+  const uint32_t k0 = P.rng.k0, k1 = P.rng.k1;
 
   RNG rng;
-  float x = 0.f, y = 0.f, z = 0.f, ux = 0.f, uy = 0.f, uz = 1.f, W = 0.f;
+  float x = 0.f, y = 0.f, z = 0.f, ux = 0.f, uy = 0.f, uz = 1.f, W = 0.f, step_u = 1.f;
   float rsp = 0.f, Atot = 0.f, E = 0.f;
   uint32_t nsc = 0, nsub = 0, fate = NMC_FATE_ALIVE, ndet = 0, nev = 0;
   unsigned long long pidx = 0;
@@ -52,13 +102,13 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
   while (true) {
     if (!alive) {
       if (have) {
-        t_S += to_fix(rsp);
-        t_A += to_fix(Atot);
-        t_E += to_fix(E);
-        t_rd2 += (double)E * (double)E;
-        t_sub += nsub;
-        t_sc += nsc;
-        ++t_ph;
+        atomicAdd(&s_tot[0], 1ull);
+        atomicAdd(&s_tot[1], (unsigned long long)nsub);
+        atomicAdd(&s_tot[2], (unsigned long long)nsc);
+        atomicAdd(&s_tot[3], to_fix(rsp));
+        atomicAdd(&s_tot[4], to_fix(Atot));
+        atomicAdd(&s_tot[5], to_fix(E));
+        if (E > 0.f) atomicAdd(&s_rd2, (double)E * (double)E);
         if (TRACE) {
           nmc_photon_record r;
           r.n_scatt = nsc;
@@ -80,73 +130,34 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
       const unsigned long long pid = P.first + pidx;
       if constexpr (std::is_same<RNG, TausRng>::value) {
         rng.init_photon(pid, P.rng.batch, false, false);
+        typename TausRng::Seq d{&rng};
+        launch_photon<FAST>(P, d, x, y, z, ux, uy, uz, rsp);
       } else {
-        rng.init(P.rng.k0, P.rng.k1, pid);
+        rng.init(pid);
+        LaunchDraws d{rng.block(0xFFFFFFFFu, k0, k1), 0};
+        launch_photon<FAST>(P, d, x, y, z, ux, uy, uz, rsp);
       }
-      // ---- LAUNCH (kernels.metal:106-168)
-      rsp = 0.f;
-      x = y = z = 0.f;
-      ux = uy = uz = 0.f;
-      if (P.mcflag == 0) {
-        const float r = rng.launch_u();
-        x = P.radius * sqrtf(r);
-        y = 0.f;
-        z = P.zs;
-        uz = 1.f;
-        float t = P.n1 / P.n2;
-        t = (1.f - t) / (1.f + t);
-        rsp = t * t;
-      } else if (P.mcflag == 1) {
-        float r;
-        while ((r = rng.launch_u()) <= 0.f) {
-        }
-        x = P.radius * sqrtf(-logf(r));
-        z = P.zs;
-        while ((r = rng.launch_u()) <= 0.f) {
-        }
-        const float xf = P.waist * sqrtf(-logf(r));
-        const float temp = sqrtf((x - xf) * (x - xf) + P.zfocus * P.zfocus);
-        const float costheta = P.zfocus / temp;
-        ux = -(x - xf) / temp;
-        uz = costheta;
-        float uzn = uz;
-        rsp = rfresnel(P.n2, P.n1, costheta, &uzn);
-        uz = uzn;
-        ux = sqrtf(fmaxf(1.f - uz * uz, 0.f));
-      } else if (P.mcflag == 2) {
-        x = P.xs;
-        y = P.ys;
-        z = P.zs;
-        const float costheta = 1.f - 2.f * rng.launch_u();
-        const float sintheta = sqrtf(fmaxf(1.f - costheta * costheta, 0.f));
-        float sp, cp;
-        sincospif(2.f * rng.launch_u(), &sp, &cp);
-        ux = sintheta * cp;
-        uy = sintheta * sp;
-        uz = costheta;
-      }
-      W = 1.f - rsp;
+      step_u = rng.first_step(k0, k1);
+      W = 1.f - rsp;  // :166-168
       Atot = 0.f;
       E = 0.f;
-      nsc = nsub = ndet = nev = 0;
-      fate = NMC_FATE_ALIVE;
+      nsc = nsub = 0;
+      if (TRACE) {
+        fate = NMC_FATE_ALIVE;
+        ndet = nev = 0;
+      }
       alive = true;
     }
 
     // ---- HOP (:183-187)
-    rng.new_hop();
-    float rnd;
-    while ((rnd = rng.step_u()) <= 0.f) {
-    }
-    const float s = -logf(rnd) / P.mut;
+    const float s = M::div(M::neglog(step_u), P.mut);
     x = fmaf(s, ux, x);
     y = fmaf(s, uy, y);
     z = fmaf(s, uz, z);
     ++nsub;
     if (P.boundaryflag == 1 && z <= P.zs) {  // ESCAPE (:190-214)
-      rnd = rng.fres_u();
       float uz1;
-      if (rnd > rfresnel(P.n1, P.n2, -uz, &uz1)) {
+      if (rng.fres_u(k0, k1) > rfresnel(P.n1, P.n2, -uz, &uz1)) {
         x = fmaf(-s, ux, x);
         y = fmaf(-s, uy, y);
         z = fmaf(-s, uz, z);
@@ -161,8 +172,10 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
         else
           atomicAdd(P.J + ir, to_fix(W));
         E += W;
-        ndet = 1;
-        fate = NMC_FATE_ESCAPED;
+        if (TRACE) {
+          ndet = 1;
+          fate = NMC_FATE_ESCAPED;
+        }
         alive = false;
         continue;
       }
@@ -184,22 +197,23 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
       else
         atomicAdd(P.F + (ir * BINS + iz), to_fix(absorb));
     }
-    // ---- SPIN (:243-279)
+    // ---- SPIN (:243-279), ROULETTE (:289-294), next HOP's draw
+    const bool need_roul = W < kTHRESHOLD;
+    const SpinDraws d = spin_draws<TT>(rng, need_roul, k0, k1);
     float costheta;
-    if (PHASE == kPhaseTT) {
-      costheta = tt_sample(P.phase, rng);
-    } else {
-      const float u = rng.cos_u();
-      costheta = (PHASE == kPhaseIsoRef) ? 2.f * u - 1.f : hg_sample(P.phase, u);
-    }
-    spin(costheta, rng.psi_u(), ux, uy, uz);
+    if (PHASE == kPhaseTT)
+      costheta = tt_sample<FAST>(P.phase, d.a, d.b);
+    else if (PHASE == kPhaseIsoRef)
+      costheta = 2.f * d.a - 1.f;  // kernels.metal:252 overrides the HG sample
+    else
+      costheta = hg_sample<FAST>(P.phase, d.a);
+    spin<FAST>(costheta, TT ? d.c : d.b, ux, uy, uz);
     ++nsc;
-    // ---- ROULETTE (:289-294)
-    if (W < kTHRESHOLD) {
-      if (rng.roul_u() <= kCHANCE)
+    if (need_roul) {
+      if (d.roul <= kCHANCE) {
         W /= kCHANCE;
-      else {
-        fate = NMC_FATE_ROULETTE;
+      } else {
+        if (TRACE) fate = NMC_FATE_ROULETTE;
         alive = false;
       }
     }
@@ -207,24 +221,23 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
       P.trace.events[pidx * P.trace.k_events + nev] = make_float4(x, y, z, W);
       ++nev;
     }
+    step_u = d.step;
     if (alive && nsub >= P.step_cap) {  // device-side cap: not a reference behaviour
-      fate = NMC_FATE_STEPCAP;
+      if (TRACE) fate = NMC_FATE_STEPCAP;
       alive = false;
       atomicOr(&P.sums->flags, (unsigned int)NMC_DEVFLAG_STEPCAP);
     }
   }
 
-  warp_add_u64(&P.sums->photons, t_ph);
-  warp_add_u64(&P.sums->substeps, t_sub);
-  warp_add_u64(&P.sums->scatters, t_sc);
-  warp_add_u64(&P.sums->S, t_S);
-  warp_add_u64(&P.sums->A, t_A);
-  warp_add_u64(&P.sums->E, t_E);
-  warp_add_u64(&P.sums->rd, t_E);
-  warp_add_f64(&P.sums->rd_sumsq, t_rd2);
-
+  __syncthreads();
+  if (threadIdx.x < 6 && s_tot[threadIdx.x]) {
+    unsigned long long* dst[6] = {&P.sums->photons, &P.sums->substeps, &P.sums->scatters,
+                                  &P.sums->S,       &P.sums->A,        &P.sums->E};
+    atomicAdd(dst[threadIdx.x], s_tot[threadIdx.x]);
+    if (threadIdx.x == 5) atomicAdd(&P.sums->rd, s_tot[5]);
+  }
+  if (threadIdx.x == 0 && s_rd2 != 0.0) atomicAdd(&P.sums->rd_sumsq, s_rd2);
   if (SMEM) {  // fold the block's tallies into the global ones (scale 2^31 -> 2^32)
-    __syncthreads();
     for (int k = threadIdx.x; k < nF; k += blockDim.x) {
       const unsigned long long v = ((unsigned long long)Fhi[k] << 32) | Flo[k];
       if (v) atomicAdd(P.F + k, v << 1);
@@ -236,22 +249,23 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
   }
 }
 
-template <int PHASE, bool TRACE, bool SMEM>
+template <int PHASE, bool TRACE, bool SMEM, bool FAST>
 const void* kernel_ptr(uint32_t rng_kind) {
-  if (rng_kind == NMC_RNG_TAUS_REF) return (const void*)mcsub_kernel<PHASE, TausRng, TRACE, SMEM>;
-  return (const void*)mcsub_kernel<PHASE, PhiloxRng<PHASE == kPhaseTT>, TRACE, SMEM>;
+  if (rng_kind == NMC_RNG_TAUS_REF) return (const void*)mcsub_kernel<PHASE, TausRng, TRACE, SMEM, FAST>;
+  return (const void*)mcsub_kernel<PHASE, PhiloxRng<PHASE == kPhaseTT>, TRACE, SMEM, FAST>;
 }
 
-template <int PHASE>
+template <int PHASE, bool FAST>
 const void* pick3(uint32_t rng_kind, bool trace, bool smem) {
-  if (trace) return smem ? kernel_ptr<PHASE, true, true>(rng_kind) : kernel_ptr<PHASE, true, false>(rng_kind);
-  return smem ? kernel_ptr<PHASE, false, true>(rng_kind) : kernel_ptr<PHASE, false, false>(rng_kind);
+  if (trace) return smem ? kernel_ptr<PHASE, true, true, FAST>(rng_kind) : kernel_ptr<PHASE, true, false, FAST>(rng_kind);
+  return smem ? kernel_ptr<PHASE, false, true, FAST>(rng_kind) : kernel_ptr<PHASE, false, false, FAST>(rng_kind);
 }
 
-const void* pick(const SubParams& p, bool trace, bool smem, int phase) {
-  if (phase == kPhaseTT) return pick3<kPhaseTT>(p.rng.kind, trace, smem);
-  if (phase == kPhaseIsoRef) return pick3<kPhaseIsoRef>(p.rng.kind, trace, smem);
-  return pick3<kPhaseHG>(p.rng.kind, trace, smem);
+template <bool FAST>
+const void* pick2(const SubParams& p, bool trace, bool smem) {
+  if (p.phase_kind == kPhaseTT) return pick3<kPhaseTT, FAST>(p.rng.kind, trace, smem);
+  if (p.phase_kind == kPhaseIsoRef) return pick3<kPhaseIsoRef, FAST>(p.rng.kind, trace, smem);
+  return pick3<kPhaseHG, FAST>(p.rng.kind, trace, smem);
 }
 
 }  // namespace
@@ -267,7 +281,7 @@ static bool smem_fits(int bins) { return mcsub_smem_bytes(bins) <= 200 * 1024; }
 
 static cudaError_t prepare(const SubParams& p, bool trace, const void** f, size_t* sh) {
   const bool smem = smem_fits(p.bins);
-  *f = pick(p, trace, smem, p.phase_kind);
+  *f = p.fast_math ? pick2<true>(p, trace, smem) : pick2<false>(p, trace, smem);
   *sh = smem ? mcsub_smem_bytes(p.bins) : 0;
   if (*sh > 48 * 1024)
     return cudaFuncSetAttribute(*f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*sh);

@@ -9,6 +9,7 @@
 #include <cooperative_groups.h>
 #include <cooperative_groups/reduce.h>
 #include <cstdint>
+#include <type_traits>
 
 #include "nmc_abi.h"
 
@@ -59,46 +60,68 @@ __device__ __forceinline__ float u01(uint32_t x) {
   return fmaf((float)(x >> 9), 0x1p-23f, 0x1p-24f);
 }
 
-// Per-photon Philox layout (identical in the oracle):
-//   key     = (seed lo, seed hi)
-//   counter = (photon lo, photon hi, c2, 0x4E4D4321)
-//   c2 = 0xFFFFFFFF launch block; c2 = h main block of hop h;
-//   c2 = h | 0x40000000 aux block of hop h.
-//   HG family: main = (step, cos, psi, roulette), aux = (fresnel)
-//   two-term:  main = (step, choice, sample, psi), aux = (fresnel, roulette)
-// The main block of a hop is generated once at the hop's start, so every
-// thread of a warp refills at the same point of the loop.
-template <bool TT>
-struct PhiloxRng {
-  uint32_t k0, k1, plo, phi, hop, nl;
-  uint4 m, l;
-  __device__ __forceinline__ void init(uint32_t key0, uint32_t key1, uint64_t photon) {
-    k0 = key0;
-    k1 = key1;
-    plo = (uint32_t)photon;
-    phi = (uint32_t)(photon >> 32);
-    hop = 0xFFFFFFFFu;
-    nl = 0;
-    l = philox4x32_10(make_uint4(plo, phi, 0xFFFFFFFFu, kPhiloxTag), k0, k1);
-  }
-  __device__ __forceinline__ float launch_u() {
-    const uint32_t k = nl++;
+// Per-photon Philox layout (identical in the oracle): key = (seed lo, seed
+// hi); counter = (photon lo, photon hi, c2, 0x4E4D4321).  Hops are numbered
+// h = 0, 1, ...; the SPIN that ends hop h-1 and the step of hop h come from
+// one block, so a block is generated and consumed at a single point of the
+// photon loop and no random state stays live across voxel sub-steps:
+//   c2 = 0xFFFFFFFF        launch block, slots in draw order
+//   c2 = h                 w = step of hop h; for h >= 1 x, y, z = SPIN draws
+//                          of the event ending hop h-1: (cos, psi, roulette)
+//                          or, two-term, (choice, sample, psi)
+//   c2 = h | 0x40000000    aux block, made only when used: x = two-term
+//                          roulette of that SPIN, y = Fresnel test of hop h
+// The key words come from the kernel parameters (uniform across the grid).
+struct SpinDraws {
+  float a, b, c;  // HG: cos, psi, roulette; two-term: choice, sample, psi
+  float roul;     // roulette draw (two-term); equal to c for HG
+  float step;     // uniform for the step of the next hop
+};
+
+struct LaunchDraws {
+  uint4 l;
+  uint32_t n;
+  __device__ __forceinline__ float next() {
+    const uint32_t k = n++;
     return u01(k == 0 ? l.x : k == 1 ? l.y : k == 2 ? l.z : l.w);
   }
-  __device__ __forceinline__ void new_hop() {
+};
+
+template <bool TT>
+struct PhiloxRng {
+  uint32_t plo, phi, hop;
+  __device__ __forceinline__ uint4 block(uint32_t c2, uint32_t k0, uint32_t k1) const {
+    return philox4x32_10(make_uint4(plo, phi, c2, kPhiloxTag), k0, k1);
+  }
+  __device__ __forceinline__ void init(uint64_t photon) {
+    plo = (uint32_t)photon;
+    phi = (uint32_t)(photon >> 32);
+    hop = 0;
+  }
+  template <class F>
+  __device__ __forceinline__ void launch(uint32_t k0, uint32_t k1, F&& use) {
+    LaunchDraws d{block(0xFFFFFFFFu, k0, k1), 0};
+    use(d);
+  }
+  __device__ __forceinline__ float first_step(uint32_t k0, uint32_t k1) {
+    hop = 0;
+    return u01(block(0u, k0, k1).w);
+  }
+  __device__ __forceinline__ SpinDraws spin_draws(bool need_roul, uint32_t k0, uint32_t k1) {
     ++hop;
-    m = philox4x32_10(make_uint4(plo, phi, hop, kPhiloxTag), k0, k1);
+    const uint4 b = block(hop, k0, k1);
+    SpinDraws d;
+    d.a = u01(b.x);
+    d.b = u01(b.y);
+    d.c = u01(b.z);
+    d.step = u01(b.w);
+    d.roul = d.c;
+    if (TT && need_roul) d.roul = u01(block(hop | 0x40000000u, k0, k1).x);
+    return d;
   }
-  __device__ __forceinline__ uint4 aux() const {
-    return philox4x32_10(make_uint4(plo, phi, hop | 0x40000000u, kPhiloxTag), k0, k1);
+  __device__ __forceinline__ float fres_u(uint32_t k0, uint32_t k1) const {
+    return u01(block(hop | 0x40000000u, k0, k1).y);
   }
-  __device__ __forceinline__ float step_u() { return u01(m.x); }
-  __device__ __forceinline__ float cos_u() { return u01(m.y); }
-  __device__ __forceinline__ float choice_u() { return u01(m.y); }
-  __device__ __forceinline__ float sample_u() { return u01(m.z); }
-  __device__ __forceinline__ float psi_u() { return u01(TT ? m.w : m.z); }
-  __device__ __forceinline__ float roul_u() { return TT ? u01(aux().y) : u01(m.w); }
-  __device__ __forceinline__ float fres_u() { return u01(aux().x); }
 };
 
 // The reference's generator (helpers.metal:319-371), drawn sequentially in
@@ -148,16 +171,48 @@ struct TausRng {
     s4 = xsh(s4);
     return (float)((s1 ^ s2 ^ s3 ^ s4) >> 8) * (1.0f / 16777216.0f);
   }
-  __device__ __forceinline__ float launch_u() { return next(); }
-  __device__ __forceinline__ void new_hop() {}
-  __device__ __forceinline__ float step_u() { return next(); }
-  __device__ __forceinline__ float cos_u() { return next(); }
-  __device__ __forceinline__ float choice_u() { return next(); }
-  __device__ __forceinline__ float sample_u() { return next(); }
-  __device__ __forceinline__ float psi_u() { return next(); }
-  __device__ __forceinline__ float roul_u() { return next(); }
-  __device__ __forceinline__ float fres_u() { return next(); }
+  // The same interface as PhiloxRng, drawing in the reference's order:
+  // launch draws, then per hop the step (with the `rnd <= 0` retry of
+  // kernels.metal:183,501), the SPIN draws, the roulette draw when W is below
+  // THRESHOLD (:289-290, :740-741).
+  struct Seq {
+    TausRng* g;
+    __device__ __forceinline__ float next() { return g->next(); }
+  };
+  template <class F>
+  __device__ __forceinline__ void launch(uint32_t, uint32_t, F&& use) {
+    Seq s{this};
+    use(s);
+  }
+  __device__ __forceinline__ float step_draw() {
+    float r;
+    while ((r = next()) <= 0.f) {
+    }
+    return r;
+  }
+  __device__ __forceinline__ float first_step(uint32_t, uint32_t) { return step_draw(); }
+  template <bool TT>
+  __device__ __forceinline__ SpinDraws spin_draws_t(bool need_roul) {
+    SpinDraws d;
+    d.a = next();
+    d.b = next();
+    if (TT) d.c = next();
+    d.roul = need_roul ? next() : 1.f;
+    if (!TT) d.c = d.roul;
+    d.step = step_draw();
+    return d;
+  }
+  __device__ __forceinline__ float fres_u(uint32_t, uint32_t) { return next(); }
 };
+
+// Uniform access to the two generators from the kernels.
+template <bool TT, class RNG>
+__device__ __forceinline__ SpinDraws spin_draws(RNG& rng, bool need_roul, uint32_t k0, uint32_t k1) {
+  if constexpr (std::is_same<RNG, TausRng>::value)
+    return rng.template spin_draws_t<TT>(need_roul);
+  else
+    return rng.spin_draws(need_roul, k0, k1);
+}
 
 // ---------------------------------------------------------------- optics
 // FltEq (helpers.metal:21-25) with error = 1.
@@ -213,7 +268,7 @@ __device__ __forceinline__ void snell(float n1, float n2, float& ux, float& uy, 
 // (g == 0), mode 2 = straight ahead (g == 1).
 // Two-term (kernels.metal:1060-1070): per branch q1/(2g), 1/q2, 1/q3,
 // -1/alpha, 1/(2g); iso flag when g == 0.
-struct PhaseConst {
+struct __align__(16) PhaseConst {
   float hg_a, hg_b, hg_c, hg_d, hg_e;
   int hg_mode;
   float cc;
@@ -222,25 +277,47 @@ struct PhaseConst {
   int f_iso, b_iso;
 };
 
+// Arithmetic of the photon step in two accuracy grades.  PRECISE uses
+// CUDA's correctly-rounded or 1-ulp library functions; FAST uses the SFU
+// approximations (MUFU lg2/ex2/sin/cos/rcp, a few ulp).  The grade in use
+// is the one whose per-photon agreement with the FP64 oracle meets the
+// parity tests' bar.
+template <bool FAST>
+struct Math {
+  static __device__ __forceinline__ float neglog(float u) { return FAST ? -__logf(u) : -logf(u); }
+  // weight absorbed over optical depth x: W (1 - e^-x)
+  static __device__ __forceinline__ float absorbed(float W, float x) {
+    return FAST ? W - W * __expf(-x) : -W * expm1f(-x);
+  }
+  static __device__ __forceinline__ float rcp(float x) { return FAST ? __fdividef(1.f, x) : __frcp_rn(x); }
+  static __device__ __forceinline__ float div(float a, float b) { return FAST ? __fdividef(a, b) : a / b; }
+  static __device__ __forceinline__ void sincos2pi(float u, float* s, float* c) {
+    if (FAST)
+      __sincosf(6.2831853071795865f * u, s, c);
+    else
+      sincospif(2.f * u, s, c);
+  }
+  static __device__ __forceinline__ float pow(float x, float y) { return FAST ? __powf(x, y) : powf(x, y); }
+};
+
+template <bool FAST>
 __device__ __forceinline__ float hg_sample(const PhaseConst& p, float u) {
   if (p.hg_mode == 1) return 2.f * u - 1.f;
   if (p.hg_mode == 2) return 1.f;
-  const float t = p.hg_a / fmaf(p.hg_c, u, p.hg_b);
+  const float t = Math<FAST>::div(p.hg_a, fmaf(p.hg_c, u, p.hg_b));
   return fmaf(-t, t, p.hg_d) * p.hg_e;
 }
 
-template <class RNG>
-__device__ __forceinline__ float tt_sample(const PhaseConst& p, RNG& rng) {
-  const float uc = rng.choice_u();
+// Two-term sample from the branch choice and the sample uniform.
+template <bool FAST>
+__device__ __forceinline__ float tt_sample(const PhaseConst& p, float uc, float u) {
   float c;
   if (uc <= p.cc) {
-    const float u = rng.sample_u();
     c = p.f_iso ? 2.f * u - 1.f
-                : p.f_q1e - powf(fmaf(u, p.f_iq2, (1.f - u) * p.f_iq3), p.f_ninva) * p.f_e;
+                : p.f_q1e - Math<FAST>::pow(fmaf(u, p.f_iq2, (1.f - u) * p.f_iq3), p.f_ninva) * p.f_e;
   } else {
-    const float u = rng.sample_u();
     c = p.b_iso ? 2.f * u - 1.f
-                : p.b_q1e - powf(fmaf(u, p.b_iq2, (1.f - u) * p.b_iq3), p.b_ninva) * p.b_e;
+                : p.b_q1e - Math<FAST>::pow(fmaf(u, p.b_iq2, (1.f - u) * p.b_iq3), p.b_ninva) * p.b_e;
     c = -c;
   }
   if (c >= 1.f) c = 1.0f - 1e-9f;
@@ -251,11 +328,12 @@ __device__ __forceinline__ float tt_sample(const PhaseConst& p, RNG& rng) {
 // SPIN (kernels.metal:253-279, :704-730): rotate (ux, uy, uz) by polar
 // cos(theta) and azimuth psi = 2 pi u.  Near |uz| -> 1 the rotation and a
 // renormalisation run in FP64 (1 - uz^2 loses all FP32 bits there).
+template <bool FAST>
 __device__ __forceinline__ void spin(float costheta, float upsi, float& ux, float& uy,
                                      float& uz) {
   const float sintheta = sqrtf(fmaxf(fmaf(-costheta, costheta, 1.f), 0.f));
   float sinpsi, cospsi;
-  sincospif(2.f * upsi, &sinpsi, &cospsi);
+  Math<FAST>::sincos2pi(upsi, &sinpsi, &cospsi);
   const float auz = fabsf(uz);
   if (auz >= 1.f) {  // 1 - |uz| <= 1e-12 in FP32
     ux = sintheta * cospsi;

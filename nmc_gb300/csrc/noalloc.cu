@@ -91,43 +91,6 @@ __global__ void finish_kernel(const NoAllocScratch* __restrict__ s, size_t nvox,
   }
 }
 
-bool feq(float a, float b) {
-  const float e = b * 1.1920928955078125e-7f * 2.f;
-  return (a >= b - e) && (a <= b + e);
-}
-
-nmc::PhaseConst phase_of(const nmc_tissue_params& tp, int t) {
-  nmc::PhaseConst p{};
-  const double g = tp.gv[t];
-  p.hg_mode = (tp.gv[t] == 0.f) ? 1 : (feq(tp.gv[t], 1.f) ? 2 : 0);
-  if (p.hg_mode == 0) {
-    p.hg_a = (float)(1.0 - g * g);
-    p.hg_b = (float)(1.0 - g);
-    p.hg_c = (float)(2.0 * g);
-    p.hg_d = (float)(1.0 + g * g);
-    p.hg_e = (float)(1.0 / (2.0 * g));
-  }
-  const double gf = tp.gf[t], af = tp.af[t], gb = tp.gb[t], ab = tp.ab[t];
-  p.cc = tp.CC[t];
-  p.f_iso = gf == 0.0;
-  p.b_iso = gb == 0.0;
-  if (!p.f_iso) {
-    p.f_q1e = (float)((1.0 + gf * gf) / (2.0 * gf));
-    p.f_iq2 = (float)(1.0 / std::pow(1.0 - gf, 2.0 * af));
-    p.f_iq3 = (float)(1.0 / std::pow(1.0 + gf, 2.0 * af));
-    p.f_ninva = (float)(-1.0 / af);
-    p.f_e = (float)(1.0 / (2.0 * gf));
-  }
-  if (!p.b_iso) {
-    p.b_q1e = (float)((1.0 + gb * gb) / (2.0 * gb));
-    p.b_iq2 = (float)(1.0 / std::pow(1.0 - gb, 2.0 * ab));
-    p.b_iq3 = (float)(1.0 / std::pow(1.0 + gb, 2.0 * ab));
-    p.b_ninva = (float)(-1.0 / ab);
-    p.b_e = (float)(1.0 / (2.0 * gb));
-  }
-  return p;
-}
-
 }  // namespace
 
 extern "C" nmc_status nmc_mcxyz_run_noalloc(const nmc_run_params* rp, const nmc_tissue_params* tp,
@@ -181,59 +144,8 @@ extern "C" nmc_status nmc_mcxyz_run_noalloc(const nmc_run_params* rp, const nmc_
 
   if (n_photons > 0) {
     nmc::XyzParams p{};
-    p.Nx = rp->Nx;
-    p.Ny = rp->Ny;
-    p.Nz = rp->Nz;
-    p.dx = rp->dx;
-    p.dy = rp->dy;
-    p.dz = rp->dz;
-    p.idx = (float)(1.0 / rp->dx);
-    p.idy = (float)(1.0 / rp->dy);
-    p.idz = (float)(1.0 / rp->dz);
-    p.dxmax = std::nextafter(rp->dx, 0.f);
-    p.dymax = std::nextafter(rp->dy, 0.f);
-    p.dzmax = std::nextafter(rp->dz, 0.f);
-    {
-      const double q = std::floor((double)rp->zsurf / (double)rp->dz);
-      double rem = (double)rp->zsurf - q * (double)rp->dz;
-      int k = (int)q;
-      if (rem < 0) { rem += rp->dz; --k; }
-      if (rem >= rp->dz) { rem -= rp->dz; ++k; }
-      p.ksurf = k;
-      p.fsurf = (float)rem >= rp->dz ? p.dzmax : (float)rem;
-    }
-    p.boundaryflag = rp->boundaryflag;
-    p.det_state = rp->det_state;
-    p.launchflag = rp->launchflag;
-    p.mcflag = rp->mcflag;
-    p.xs = rp->xs;
-    p.ys = rp->ys;
-    p.zs = rp->zs;
-    p.ux0 = rp->ux0;
-    p.uy0 = rp->uy0;
-    p.uz0 = rp->uz0;
-    p.radius = rp->radius;
-    p.waist = rp->waist;
-    p.zfocus = rp->zfocus;
-    p.n1 = rp->n1;
-    p.n2 = rp->n2;
-    if (feq(rp->xd, 0.f)) {
-      p.r_min = 0.f;
-      p.r_max = rp->det_radius;
-    } else {
-      p.r_min = rp->xd - rp->det_radius;
-      p.r_max = p.r_min + 2.f * rp->det_radius;
-    }
-    p.na = rp->na;
-    p.det_everything = (p.r_min <= 0.f && std::isinf(p.r_max) && rp->na >= 90.f) ? 1 : 0;
+    nmc::fill_xyz(p, *rp, *tp, *ext, rp->mckernelflag);
     p.V = d_v;
-    for (int t = 0; t < NMC_NTISS; ++t) {
-      const float mus = tp->musv[t];
-      p.core[t] = make_float4(tp->muav[t], mus, mus > 0.f ? (float)(1.0 / mus) : 0.f, tp->gv[t]);
-      p.phase[t] = phase_of(*tp, t);
-    }
-    p.flags = ext->flags;
-    p.step_cap = 4000000u;
     p.F3D = S->F3D;
     p.Rd2D = S->Rd2D;
     p.Det2D = S->Det;
@@ -242,12 +154,6 @@ extern "C" nmc_status nmc_mcxyz_run_noalloc(const nmc_run_params* rp, const nmc_
     p.sums = &S->sums;
     p.first = first_photon;
     p.n = n_photons;
-    p.rng.kind = ext->rng;
-    p.rng.k0 = (uint32_t)ext->seed;
-    p.rng.k1 = (uint32_t)(ext->seed >> 32);
-    p.rng.tt_replay =
-        (rp->mckernelflag == NMC_SIM_MCXYZ_TT && (ext->flags & NMC_FLAG_TT_REPLAY_RUN1)) ? 1u : 0u;
-    p.rng.batch = ext->photons_per_dispatch;
     p.trace = nmc::TraceParams{nullptr, nullptr, 0};
     const bool tt = rp->mckernelflag == NMC_SIM_MCXYZ_TT;
     const int block = 256;

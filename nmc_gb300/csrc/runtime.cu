@@ -101,165 +101,27 @@ void free_buffers(nmc_handle* h) {
 
 bool finite_nonneg(float v) { return std::isfinite(v) && v >= 0.f; }
 
-bool flt_eq_host(float a, float b) {
-  const float e = b * 1.1920928955078125e-7f * 2.f;
-  return (a >= b - e) && (a <= b + e);
-}
-
-// Phase-function constants for one tissue, computed in double.
-nmc::PhaseConst phase_const(const nmc_tissue_params& tp, int t) {
-  nmc::PhaseConst p{};
-  const double g = tp.gv[t];
-  p.hg_mode = (tp.gv[t] == 0.f) ? 1 : (flt_eq_host(tp.gv[t], 1.f) ? 2 : 0);
-  if (p.hg_mode == 0) {
-    p.hg_a = (float)(1.0 - g * g);
-    p.hg_b = (float)(1.0 - g);
-    p.hg_c = (float)(2.0 * g);
-    p.hg_d = (float)(1.0 + g * g);
-    p.hg_e = (float)(1.0 / (2.0 * g));
-  }
-  const double gf = tp.gf[t], af = tp.af[t], gb = tp.gb[t], ab = tp.ab[t];
-  p.cc = tp.CC[t];
-  p.f_iso = gf == 0.0;
-  p.b_iso = gb == 0.0;
-  if (!p.f_iso) {
-    const double q1 = 1.0 + gf * gf, q2 = std::pow(1.0 - gf, 2.0 * af), q3 = std::pow(1.0 + gf, 2.0 * af);
-    p.f_q1e = (float)(q1 / (2.0 * gf));
-    p.f_iq2 = (float)(1.0 / q2);
-    p.f_iq3 = (float)(1.0 / q3);
-    p.f_ninva = (float)(-1.0 / af);
-    p.f_e = (float)(1.0 / (2.0 * gf));
-  }
-  if (!p.b_iso) {
-    const double q1 = 1.0 + gb * gb, q2 = std::pow(1.0 - gb, 2.0 * ab), q3 = std::pow(1.0 + gb, 2.0 * ab);
-    p.b_q1e = (float)(q1 / (2.0 * gb));
-    p.b_iq2 = (float)(1.0 / q2);
-    p.b_iq3 = (float)(1.0 / q3);
-    p.b_ninva = (float)(-1.0 / ab);
-    p.b_e = (float)(1.0 / (2.0 * gb));
-  }
-  return p;
-}
-
-nmc::RngParams rng_params(const nmc_ext& e, int sim) {
-  nmc::RngParams r{};
-  r.kind = e.rng;
-  r.k0 = (uint32_t)e.seed;
-  r.k1 = (uint32_t)(e.seed >> 32);
-  r.tt_replay = (sim == NMC_SIM_MCXYZ_TT && (e.flags & NMC_FLAG_TT_REPLAY_RUN1)) ? 1u : 0u;
-  r.batch = e.photons_per_dispatch;
-  return r;
-}
-
-void lattice_split(float zsurf, float dz, int* k, float* f) {
-  const double q = std::floor((double)zsurf / (double)dz);
-  double rem = (double)zsurf - q * (double)dz;
-  int kk = (int)q;
-  if (rem < 0) {
-    rem += dz;
-    --kk;
-  }
-  if (rem >= dz) {
-    rem -= dz;
-    ++kk;
-  }
-  *k = kk;
-  *f = (float)rem;
-  if (*f >= dz) *f = std::nextafter(dz, 0.f);
-}
-
 nmc_status build_xyz(nmc_handle* h) {
-  const nmc_run_params& rp = h->rp;
   nmc::XyzParams& p = h->xp;
   p = nmc::XyzParams{};
-  p.Nx = rp.Nx;
-  p.Ny = rp.Ny;
-  p.Nz = rp.Nz;
-  p.dx = rp.dx;
-  p.dy = rp.dy;
-  p.dz = rp.dz;
-  p.idx = (float)(1.0 / rp.dx);
-  p.idy = (float)(1.0 / rp.dy);
-  p.idz = (float)(1.0 / rp.dz);
-  p.dxmax = std::nextafter(rp.dx, 0.f);
-  p.dymax = std::nextafter(rp.dy, 0.f);
-  p.dzmax = std::nextafter(rp.dz, 0.f);
-  lattice_split(rp.zsurf, rp.dz, &p.ksurf, &p.fsurf);
-  p.boundaryflag = rp.boundaryflag;
-  p.det_state = rp.det_state;
-  p.launchflag = rp.launchflag;
-  p.mcflag = rp.mcflag;
-  p.xs = rp.xs;
-  p.ys = rp.ys;
-  p.zs = rp.zs;
-  p.ux0 = rp.ux0;
-  p.uy0 = rp.uy0;
-  p.uz0 = rp.uz0;
-  p.radius = rp.radius;
-  p.waist = rp.waist;
-  p.zfocus = rp.zfocus;
-  p.n1 = rp.n1;
-  p.n2 = rp.n2;
-  if (flt_eq_host(rp.xd, 0.f)) {  // kernels.metal:590-599
-    p.r_min = 0.f;
-    p.r_max = rp.det_radius;
-  } else {
-    p.r_min = rp.xd - rp.det_radius;
-    p.r_max = p.r_min + 2.f * rp.det_radius;
-  }
-  p.na = rp.na;
-  p.det_everything = (p.r_min <= 0.f && std::isinf(p.r_max) && rp.na >= 90.f) ? 1 : 0;
+  nmc::fill_xyz(p, h->rp, h->tp, h->ext, h->sim);
   p.V = h->d_V;
-  for (int t = 0; t < NMC_NTISS; ++t) {
-    const float mus = h->tp.musv[t];
-    p.core[t] = make_float4(h->tp.muav[t], mus, mus > 0.f ? (float)(1.0 / mus) : 0.f, h->tp.gv[t]);
-    p.phase[t] = phase_const(h->tp, t);
-  }
-  p.flags = h->ext.flags;
-  p.step_cap = 4000000u;
   p.F3D = h->d_F3D;
   p.Rd2D = h->d_Rd2D;
   p.Det2D = h->d_Det;
   p.rd_slots = h->d_slots;
   p.nslots = h->nslots;
   p.sums = h->d_sums;
-  p.rng = rng_params(h->ext, h->sim);
   return NMC_OK;
 }
 
 nmc_status build_sub(nmc_handle* h) {
-  const nmc_ext& e = h->ext;
   nmc::SubParams& p = h->sp;
   p = nmc::SubParams{};
-  const int L = 1;  // FIRST_TISSUE_LAYER_MCSUB
-  p.mua = h->tp.muav[L];
-  p.mus = h->tp.musv[L];
-  p.mut = p.mua + p.mus;
-  p.albedo = p.mus / p.mut;
-  p.n1 = h->rp.n1;
-  p.n2 = h->rp.n2;
-  p.dr = e.sub_dr;
-  p.dz = e.sub_dz;
-  p.idr = (float)(1.0 / e.sub_dr);
-  p.idz = (float)(1.0 / e.sub_dz);
-  p.bins = e.sub_bins;
-  p.mcflag = e.sub_mcflag;
-  p.boundaryflag = e.sub_boundaryflag;
-  p.radius = e.sub_radius;
-  p.waist = e.sub_waist;
-  p.zfocus = e.sub_zfocus;
-  p.xs = e.sub_xs;
-  p.ys = e.sub_ys;
-  p.zs = e.sub_zs;
-  p.phase = phase_const(h->tp, L);
-  p.phase_kind = e.phase == NMC_PHASE_TWO_TERM ? nmc::kPhaseTT
-                 : e.phase == NMC_PHASE_ISOTROPIC_REF ? nmc::kPhaseIsoRef
-                                                      : nmc::kPhaseHG;
+  nmc::fill_sub(p, h->rp, h->tp, h->ext);
   p.J = h->d_J;
   p.F = h->d_F;
   p.sums = h->d_sums;
-  p.rng = rng_params(e, h->sim);
-  p.step_cap = 10000000u;
   return NMC_OK;
 }
 

@@ -76,21 +76,25 @@ enum Draw { D_LAUNCH, D_STEP, D_COS, D_PSI, D_ROUL, D_FRES, D_CHOICE, D_SAMPLE }
 
 // Philox layout of the GPU engine (same definition as in the CUDA
 // kernels): key = (seed lo, seed hi); counter = (photon lo, photon hi, c2,
-// 0x4E4D4321) with
-//   c2 = 0xFFFFFFFF          launch block, slots used in draw order;
-//   c2 = h                   main block of hop h (h = 0, 1, ...);
-//   c2 = h | 0x40000000      aux block of hop h, generated only when used.
-// Slots:   HG / isotropic     main = (step, cos, psi, roulette), aux = (fresnel)
-//          two-term           main = (step, choice, sample, psi),
-//                             aux  = (fresnel, roulette)
+// 0x4E4D4321).  Hops are numbered h = 0, 1, ...; the SPIN that ends hop h
+// and the step of hop h+1 come from one block, so each block is consumed at
+// one point of the photon loop:
+//   c2 = 0xFFFFFFFF          launch block, slots used in draw order
+//   c2 = h                   event block h: w = step of hop h; for h >= 1
+//                            x, y, z are the draws of the SPIN ending hop h-1
+//                              HG / isotropic: x = cos, y = psi, z = roulette
+//                              two-term:       x = choice, y = sample, z = psi
+//   c2 = h | 0x40000000      aux block h, generated only when used:
+//                            x = roulette of the SPIN ending hop h-1 (two-term),
+//                            y = Fresnel test during hop h (mcsub)
 // u = (2k+1) 2^-24 with k the top 23 bits of the word: 0 < u < 1, exact in
 // float and double, so the reference's `while (rnd <= 0)` loops never repeat.
 struct PhiloxStream {
   uint32_t k0, k1, id_lo, id_hi;
   bool tt;
   uint32_t hop = 0xFFFFFFFFu, nlaunch = 0;
-  uint32_t mb[4], ab[4], lb[4];
-  bool m_ok = false, a_ok = false, l_ok = false;
+  uint32_t cb[4], nb[4], ab[4], nab[4], lb[4];
+  bool c_ok = false, n_ok = false, a_ok = false, na_ok = false, l_ok = false;
   PhiloxStream(uint64_t seed, uint64_t photon, bool two_term)
       : k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), id_lo((uint32_t)photon),
         id_hi((uint32_t)(photon >> 32)), tt(two_term) {}
@@ -101,21 +105,40 @@ struct PhiloxStream {
   }
   void new_hop() {
     ++hop;
-    m_ok = a_ok = false;
+    // the "next" blocks of the previous hop are this hop's current ones
+    if (n_ok) std::memcpy(cb, nb, sizeof cb);
+    c_ok = n_ok;
+    if (na_ok) std::memcpy(ab, nab, sizeof ab);
+    a_ok = na_ok;
+    n_ok = na_ok = false;
   }
-  uint32_t main_slot(int k) {
-    if (!m_ok) {
-      gen(hop, mb);
-      m_ok = true;
+  uint32_t cur(int k) {
+    if (!c_ok) {
+      gen(hop, cb);
+      c_ok = true;
     }
-    return mb[k];
+    return cb[k];
   }
-  uint32_t aux_slot(int k) {
+  uint32_t next(int k) {
+    if (!n_ok) {
+      gen(hop + 1, nb);
+      n_ok = true;
+    }
+    return nb[k];
+  }
+  uint32_t aux_cur(int k) {
     if (!a_ok) {
       gen(hop | 0x40000000u, ab);
       a_ok = true;
     }
     return ab[k];
+  }
+  uint32_t aux_next(int k) {
+    if (!na_ok) {
+      gen((hop + 1) | 0x40000000u, nab);
+      na_ok = true;
+    }
+    return nab[k];
   }
   uint32_t word(Draw d) {
     switch (d) {
@@ -125,13 +148,13 @@ struct PhiloxStream {
           l_ok = true;
         }
         return lb[(nlaunch++) & 3];
-      case D_STEP: return main_slot(0);
-      case D_COS: return main_slot(1);
-      case D_CHOICE: return main_slot(1);
-      case D_SAMPLE: return main_slot(2);
-      case D_PSI: return tt ? main_slot(3) : main_slot(2);
-      case D_ROUL: return tt ? aux_slot(1) : main_slot(3);
-      case D_FRES: return aux_slot(0);
+      case D_STEP: return cur(3);
+      case D_COS: return next(0);
+      case D_CHOICE: return next(0);
+      case D_SAMPLE: return next(1);
+      case D_PSI: return tt ? next(2) : next(1);
+      case D_ROUL: return tt ? aux_next(0) : next(2);
+      case D_FRES: return aux_cur(1);
     }
     return 0;
   }
