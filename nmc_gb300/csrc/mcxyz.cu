@@ -256,17 +256,21 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
     // on the crossing, so the lanes of a warp stay together.
     const float4 c = s_core[tiss];  // mua, mus, 1/mus, g
     float s = sleft * c.z;
-    const float ex = fmaf(s, ux, fx), ey = fmaf(s, uy, fy), ez = fmaf(s, uz, fz);
-    // SameVoxel (helpers.metal:27-39) in cell-local form
-    const bool sv = (ex <= P.dx) && (ex >= 0.f || (fx == 0.f && ex >= -P.dx)) && (ey <= P.dy) &&
-                    (ey >= 0.f || (fy == 0.f && ey >= -P.dy)) && (ez >= 0.f) && (ez <= P.dz);
     ++nsub;
     ++depth;
-    // FindVoxelFace2 (helpers.metal:85-114) in cell-local form
-    const float tx = (ux >= 0.f ? P.dx - fx : fx) * M::rcp(fabsf(ux));
-    const float ty = (uy >= 0.f ? P.dy - fy : fy) * M::rcp(fabsf(uy));
-    const float tz = (uz >= 0.f ? P.dz - fz : fz) * M::rcp(fabsf(uz));
+    // FindVoxelFace2 (helpers.metal:85-114) in cell-local form: path length
+    // to the face ahead on each axis
+    const float rx = M::rcp(fabsf(ux)), ry = M::rcp(fabsf(uy)), rz = M::rcp(fabsf(uz));
+    const float tx = (ux >= 0.f ? P.dx - fx : fx) * rx;
+    const float ty = (uy >= 0.f ? P.dy - fy : fy) * ry;
+    const float tz = (uz >= 0.f ? P.dz - fz : fz) * rz;
     const int ax = (tx <= ty) ? ((tx <= tz) ? 0 : 2) : ((ty <= tz) ? 1 : 2);
+    // SameVoxel (helpers.metal:27-39): the end point stays in the cell, upper
+    // faces included; a photon on a lower x or y face moving down stays for
+    // up to one cell (the reference compares with the cell below's upper face)
+    const float sx = (ux < 0.f && fx == 0.f) ? P.dx * rx : tx;
+    const float sy = (uy < 0.f && fy == 0.f) ? P.dy * ry : ty;
+    const bool sv = s <= fminf(sx, fminf(sy, tz));
     if (!sv) s = kLS + fminf(tx, fminf(ty, tz));
     {
       const float absorb = M::absorbed(W, c.x * s);
@@ -323,9 +327,9 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
         }
       }
       if (!moved) {
-        fx = sv ? ex : fmaf(s, ux, fx);
-        fy = sv ? ey : fmaf(s, uy, fy);
-        fz = sv ? ez : fmaf(s, uz, fz);
+        fx = fmaf(s, ux, fx);
+        fy = fmaf(s, uy, fy);
+        fz = fmaf(s, uz, fz);
         if (!sv) {
           // the face the step aims at is crossed by exactly ls*|u| (as in FP64)
           if (ax == 0) {
@@ -342,9 +346,13 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
             fz = p ? kLS * uz : fminf(fmaf(kLS, uz, P.dz), P.dzmax);
           }
         }
-        norm_axis(kx, fx, P.dx, P.dxmax);
-        norm_axis(ky, fy, P.dy, P.dymax);
-        norm_axis(kz, fz, P.dz, P.dzmax);
+        // offsets leave [0, d) only when a point lands on a face (an upper
+        // face of the same-voxel end point, a tie between faces)
+        if (fx < 0.f || fx >= P.dx || fy < 0.f || fy >= P.dy || fz < 0.f || fz >= P.dz) {
+          norm_axis(kx, fx, P.dx, P.dxmax);
+          norm_axis(ky, fy, P.dy, P.dymax);
+          norm_axis(kz, fz, P.dz, P.dzmax);
+        }
       }
     }
     if (!sv) {

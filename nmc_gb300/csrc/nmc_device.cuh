@@ -55,9 +55,11 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1
   return c;
 }
 
-// 0 < u < 1, u = (2k+1) 2^-24 from the top 23 bits (exact in float).
+// 0 < u < 1, u = (2k+1) 2^-24 from the top 23 bits k of x (exact in float).
+// Built without an int->float conversion: 1 + k 2^-23 is the float with
+// mantissa k, and (1 + k 2^-23) - (1 - 2^-24) is exact (Sterbenz).
 __device__ __forceinline__ float u01(uint32_t x) {
-  return fmaf((float)(x >> 9), 0x1p-23f, 0x1p-24f);
+  return __uint_as_float((x >> 9) | 0x3F800000u) - 0.99999994039535522f;
 }
 
 // Per-photon Philox layout (identical in the oracle): key = (seed lo, seed
@@ -298,6 +300,10 @@ struct Math {
       sincospif(2.f * u, s, c);
   }
   static __device__ __forceinline__ float pow(float x, float y) { return FAST ? __powf(x, y) : powf(x, y); }
+  // sqrt of x >= 0
+  static __device__ __forceinline__ float sqrt(float x) {
+    return FAST ? x * rsqrtf(fmaxf(x, 1e-30f)) : sqrtf(x);
+  }
 };
 
 template <bool FAST>
@@ -331,7 +337,7 @@ __device__ __forceinline__ float tt_sample(const PhaseConst& p, float uc, float 
 template <bool FAST>
 __device__ __forceinline__ void spin(float costheta, float upsi, float& ux, float& uy,
                                      float& uz) {
-  const float sintheta = sqrtf(fmaxf(fmaf(-costheta, costheta, 1.f), 0.f));
+  const float sintheta = Math<FAST>::sqrt(fmaxf(fmaf(-costheta, costheta, 1.f), 0.f));
   float sinpsi, cospsi;
   Math<FAST>::sincos2pi(upsi, &sinpsi, &cospsi);
   const float auz = fabsf(uz);
