@@ -42,6 +42,10 @@ WORKLOAD = "mcxyz skin-vessel 200^3 @0.005 cm, 1e8 photons per GPU per step"
 # per-hop SPIN/roulette share.  Fixed once; see the design doc.
 OPS_PER_SUBSTEP = 64.0
 MUFU_PER_SUBSTEP = 3.0
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 1e8-photon
+# launch of the transport kernel, from one ncu capture of that launch.
+TRAFFIC_BYTES_1E8 = 72_138_240 + 28_571_801_856
+HBM_PEAK_FALLBACK_GBS = 6800.0
 
 
 def _clock_sampler(stop: threading.Event, out: list, dev: int):
@@ -243,6 +247,14 @@ def run_ours(args) -> dict:
     kernel_s = kernel_ms * 1e-3
     achieved = substeps * OPS_PER_SUBSTEP / kernel_s / 1e12 if kernel_s > 0 else None
     peak = ffma / 1e12
+    traffic = TRAFFIC_BYTES_1E8 * P / 1e8  # per launch; writes grow with the launch's duration
+    try:
+        hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+        hbm_src = "measured"
+    except Exception:
+        hbm_peak, hbm_src = HBM_PEAK_FALLBACK_GBS, "fallback"
+    launch_s = kernel_s / max(launches, 1)
+    hbm_gbs = traffic / launch_s / 1e9 if launch_s > 0 else None
     out = {
         "metric": METRIC, "value": value, "unit": "photons/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -255,10 +267,13 @@ def run_ours(args) -> dict:
         "e2e": {"value": e2e_value, "unit": "photons/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "fp32_issue", "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "kernel": "mcxyz_kernel", "ops_per_substep": OPS_PER_SUBSTEP,
                      "substeps_per_s": substeps / kernel_s if kernel_s > 0 else None,
-                     "mufu_peak_tlanes": mufu / 1e12, "peak_source": "measured live (nmc_probe_issue_peaks)"},
+                     "mufu_peak_tlanes": mufu / 1e12,
+                     "peak_source": "of measured FP32 FMA lane rate (nmc_probe_issue_peaks, live)",
+                     "hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": hbm_peak, "peak_source": hbm_src,
+                             "frac": (hbm_gbs / hbm_peak) if hbm_gbs else None}},
         "gpu_launches": launches,
         "clocks": _clocks_summary(clock_lines),
     }
@@ -274,6 +289,98 @@ def run_ours(args) -> dict:
     return out if rank == 0 else {}
 
 
+def run_sweep_workload(args) -> dict:
+    """351-wavelength batched sweep on the mcsub geometry (two-term phase
+    function, budgets log-uniform in 1e5-1e7).  Two comparisons on the same
+    photon streams: (1) every set's full budget in one persistent launch
+    against 351 plain per-wavelength runs; (2) time until every set reaches
+    1% relative standard error in Rd (pilot + top-up), batched (2 launches)
+    against plain (2 runs per wavelength)."""
+    import numpy as np
+    import torch
+
+    import nmc_cases as cases
+    from nmc_gb300 import abi, build, engine
+    from nmc_gb300 import sweep as nsweep
+
+    build.build()
+    torch.cuda.set_device(0)
+    lam, sets = cases.spectral_sweep_sets()
+    total = int(sum(s.photons for s in sets))
+    flags = abi.FLAG_SKIP_FLUENCE  # both sides tally Rd, J and totals only
+
+    def ext_for(seed):
+        return abi.ext_defaults(phase=abi.PHASE_TWO_TERM, sub_bins=101, sub_dr=0.01, sub_dz=0.01, seed=seed,
+                                flags=flags)
+
+    rp, tp, _ = cases.mcsub_case(tt=(0.9, 0.5, 0.3, 0.5, 0.9))
+    e = engine.Engine(abi.SIM_MCSUB, 0, ext_for(11))
+    e.prepare_data(rp, tp)
+    warm = [nsweep._copy(s, photons=20000) for s in sets[:8]]
+    e.run_sweep(warm)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    res, batched_s = timed(lambda: e.run_sweep(sets))
+    tgt, batched_tgt_s = timed(lambda: nsweep.sweep(e, sets, target_rel_se=0.01))
+
+    def plain(target):
+        rd = np.zeros(len(sets))
+        rse = np.zeros(len(sets))
+        photons = 0
+        for i, q in enumerate(sets):
+            e.set_ext(ext_for(11 + (i << 32)))
+            tps = abi.tissue_params(mua=[q.mua], mus=[q.mus], g=[q.g], gf=[q.gf], af=[q.af], gb=[q.gb],
+                                    ab=[q.ab], cc=[q.cc])
+            rp.n1, rp.n2 = q.n1, q.n2
+            e.prepare_data(rp, tps)
+            if target is None:
+                e.run(0, q.photons)
+            else:  # same pilot + top-up rule as the batched sweep
+                n1 = min(20000, q.photons)
+                e.run(0, n1)
+                s1 = e.summary()
+                me = s1["E"] / n1
+                var = max(s1["rd_sumsq"] / n1 - me * me, 1e-30)
+                rd1 = (s1["S"] + s1["E"]) / n1
+                need = int(np.ceil(1.15 * var / (target * max(rd1, 1e-30)) ** 2))
+                extra = max(min(need, q.photons) - n1, 0)
+                if extra:
+                    e.run(n1, extra)
+            sm = e.summary()
+            n = sm["photons"]
+            photons += n
+            me = sm["E"] / n
+            rd[i] = (sm["S"] + sm["E"]) / n
+            rse[i] = np.sqrt(max(sm["rd_sumsq"] / n - me * me, 0) / n) / rd[i]
+        return rd, rse, photons
+
+    (plain_rd, _, _), plain_s = timed(lambda: plain(None))
+    (plain_tgt_rd, plain_tgt_rse, plain_tgt_n), plain_tgt_s = timed(lambda: plain(0.01))
+    e.close()
+    rel_se = res["Rd_se"] / res["Rd"]
+    tgt_rel = tgt["Rd_se"] / tgt["Rd"]
+    return {
+        "metric": "photons/s, 351-wavelength batched sweep vs plain per-wavelength runs", "unit": "photons/s",
+        "value": total / batched_s, "plain_value": total / plain_s, "speedup": plain_s / batched_s,
+        "photons": total, "batched_s": batched_s, "plain_s": plain_s, "n_sets": len(sets),
+        "sets_at_1pct_se": int((rel_se <= 0.01).sum()), "max_rel_se": float(rel_se.max()),
+        "rd_matches_plain": float(np.max(np.abs(plain_rd - res["Rd"]) / res["Rd"])),
+        "to_1pct_se": {"batched_s": batched_tgt_s, "plain_s": plain_tgt_s, "speedup": plain_tgt_s / batched_tgt_s,
+                       "photons": int(tgt["photons"].sum()), "plain_photons": int(plain_tgt_n),
+                       "launches": tgt["launches"], "max_rel_se": float(tgt_rel.max()),
+                       "plain_max_rel_se": float(plain_tgt_rse.max())},
+        "hops_per_photon": float(res["hops"].sum() / total), "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "mcsub semi-infinite, 351 wavelengths 400-750 nm, two-term HG, budgets 1e5-1e7",
+                   "rng": "philox4x32-10", "tallies": "Rd, J(r), S/A/E per set (no F(r,z) on either side)"},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -284,8 +391,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warm-up and timed transport launches (for ncu)")
+    ap.add_argument("--workload", default="skinvessel", choices=["skinvessel", "sweep"])
     args = ap.parse_args()
-    out = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if args.workload == "sweep":
+        out = run_sweep_workload(args)
+    else:
+        out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if out:
         print(json.dumps(out))
 

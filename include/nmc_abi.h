@@ -145,7 +145,10 @@ enum {
   NMC_FLAG_NO_HARD_KILL = 1u << 1,
   /* Use CUDA's correctly rounded / 1-ulp log, exp, sin/cos, reciprocal and
    * pow in the photon step instead of the SFU approximations. */
-  NMC_FLAG_PRECISE_MATH = 1u << 2
+  NMC_FLAG_PRECISE_MATH = 1u << 2,
+  /* Skip the fluence tally (mcsub F(r,z)) when only Rd, J and the totals
+   * are wanted. */
+  NMC_FLAG_SKIP_FLUENCE = 1u << 3
 };
 
 typedef struct nmc_ext {
@@ -313,6 +316,45 @@ const char* nmc_last_error(const nmc_handle* h);
 
 /* Frees the handle and its device memory. */
 void nmc_destroy(nmc_handle* h);
+
+/* ------------------------------------------------------- batched sweeps */
+/* One parameter set of a batched sweep (e.g. one wavelength) on the mcsub
+ * geometry (semi-infinite medium, the handle's nmc_ext beam, bins and phase
+ * function).  Replaces one `nmc` process per wavelength
+ * (NMC-samples/example3.ipynb cell 5 rewrites _H.mci and relaunches nmc for
+ * every wavelength). */
+typedef struct nmc_sweep_set {
+  float mua, mus;           /* cm^-1 */
+  float g;                  /* HG anisotropy (phase NMC_PHASE_HG) */
+  float gf, af, gb, ab, cc; /* two-term parameters (NMC_PHASE_TWO_TERM) */
+  float n1, n2;             /* tissue / outside refractive index */
+  uint32_t pad;
+  uint64_t photons;         /* photon budget of this set */
+  uint64_t first_photon;    /* id of the set's first photon (0, or where a
+                               previous sweep of this set stopped) */
+} nmc_sweep_set;
+
+/* Per-set results of nmc_run_sweep, NMC_SWEEP_FIELDS doubles per set. */
+enum {
+  NMC_SWEEP_PHOTONS = 0,  /* photons completed */
+  NMC_SWEEP_HOPS = 1,     /* hops (steps) */
+  NMC_SWEEP_S = 2,        /* specular weight */
+  NMC_SWEEP_A = 3,        /* absorbed weight */
+  NMC_SWEEP_E = 4,        /* escaped weight */
+  NMC_SWEEP_E2 = 5,       /* sum over photons of escaped weight squared */
+  NMC_SWEEP_RD = 6,       /* Rd = (S + E) / photons, as main.m:238-242 */
+  NMC_SWEEP_RD_SE = 7,    /* standard error of Rd */
+  NMC_SWEEP_FIELDS = 8
+};
+
+/* Runs every set's photon budget in one persistent launch on a handle made
+ * with NMC_SIM_MCSUB (nmc_prepare called; its tissue layer is replaced by
+ * the sets).  Photons of set s use Philox key (seed lo, seed hi + s), so set
+ * s reproduces a plain run with seed + (s << 32).  `out` holds n_sets *
+ * NMC_SWEEP_FIELDS doubles; `J` (optional) n_sets * (BINS+1) doubles of the
+ * escaping flux J[ir] per set (un-normalised). */
+nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_sets, double* out,
+                         double* J);
 
 /* Measurement support (no counterpart in the reference): FP32 FMA lanes per
  * second and MUFU (ex2) lanes per second sustained on `device`, the issue

@@ -40,6 +40,7 @@ PHASE_TWO_TERM = 2
 FLAG_TT_REPLAY_RUN1 = 1 << 0
 FLAG_NO_HARD_KILL = 1 << 1
 FLAG_PRECISE_MATH = 1 << 2
+FLAG_SKIP_FLUENCE = 1 << 3
 
 FATE_ALIVE, FATE_ESCAPED, FATE_ROULETTE, FATE_MINWEIGHT, FATE_MAXSCATT, FATE_BOUNDARY, FATE_STEPCAP = range(7)
 
@@ -179,6 +180,28 @@ class PhotonRecord(C.Structure):
         ("z", C.c_float),
     ]
 
+
+class SweepSet(C.Structure):
+    """nmc_sweep_set: one parameter set of a batched sweep."""
+
+    _fields_ = [
+        ("mua", C.c_float),
+        ("mus", C.c_float),
+        ("g", C.c_float),
+        ("gf", C.c_float),
+        ("af", C.c_float),
+        ("gb", C.c_float),
+        ("ab", C.c_float),
+        ("cc", C.c_float),
+        ("n1", C.c_float),
+        ("n2", C.c_float),
+        ("pad", C.c_uint32),
+        ("photons", C.c_uint64),
+        ("first_photon", C.c_uint64),
+    ]
+
+
+SWEEP_FIELDS = ("photons", "hops", "S", "A", "E", "E2", "Rd", "Rd_se")
 
 PHOTON_RECORD_DTYPE = np.dtype(
     [

@@ -54,6 +54,7 @@ struct SubParams {
   PhaseConst phase;  // tissue 1
   int phase_kind;    // SubPhase
   int fast_math;
+  int skip_F;        // no F(r,z) tally
   unsigned long long* J;  // fixed point 2^-32, BINS+1
   unsigned long long* F;  // (BINS+1)^2
   DevSums* sums;
@@ -64,6 +65,35 @@ struct SubParams {
 };
 
 enum SubPhase { kPhaseHG = 0, kPhaseIsoRef = 1, kPhaseTT = 2 };
+
+// One parameter set of a batched sweep, as the kernel reads it.
+struct __align__(16) SweepSetDev {
+  float mut, albedo, n1, n2, rsp, pad;
+  unsigned long long first;  // id of the set's first photon
+  PhaseConst ph;
+};
+
+struct SweepParams {
+  int nsets;
+  const SweepSetDev* sets;
+  const unsigned long long* prefix;  // nsets + 1 prefix sums of the budgets
+  unsigned long long total;
+  int bins;
+  float idr;
+  int mcflag, boundaryflag;
+  float radius, waist, zfocus, xs, ys, zs;
+  unsigned long long* J;     // nsets x (bins + 1), may be null
+  unsigned long long* sums;  // nsets x 5
+  double* e2;                // nsets
+  unsigned long long* work;
+  unsigned int* flags;
+  uint32_t k0, k1;
+  int phase_kind, fast;
+  uint32_t step_cap;
+};
+
+cudaError_t launch_sweep(const SweepParams& p, int grid, int block, cudaStream_t stream);
+cudaError_t sweep_occupancy(const SweepParams& p, int block, int* blocks_per_sm);
 
 // Parameter blocks from the reference's configuration (params.cu); device
 // pointers are left for the caller to set.

@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
     const float absorb = W * (1.f - P.albedo);
     W -= absorb;
     Atot += absorb;
-    {
+    if (!P.skip_F) {
       const float r = sqrtf(x * x + y * y);
       int ir = (int)fminf(r * P.idr, (float)BINS) + 1;
       int iz = (int)fminf(fabsf(z) * P.idz, (float)BINS) + 1;
@@ -280,7 +280,7 @@ size_t mcsub_smem_bytes(int bins) {
 static bool smem_fits(int bins) { return mcsub_smem_bytes(bins) <= 200 * 1024; }
 
 static cudaError_t prepare(const SubParams& p, bool trace, const void** f, size_t* sh) {
-  const bool smem = smem_fits(p.bins);
+  const bool smem = !p.skip_F && smem_fits(p.bins);
   *f = p.fast_math ? pick2<true>(p, trace, smem) : pick2<false>(p, trace, smem);
   *sh = smem ? mcsub_smem_bytes(p.bins) : 0;
   if (*sh > 48 * 1024)

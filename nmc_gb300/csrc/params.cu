@@ -159,6 +159,7 @@ void fill_sub(SubParams& p, const nmc_run_params& rp, const nmc_tissue_params& t
                  : e.phase == NMC_PHASE_ISOTROPIC_REF ? kPhaseIsoRef
                                                       : kPhaseHG;
   p.fast_math = (e.flags & NMC_FLAG_PRECISE_MATH) ? 0 : 1;
+  p.skip_F = (e.flags & NMC_FLAG_SKIP_FLUENCE) ? 1 : 0;
   p.rng = rng_params(e, NMC_SIM_MCSUB);
   p.step_cap = 10000000u;
 }

@@ -598,6 +598,139 @@ nmc_status nmc_get_summary(nmc_handle* h, nmc_summary* out) {
   return NMC_OK;
 }
 
+nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_sets, double* out,
+                         double* J) {
+  if (!h || !sets || !out) return fail(h, NMC_EINVAL, "null argument");
+  if (h->sim != NMC_SIM_MCSUB) return fail(h, NMC_EINVAL, "sweeps run on an NMC_SIM_MCSUB handle");
+  if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
+  if (n_sets < 1 || n_sets > 1024) return fail(h, NMC_EINVAL, "n_sets must be in [1, 1024]");
+  if (h->ext.rng != NMC_RNG_PHILOX) return fail(h, NMC_EINVAL, "sweeps use the Philox streams");
+  nmc_status st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  const int bins = h->ext.sub_bins, nJ = bins + 1;
+  std::vector<nmc::SweepSetDev> hs(n_sets);
+  std::vector<unsigned long long> prefix(n_sets + 1, 0ull);
+  for (int s = 0; s < n_sets; ++s) {
+    const nmc_sweep_set& q = sets[s];
+    const float vals[] = {q.mua, q.mus, q.g, q.gf, q.af, q.gb, q.ab, q.cc, q.n1, q.n2};
+    for (float v : vals)
+      if (!std::isfinite(v)) return fail(h, NMC_EINVAL, "sweep set with a non-finite parameter");
+    if (q.mua < 0.f || q.mus < 0.f || !(q.mua + q.mus > 0.f) || !(q.n1 > 0.f) || !(q.n2 > 0.f))
+      return fail(h, NMC_EINVAL, "sweep set needs mua, mus >= 0, mua + mus > 0 and n1, n2 > 0");
+    nmc_tissue_params tp{};
+    tp.muav[1] = q.mua;
+    tp.musv[1] = q.mus;
+    tp.gv[1] = q.g;
+    tp.gf[1] = q.gf;
+    tp.af[1] = q.af;
+    tp.gb[1] = q.gb;
+    tp.ab[1] = q.ab;
+    tp.CC[1] = q.cc;
+    nmc::SweepSetDev& d = hs[s];
+    d = nmc::SweepSetDev{};
+    d.mut = q.mua + q.mus;
+    d.albedo = q.mus / d.mut;
+    d.n1 = q.n1;
+    d.n2 = q.n2;
+    float t = q.n1 / q.n2;  // kernels.metal:118-120
+    t = (1.f - t) / (1.f + t);
+    d.rsp = t * t;
+    d.first = q.first_photon;
+    d.ph = nmc::phase_const(tp, 1);
+    prefix[s + 1] = prefix[s] + q.photons;
+  }
+  nmc::SweepParams p{};
+  p.nsets = n_sets;
+  p.total = prefix[n_sets];
+  p.bins = bins;
+  p.idr = (float)(1.0 / h->ext.sub_dr);
+  p.mcflag = h->ext.sub_mcflag;
+  p.boundaryflag = h->ext.sub_boundaryflag;
+  p.radius = h->ext.sub_radius;
+  p.waist = h->ext.sub_waist;
+  p.zfocus = h->ext.sub_zfocus;
+  p.xs = h->ext.sub_xs;
+  p.ys = h->ext.sub_ys;
+  p.zs = h->ext.sub_zs;
+  p.k0 = (uint32_t)h->ext.seed;
+  p.k1 = (uint32_t)(h->ext.seed >> 32);
+  p.phase_kind = h->sp.phase_kind;
+  p.fast = h->sp.fast_math;
+  p.step_cap = h->sp.step_cap;
+  p.flags = &h->d_sums->flags;
+  // device buffers for this sweep: sets, prefix, per-set sums, counter, J
+  char* base = nullptr;
+  const size_t b_sets = sizeof(nmc::SweepSetDev) * n_sets, b_pre = 8 * (n_sets + 1),
+               b_sums = 8 * 5 * (size_t)n_sets, b_e2 = 8 * (size_t)n_sets, b_work = 8,
+               b_J = J ? 8 * (size_t)nJ * n_sets : 0;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t total_b = al(b_sets) + al(b_pre) + al(b_sums) + al(b_e2) + al(b_work) + al(b_J);
+  NMC_CUDA(h, cudaMalloc((void**)&base, total_b));
+  char* cur = base;
+  auto take = [&](size_t b) {
+    char* r = cur;
+    cur += al(b);
+    return r;
+  };
+  p.sets = (const nmc::SweepSetDev*)take(b_sets);
+  p.prefix = (const unsigned long long*)take(b_pre);
+  p.sums = (unsigned long long*)take(b_sums);
+  p.e2 = (double*)take(b_e2);
+  p.work = (unsigned long long*)take(b_work);
+  p.J = J ? (unsigned long long*)take(b_J) : nullptr;
+  auto cleanup = [&](nmc_status s) {
+    cudaFree(base);
+    return s;
+  };
+  if (cudaMemcpyAsync((void*)p.sets, hs.data(), b_sets, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync((void*)p.prefix, prefix.data(), b_pre, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+      // sums, e2, counter and J are contiguous: clear them together
+      cudaMemsetAsync(p.sums, 0, al(b_sums) + al(b_e2) + al(b_work) + al(b_J), h->stream) != cudaSuccess)
+    return cleanup(fail(h, NMC_EDEVICE, "sweep buffer set-up"));
+  const int block = h->ext.block_size > 0 ? h->ext.block_size : 256;
+  int per_sm = 0;
+  if (nmc::sweep_occupancy(p, block, &per_sm) != cudaSuccess || per_sm < 1)
+    return cleanup(fail(h, NMC_EDEVICE, "sweep kernel does not fit on an SM"));
+  if (h->ext.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)h->ext.blocks_per_sm);
+  uint64_t grid = (uint64_t)h->nsm * per_sm;
+  grid = std::max<uint64_t>(1, std::min<uint64_t>(grid, (p.total + block - 1) / block));
+  EventPair ev = get_pair(h);
+  cudaEventRecord(ev.a, h->stream);
+  if (p.total > 0 && nmc::launch_sweep(p, (int)grid, block, h->stream) != cudaSuccess)
+    return cleanup(fail(h, NMC_EDEVICE, "sweep launch"));
+  cudaEventRecord(ev.b, h->stream);
+  h->pending.push_back(ev);
+  ++h->launches;
+  st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return cleanup(st);
+  std::vector<unsigned long long> sums(5 * (size_t)n_sets);
+  std::vector<double> e2(n_sets);
+  if (cudaMemcpy(sums.data(), p.sums, b_sums, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(e2.data(), p.e2, b_e2, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return cleanup(fail(h, NMC_EDEVICE, "sweep results"));
+  if (J) {
+    std::vector<unsigned long long> hj((size_t)nJ * n_sets);
+    if (cudaMemcpy(hj.data(), p.J, b_J, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return cleanup(fail(h, NMC_EDEVICE, "sweep J"));
+    for (size_t k = 0; k < hj.size(); ++k) J[k] = (double)hj[k] * nmc::kUnfix;
+  }
+  for (int s = 0; s < n_sets; ++s) {
+    double* o = out + (size_t)s * NMC_SWEEP_FIELDS;
+    const unsigned long long* u = &sums[5 * (size_t)s];
+    const double n = (double)u[0];
+    o[NMC_SWEEP_PHOTONS] = n;
+    o[NMC_SWEEP_HOPS] = (double)u[1];
+    o[NMC_SWEEP_S] = (double)u[2] * nmc::kUnfix;
+    o[NMC_SWEEP_A] = (double)u[3] * nmc::kUnfix;
+    o[NMC_SWEEP_E] = (double)u[4] * nmc::kUnfix;
+    o[NMC_SWEEP_E2] = e2[s];
+    const double me = n > 0 ? o[NMC_SWEEP_E] / n : 0.0;
+    o[NMC_SWEEP_RD] = n > 0 ? (o[NMC_SWEEP_S] + o[NMC_SWEEP_E]) / n : 0.0;
+    o[NMC_SWEEP_RD_SE] = n > 1 ? std::sqrt(std::max(0.0, e2[s] / n - me * me) / n) : 0.0;
+  }
+  return cleanup(st);
+}
+
 void* nmc_stream(nmc_handle* h) { return h ? (void*)h->stream : nullptr; }
 
 const char* nmc_last_error(const nmc_handle* h) { return h ? h->err.c_str() : "null handle"; }

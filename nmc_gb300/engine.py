@@ -64,6 +64,8 @@ def lib() -> C.CDLL:
         L.nmc_last_error.restype = C.c_char_p
         L.nmc_destroy.argtypes = [H]
         L.nmc_probe_issue_peaks.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.nmc_run_sweep.argtypes = [H, C.POINTER(abi.SweepSet), C.c_int32, _P, _P]
+        L.nmc_run_sweep.restype = C.c_int
         for name in ("nmc_create", "nmc_prepare", "nmc_set_ext", "nmc_set_num_runs_seed",
                      "nmc_send_compute_command", "nmc_run", "nmc_run_async", "nmc_synchronize",
                      "nmc_run_traced", "nmc_get_compute_results", "nmc_get_summary",
@@ -189,6 +191,19 @@ class Engine:
 
     def reset(self):
         self._check(self._L.nmc_reset(self._h), "nmc_reset")
+
+    def run_sweep(self, sets, with_J: bool = False) -> dict:
+        """Batched sweep (mcsub handle): `sets` is a sequence of abi.SweepSet.
+        Returns per-set arrays named as abi.SWEEP_FIELDS (and J if asked)."""
+        n = len(sets)
+        arr = (abi.SweepSet * n)(*sets)
+        out = np.zeros((n, len(abi.SWEEP_FIELDS)), np.float64)
+        J = np.zeros((n, self.ext.sub_bins + 1), np.float64) if with_J else None
+        self._check(self._L.nmc_run_sweep(self._h, arr, n, _ptr(out), _ptr(J)), "nmc_run_sweep")
+        res = {k: out[:, i] for i, k in enumerate(abi.SWEEP_FIELDS)}
+        if with_J:
+            res["J"] = J
+        return res
 
     @property
     def stream(self) -> int:

@@ -99,3 +99,34 @@ def match_fraction(a, b, rel=1e-3, abs_=1e-6, fields=("detected", "absorbed")):
         y = b[f].astype(np.float64)
         ok &= np.abs(x - y) <= abs_ + rel * np.maximum(np.abs(x), np.abs(y))
     return float(np.mean(ok)), ok
+
+
+def spectral_sweep_sets(n_wavelengths: int = 351, seed: int = 2024, budget_lo: float = 1e5,
+                        budget_hi: float = 1e7, n1: float = 1.37, n2: float = 1.0):
+    """Batched spectral sweep on the mcsub geometry: wavelengths 400-750 nm;
+    reduced scattering mus' = a (lambda / 500 nm)^-b with a in [10, 40] /cm and
+    b in [0.8, 2.0] (seeded); mua a seeded sum of 3-6 Gaussians (amplitudes
+    0.05-2 /cm, centres 400-750 nm, widths 10-60 nm) over 0.01 /cm; two-term
+    phase function g_f = 0.9, backward branch g_b = 0.3 sampled and negated
+    (mean cosine -0.3), alpha = 0.5 (HG shape per branch), forward weight 0.9;
+    mus = mus' / (1 - g_eff) with g_eff = 0.9*0.9 + 0.1*(-0.3) = 0.78; budgets
+    log-uniform in [1e5, 1e7] photons.  Returns (wavelengths, list of
+    abi.SweepSet)."""
+    rng = np.random.default_rng(seed)
+    lam = np.linspace(400.0, 750.0, n_wavelengths)
+    a = rng.uniform(10.0, 40.0)
+    b = rng.uniform(0.8, 2.0)
+    k = int(rng.integers(3, 7))
+    amp = rng.uniform(0.05, 2.0, k)
+    cen = rng.uniform(400.0, 750.0, k)
+    wid = rng.uniform(10.0, 60.0, k)
+    mua = 0.01 + (amp[None, :] * np.exp(-((lam[:, None] - cen[None, :]) ** 2) / (2 * wid[None, :] ** 2))).sum(1)
+    gf, af, gb, ab, cc = 0.9, 0.5, 0.3, 0.5, 0.9
+    g_eff = cc * gf + (1 - cc) * (-gb)
+    mus = a * (lam / 500.0) ** (-b) / (1.0 - g_eff)
+    budgets = np.exp(rng.uniform(np.log(budget_lo), np.log(budget_hi), n_wavelengths)).astype(np.int64)
+    sets = []
+    for i in range(n_wavelengths):
+        sets.append(abi.SweepSet(mua=float(mua[i]), mus=float(mus[i]), g=g_eff, gf=gf, af=af, gb=gb, ab=ab,
+                                 cc=cc, n1=n1, n2=n2, pad=0, photons=int(budgets[i])))
+    return lam, sets
