@@ -186,7 +186,11 @@ typedef struct nmc_summary {
   uint32_t device_flags; /* NMC_DEVFLAG_* raised by kernels */
 } nmc_summary;
 
-enum { NMC_DEVFLAG_STEPCAP = 1u << 0, NMC_DEVFLAG_BADTISSUE = 1u << 1 };
+enum {
+  NMC_DEVFLAG_STEPCAP = 1u << 0,
+  NMC_DEVFLAG_BADTISSUE = 1u << 1,
+  NMC_DEVFLAG_REPLAY = 1u << 2 /* an adjoint replay did not reproduce a photon's recorded detections */
+};
 
 /* FP64 tallies readable with nmc_get_tally_f64. */
 typedef enum nmc_tally {
@@ -195,7 +199,8 @@ typedef enum nmc_tally {
   NMC_TALLY_F3D = 2,      /* mcxyz deposition, Nx*Ny*Nz, index iz*Ny*Nx + ix*Ny + iy */
   NMC_TALLY_RD2D = 3,     /* mcxyz detected weight map, Nx*Ny, index ix*Ny + iy */
   NMC_TALLY_DETPHOT2D = 4,/* mcxyz detected photon counts, Nx*Ny */
-  NMC_TALLY_RD_SLOTS = 5  /* per dispatch slot Rd (kernels.metal:753), photons_per_dispatch */
+  NMC_TALLY_RD_SLOTS = 5, /* per dispatch slot Rd (kernels.metal:753), photons_per_dispatch */
+  NMC_TALLY_RD_R = 6      /* radial Rd(r) at the detection plane, bins + 1 (last = overflow) */
 } nmc_tally;
 
 /* Per-photon record written by nmc_run_traced (parity tests). */
@@ -316,6 +321,34 @@ const char* nmc_last_error(const nmc_handle* h);
 
 /* Frees the handle and its device memory. */
 void nmc_destroy(nmc_handle* h);
+
+/* ------------------------------------------ per-voxel media and adjoint */
+/* Gives every voxel its own absorption, scattering and HG anisotropy
+ * (Nx*Ny*Nz floats each, index iz*Ny*Nx + ix*Ny + iy; g may be NULL to use
+ * gv[1] everywhere).  No reference counterpart: the reference indexes at
+ * most 18 tissue types through the uint8 map (definitions.h:57).  From this
+ * call on, an NMC_SIM_MCXYZ handle ignores its tissue map (Philox streams,
+ * one-term HG).  Requires mua >= 0, mus > 0, -1 < g < 1, all finite. */
+nmc_status nmc_set_voxel_props(nmc_handle* h, const float* mua, const float* mus, const float* g);
+
+/* Adds a radial reflectance tally Rd(r): detected weight binned by the
+ * distance from the z axis where it leaves the detection plane, `bins` bins
+ * of width `dr` plus one overflow bin (NMC_TALLY_RD_R). */
+nmc_status nmc_set_radial_tally(nmc_handle* h, int32_t bins, float dr);
+
+/* Perturbation Monte Carlo adjoint of the radial reflectance for per-voxel
+ * media.  nmc_adjoint_forward runs photons [first, first+n) like nmc_run and
+ * also records every detection event (photon, radial bin, weight); up to
+ * `event_capacity` events are kept (NMC_EINVAL if more occurred).
+ * nmc_adjoint_backward takes the upstream gradient dL/dRdr[b] of the
+ * un-normalised radial tally (bins + 1 floats) and replays the detected
+ * photons of the last forward to return, per voxel,
+ *   grad_mua = dL/dmua, grad_mus = dL/dmus, grad_g = dL/dg
+ * (Nx*Ny*Nz doubles each, any may be NULL), the path-length and
+ * likelihood-ratio estimator of the same photons. */
+nmc_status nmc_adjoint_forward(nmc_handle* h, uint64_t first, uint64_t n, uint64_t event_capacity);
+nmc_status nmc_adjoint_backward(nmc_handle* h, const float* grad_rd_r, double* grad_mua,
+                                double* grad_mus, double* grad_g);
 
 /* ------------------------------------------------------- batched sweeps */
 /* One parameter set of a batched sweep (e.g. one wavelength) on the mcsub

@@ -44,7 +44,7 @@ FLAG_SKIP_FLUENCE = 1 << 3
 
 FATE_ALIVE, FATE_ESCAPED, FATE_ROULETTE, FATE_MINWEIGHT, FATE_MAXSCATT, FATE_BOUNDARY, FATE_STEPCAP = range(7)
 
-TALLY_J, TALLY_F, TALLY_F3D, TALLY_RD2D, TALLY_DETPHOT2D, TALLY_RD_SLOTS = range(6)
+TALLY_J, TALLY_F, TALLY_F3D, TALLY_RD2D, TALLY_DETPHOT2D, TALLY_RD_SLOTS, TALLY_RD_R = range(7)
 
 STATUS = {
     0: "NMC_OK",

@@ -1,0 +1,81 @@
+"""Differentiable radial reflectance for per-voxel media.
+
+``radial_reflectance(mua, mus, g, engine, first, n)`` returns Rd(r) — the
+weight detected at the detection plane per launched photon, binned by the
+distance from the z axis (``engine.set_radial_tally`` bins plus one overflow
+bin) — as a torch tensor whose gradient with respect to the per-voxel
+absorption ``mua``, scattering ``mus`` and anisotropy ``g`` is the
+perturbation Monte Carlo adjoint of the same photons (``nmc_adjoint_forward``
+/ ``nmc_adjoint_backward`` in include/nmc_abi.h):
+
+* d/dmua: pathwise, the detected weight carries exp(-sum mua * path);
+* d/dmus, d/dg: likelihood ratio of the sampled scattering points and angles.
+
+The reference has no gradient path (it tallies forward only, kernels.metal
+:321-754); this is the inverse-problem entry point built on the same
+transport.  Tensors may live on any device: properties go to the engine as
+host arrays (the engine keeps its own device copy), results come back on the
+device and dtype of ``mua``.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import abi
+from .engine import Engine
+
+
+class _RadialReflectance(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, mua, mus, g, engine: Engine, first: int, n: int, event_capacity: int | None):
+        ctx.engine, ctx.first, ctx.n, ctx.cap = engine, int(first), int(n), event_capacity
+        ctx.shape = tuple(mua.shape)
+        ctx.save_for_backward(mua, mus, g)
+        _forward(engine, mua, mus, g, first, n, event_capacity)
+        ctx.token = engine._adj_token
+        rd = engine.tally(abi.TALLY_RD_R) / float(n)
+        return torch.as_tensor(rd, dtype=mua.dtype, device=mua.device)
+
+    @staticmethod
+    def backward(ctx, grad_rd):
+        e: Engine = ctx.engine
+        if getattr(e, "_adj_token", None) != ctx.token:
+            # the handle ran another forward since: record this one again
+            # (same photon streams, so the same events)
+            mua, mus, g = ctx.saved_tensors
+            _forward(e, mua, mus, g, ctx.first, ctx.n, ctx.cap)
+            ctx.token = e._adj_token
+        G = grad_rd.detach().to("cpu", torch.float64).numpy() / float(ctx.n)
+        ga, gs, gg = e.adjoint_backward(G.astype(np.float32))
+        mua = ctx.saved_tensors[0]
+
+        def out(a, need):
+            if not need:
+                return None
+            return torch.as_tensor(a.reshape(ctx.shape), dtype=mua.dtype, device=mua.device)
+
+        need = ctx.needs_input_grad
+        return out(ga, need[0]), out(gs, need[1]), out(gg, need[2]), None, None, None, None
+
+
+def _forward(e: Engine, mua, mus, g, first, n, cap):
+    def host(t):
+        return t.detach().to("cpu", torch.float32).contiguous().numpy().ravel()
+
+    e.set_voxel_props(host(mua), host(mus), host(g))
+    e.reset()
+    e.adjoint_forward(first, n, cap)
+    e._adj_token = getattr(e, "_adj_token", 0) + 1
+
+
+def radial_reflectance(mua: torch.Tensor, mus: torch.Tensor, g: torch.Tensor, engine: Engine,
+                       first: int = 0, n: int = 1_000_000, event_capacity: int | None = None) -> torch.Tensor:
+    """Rd(r) per launched photon (bins + 1 values, last = overflow) of photons
+    [first, first + n) through per-voxel media (arrays of Nz x Nx x Ny or flat,
+    engine voxel order), differentiable in mua, mus and g.  `engine` is an
+    NMC_SIM_MCXYZ Engine after prepare_data and set_radial_tally; its other
+    tallies hold this forward's photons afterwards."""
+    if engine.sim_type != abi.SIM_MCXYZ:
+        raise ValueError("radial_reflectance needs an NMC_SIM_MCXYZ engine")
+    return _RadialReflectance.apply(mua, mus, g, engine, first, n, event_capacity)

@@ -11,6 +11,14 @@
 
 namespace nmc {
 
+// One detection event recorded by the adjoint's forward pass.
+struct AdjEvent {
+  unsigned int photon;  // photon index within the launch
+  unsigned int bin;     // radial bin
+  float w;              // detected weight
+  float pad;
+};
+
 // Voxel kernels (MCXYZKernel kernels.metal:321-754 and MCXYZKernelTT
 // :757-1118).  Photon positions are kept as an integer voxel-lattice cell
 // (k = floor(x / d), unbounded) plus an FP32 offset inside the cell.
@@ -42,7 +50,25 @@ struct XyzParams {
   unsigned long long first, n;
   RngParams rng;
   TraceParams trace;
+  // media with per-voxel optical properties (no reference counterpart)
+  const float4* vox;          // (mua, mus, 1/mus, g) per voxel
+  // radial reflectance Rd(r) at the detection plane, u64 fixed point
+  unsigned long long* rd_r;   // rd_bins + 1 entries (last = overflow), may be null
+  int rd_bins;
+  float rd_idr;
+  // perturbation Monte Carlo adjoint
+  int adj_pass;               // 0: record detection events, 1: backward replay
+  AdjEvent* ev;
+  unsigned long long* ev_count;
+  unsigned int ev_cap;
+  const float* adj_D;         // per photon detected score (backward)
+  const float* adj_G;         // upstream gradient per radial bin (backward)
+  double* gL;                 // per voxel: sum D * charged path length (absorption)
+  double* gM;                 // per voxel: d ln p(path)/dmus terms weighted by D
+  double* gQ;                 // per voxel: sum D * dln p_HG / dg over scatterings
 };
+
+enum XyzMode { kTissue = 0, kVoxel = 1, kAdjoint = 2 };
 
 // Layered semi-infinite kernel (MCSubKernel kernels.metal:59-319).
 struct SubParams {
@@ -107,6 +133,13 @@ void fill_sub(SubParams& p, const nmc_run_params& rp, const nmc_tissue_params& t
 cudaError_t launch_mcxyz(const XyzParams& p, bool two_term, bool trace, int grid, int block,
                          cudaStream_t stream);
 cudaError_t mcxyz_occupancy(bool two_term, bool trace, int block, int* blocks_per_sm);
+// per-voxel media (mode kVoxel or kAdjoint), Philox streams, one-term HG
+cudaError_t launch_mcxyz_voxel(const XyzParams& p, int mode, bool trace, int grid, int block,
+                               cudaStream_t stream);
+cudaError_t mcxyz_voxel_occupancy(int mode, bool trace, int block, int* blocks_per_sm);
+// D[photon] += G[bin] * w over recorded events
+cudaError_t launch_adjoint_scores(const AdjEvent* ev, unsigned int n_ev, const float* G, float* D,
+                                  cudaStream_t stream);
 
 cudaError_t launch_mcsub(const SubParams& p, bool trace, int grid, int block, cudaStream_t stream);
 cudaError_t mcsub_occupancy(const SubParams& p, bool trace, int block, int* blocks_per_sm);

@@ -1,0 +1,580 @@
+// mcxyz_kernel.cuh - voxel photon transport (MCXYZKernel,
+// kernels.metal:321-754, and the two-term variant MCXYZKernelTT,
+// kernels.metal:757-1118) as one persistent CUDA kernel for sm_103a,
+// instantiated by mcxyz.cu (tissue-map media) and mcxyz_voxel.cu (media with
+// per-voxel optical properties, forward and adjoint).
+//
+// Modes: kTissue reads a uint8 tissue map and a 19-entry table (the
+// reference's model); kVoxel reads (mua, mus, 1/mus, g) per voxel; kAdjoint
+// is kVoxel plus the perturbation Monte Carlo adjoint: in its record pass it
+// appends every detection event (photon, radial bin, weight) to a list, and
+// in its backward pass it replays each detected photon (the same compiled
+// code and random streams, hence the same trajectory) carrying D = the
+// photon's remaining detected score sum_k G[bin_k] w_k over events not yet
+// passed, and accumulates per voxel v (the voxel whose properties the step
+// used)
+//   L_v += D * s        for every charged path length s (absorption),
+//   M_v += D / mus_v - D * s'   for the scatterings and the hop lengths s'
+//                       whose probability depends on mus_v,
+//   Q_v += D * dln p_HG(cos; g_v)/dg  for every scattering in voxel v,
+// from which dScore/dmua_v = -L_v (pathwise: the weight is exp(-sum mua s)),
+// dScore/dmus_v = M_v and dScore/dg_v = Q_v (likelihood ratio).  s' = s
+// except at the detection plane, where the reference relocates the photon
+// to the plane after charging the whole step: when the hop would have ended
+// in the voxel, s' = the distance to the plane (the rest of the hop is
+// consumed afterwards, memorylessly); when the step ran to the voxel face,
+// the rest of the hop becomes a fixed length (kernels.metal:571-573), so
+// s' = s and neither the rest nor the scattering that ends it depend on
+// the exponential draw.
+//
+// Design:
+//  * persistent threads: the grid fills the GPU once; a thread that retires a
+//    photon takes the next photon index from a warp-aggregated counter;
+//  * one voxel sub-step per loop trip (the reference's inner do-while over
+//    RAY_DEPTH crossings, :505-685, flattened); the SPIN, roulette and the
+//    next hop's step run together at a hop's end from one Philox block, so
+//    no random state is carried across sub-steps;
+//  * positions are an integer voxel-lattice cell plus an FP32 offset in the
+//    cell: the "littlest step" ls = 1e-7 (definitions.h:59) stays ~200 ulps
+//    above the offset's rounding, so FP32 stepping walks voxels the way FP64
+//    arithmetic does (the reference's global FP32 coordinates round ls away
+//    at mm-scale positions and stall photons at faces);
+//  * optical properties live in shared memory, re-read each sub-step rather
+//    than held in registers; the uint8 tissue map is read through the
+//    read-only path (L2-resident: 8 MB for 200^3);
+//  * deposits are merged in a register while the photon stays in one voxel
+//    and flushed as u64 fixed-point atomics (exact, bit-reproducible);
+//    per-photon totals go to shared-memory block sums.
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "engine.h"
+
+namespace nmc {
+namespace {
+
+constexpr uint32_t kAlive = 1u, kBflag = 2u, kSurf = 4u, kHave = 8u, kFixed = 16u;
+
+__device__ __forceinline__ void to_lattice(float x, float d, float dmax, int& k, float& f) {
+  const float q = floorf(__fdiv_rn(x, d));
+  k = (int)q;
+  f = fmaf(-q, d, x);
+  if (f < 0.f) {
+    --k;
+    f = fminf(f + d, dmax);
+  } else if (f >= d) {
+    ++k;
+    f -= d;
+  }
+}
+
+// Brings an offset that left [0, d) by less than one cell back into it.
+__device__ __forceinline__ void norm_axis(int& k, float& f, float d, float dmax) {
+  const bool up = f >= d, dn = f < 0.f;
+  k += (int)up - (int)dn;
+  f = up ? f - d : (dn ? fminf(f + d, dmax) : f);
+}
+
+// The reference's voxel index `(int)(N/2.0 + x/d)` (kernels.metal:641-643,
+// C truncation toward zero) from cell k and offset f: half = N/2 rounded
+// down, odd = N is odd (then the index steps at f = d/2, hd = d/2).  The
+// launch formula `(int)(N/2 + x/d)` (:472-474) is the even case with half = N/2.
+__device__ __forceinline__ int lookup_index(int k, float f, int half, int odd, float hd) {
+  int A = half + k;
+  bool frac_pos;
+  if (odd) {
+    const bool up = f >= hd;
+    A += (int)up;
+    frac_pos = !up || f > hd;
+  } else {
+    frac_pos = f > 0.f;
+  }
+  return A + (int)((A < 0) & frac_pos);
+}
+
+struct Deposit {
+  unsigned int idx;
+  float acc;
+  __device__ __forceinline__ void flush(unsigned long long* F3D) {
+    if (acc > 0.f) atomicAdd(F3D + idx, to_fix(acc));
+    acc = 0.f;
+  }
+  __device__ __forceinline__ void add(unsigned long long* F3D, unsigned int i, float v) {
+    if (i != idx) {
+      flush(F3D);
+      idx = i;
+    }
+    acc += v;
+  }
+};
+
+// LAUNCH (kernels.metal:349-463; the two-term kernel :778-870 has no
+// Gaussian branch).  `d.next()` yields launch uniforms in draw order.
+template <bool TT, bool FAST, class D>
+__device__ __forceinline__ void launch_photon(const XyzParams& P, D& d, float& x, float& y, float& z,
+                                              float& ux, float& uy, float& uz, float& W) {
+  using M = Math<FAST>;
+  W = 1.f;
+  x = y = z = 0.f;
+  ux = uy = uz = 0.f;  // tagPhoton() zero initialisation
+  if (P.launchflag == 1) {
+    x = P.xs;
+    y = P.ys;
+    z = P.zs;
+    ux = P.ux0;
+    uy = P.uy0;
+    uz = P.uz0;
+  } else if (P.mcflag == 0 || (P.mcflag == 1 && !TT)) {
+    const bool gauss = P.mcflag == 1;
+    float r, sp, cp;
+    while ((r = d.next()) <= 0.f) {
+    }
+    float rad = gauss ? P.radius * sqrtf(-logf(r)) : P.radius * sqrtf(r);
+    while ((r = d.next()) <= 0.f) {
+    }
+    M::sincos2pi(r, &sp, &cp);
+    x = P.xs + rad * cp;
+    y = P.ys + rad * sp;
+    z = P.zs;
+    while ((r = d.next()) <= 0.f) {
+    }
+    rad = P.waist * sqrtf(r);
+    while ((r = d.next()) <= 0.f) {
+    }
+    M::sincos2pi(r, &sp, &cp);
+    const float xf = rad * cp, yf = rad * sp;
+    const float temp = sqrtf((x - xf) * (x - xf) + (y - yf) * (y - yf) + P.zfocus * P.zfocus);
+    ux = -(x - xf) / temp;
+    uy = -(y - yf) / temp;
+    uz = sqrtf(1.f - ux * ux - uy * uy);
+    if (gauss) {  // :423-427
+      float uz_new = uz;
+      const float int_rsp = rfresnel(P.n2, P.n1, fabsf(uz), &uz_new);
+      W = W * (1.f - int_rsp);
+      snell(P.n2, P.n1, ux, uy, uz);
+    }
+  } else if (P.mcflag == 2) {
+    const float costheta = 1.f - 2.f * d.next();
+    const float sintheta = sqrtf(fmaxf(1.f - costheta * costheta, 0.f));
+    float sp, cp;
+    M::sincos2pi(d.next(), &sp, &cp);
+    x = P.xs;
+    y = P.ys;
+    z = P.zs;
+    ux = sintheta * cp;
+    uy = sintheta * sp;
+    uz = costheta;
+  } else if (P.mcflag == 3) {
+    float r;
+    while ((r = d.next()) <= 0.f) {
+    }
+    x = P.radius * (r * 2.f - 1.f);
+    while ((r = d.next()) <= 0.f) {
+    }
+    y = P.radius * (r * 2.f - 1.f);
+    z = P.zs;
+    uz = 1.f;
+  } else if (P.mcflag == 4) {
+    z = P.zs;
+    uz = 1.f;
+  }
+}
+
+// Adjoint sums of the voxel the photon is in, merged while it stays there.
+struct AdjAcc {
+  unsigned int idx;
+  float L, M, Q;
+  __device__ __forceinline__ void flush(const XyzParams& P) {
+    if (idx != 0xFFFFFFFFu) {
+      if (L != 0.f) atomicAdd(P.gL + idx, (double)L);
+      if (M != 0.f) atomicAdd(P.gM + idx, (double)M);
+      if (Q != 0.f) atomicAdd(P.gQ + idx, (double)Q);
+    }
+    L = M = Q = 0.f;
+  }
+  __device__ __forceinline__ void at(const XyzParams& P, unsigned int i) {
+    if (i != idx) {
+      flush(P);
+      idx = i;
+    }
+  }
+};
+
+// Henyey-Greenstein cos(theta) for a per-voxel g (kernels.metal:696-703),
+// rounded like the tissue table's constants (phase_const): 1-g^2, 1+g^2 in
+// one rounding, 1/(2g) correctly rounded, so a per-voxel medium and the same
+// medium as a tissue map sample the same angles.
+template <bool FAST>
+__device__ __forceinline__ float hg_from_g(float g, float u) {
+  if (g == 0.f) return 2.f * u - 1.f;
+  if (flt_eq(g, 1.f)) return 1.f;
+  const float t = Math<FAST>::div(fmaf(-g, g, 1.f), fmaf(2.f * g, u, 1.f - g));
+  return fmaf(-t, t, fmaf(g, g, 1.f)) * __frcp_rn(2.f * g);
+}
+
+// d ln p_HG(mu; g) / dg for p = (1-g^2) / (1+g^2-2 g mu)^(3/2) / 2.
+__device__ __forceinline__ float dlnhg_dg(float g, float mu) {
+  return -2.f * g / (1.f - g * g) - 3.f * (g - mu) / (1.f + g * g - 2.f * g * mu);
+}
+
+template <bool TT, class RNG, bool TRACE, bool FAST, int MODE>
+__global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(const XyzParams P) {
+  using M = Math<FAST>;
+  constexpr bool VOX = MODE != kTissue;
+  constexpr bool ADJ = MODE == kAdjoint;
+  __shared__ float4 s_core[NMC_NTISS];
+  __shared__ PhaseConst s_ph[NMC_NTISS];
+  __shared__ unsigned long long s_tot[5];  // photons, substeps, scatters, A, rd
+  __shared__ double s_rd2;
+  if (!VOX) {
+    for (int t = threadIdx.x; t < NMC_NTISS; t += blockDim.x) {
+      s_core[t] = P.core[t];
+      s_ph[t] = P.phase[t];
+    }
+  }
+  if (threadIdx.x < 5) s_tot[threadIdx.x] = 0ull;
+  if (threadIdx.x == 0) s_rd2 = 0.0;
+  __syncthreads();
+
+  const uint32_t k0 = P.rng.k0, k1 = P.rng.k1;
+  const bool hard_kill = !(P.flags & NMC_FLAG_NO_HARD_KILL);
+  const bool back = ADJ && P.adj_pass == 1;  // backward replay: no tallies
+  const int NyNx = P.Ny * P.Nx;
+
+  RNG rng;
+  int kx = 0, ky = 0, kz = 0, tiss = 0, depth = 0;
+  float fx = 0.f, fy = 0.f, fz = 0.f, ux = 0.f, uy = 0.f, uz = 1.f;
+  float W = 0.f, sleft = 0.f, Rd_loc = 0.f, Atot = 0.f;
+  float D = 0.f, Dabs = 0.f;  // adjoint: remaining detected score, sum of |event scores| replayed
+  unsigned int i = 0, slot = 0, nsc = 0, nsub = 0, st = 0;
+  unsigned long long pidx = 0;
+  uint32_t fate = NMC_FATE_ALIVE, ndet = 0, nev = 0;  // trace only
+  Deposit dep{0xFFFFFFFFu, 0.f};
+  AdjAcc adj{0xFFFFFFFFu, 0.f, 0.f, 0.f};
+
+  auto kill = [&](uint32_t why) {
+    if (TRACE && (st & kAlive)) fate = why;
+    st &= ~kAlive;
+  };
+
+  while (true) {
+    if (!(st & kAlive)) {
+      if (back && (st & kHave)) {
+        adj.flush(P);
+        // every recorded event has been met again: D is back to zero up to
+        // the rounding of the two summation orders
+        if (!(fabsf(D) <= 1e-4f * Dabs)) atomicOr(&P.sums->flags, (unsigned int)NMC_DEVFLAG_REPLAY);
+      }
+      if ((st & kHave) && !back) {  // retire the finished photon
+        dep.flush(P.F3D);
+        if (Rd_loc > 0.f) atomicAdd(P.rd_slots + slot, to_fix(Rd_loc));  // :753
+        atomicAdd(&s_tot[0], 1ull);
+        atomicAdd(&s_tot[1], (unsigned long long)nsub);
+        atomicAdd(&s_tot[2], (unsigned long long)nsc);
+        atomicAdd(&s_tot[3], to_fix(Atot));
+        atomicAdd(&s_tot[4], to_fix(Rd_loc));
+        if (Rd_loc > 0.f) atomicAdd(&s_rd2, (double)Rd_loc * (double)Rd_loc);
+        if (TRACE) {
+          nmc_photon_record r;
+          r.n_scatt = nsc;
+          r.n_sub = nsub;
+          r.fate = fate;
+          r.n_detect = ndet;
+          r.w_final = W;
+          r.absorbed = Atot;
+          r.detected = Rd_loc;
+          r.x = (float)kx * P.dx + fx;
+          r.y = (float)ky * P.dy + fy;
+          r.z = (float)kz * P.dz + fz;
+          P.trace.recs[pidx] = r;
+        }
+      }
+      pidx = next_photon(&P.sums->work);
+      if (pidx >= P.n) break;
+      if (back) {  // only photons with a detected score contribute
+        D = P.adj_D[pidx];
+        Dabs = 0.f;
+        if (D == 0.f) {
+          st = 0;
+          continue;
+        }
+      }
+      const unsigned long long pid = P.first + pidx;
+      slot = (unsigned int)(pid % P.nslots);
+      float x, y, z;
+      if constexpr (std::is_same<RNG, TausRng>::value) {
+        rng.init_photon(pid, P.rng.batch, TT, P.rng.tt_replay != 0);
+        typename TausRng::Seq d{&rng};
+        launch_photon<TT, FAST>(P, d, x, y, z, ux, uy, uz, W);
+      } else {
+        rng.init(pid);
+        LaunchDraws d{rng.block(0xFFFFFFFFu, k0, k1), 0};
+        launch_photon<TT, FAST>(P, d, x, y, z, ux, uy, uz, W);
+      }
+      to_lattice(x, P.dx, P.dxmax, kx, fx);
+      to_lattice(y, P.dy, P.dymax, ky, fy);
+      to_lattice(z, P.dz, P.dzmax, kz, fz);
+      const int ix = min(max(lookup_index(kx, fx, P.Nx / 2, 0, 0.f), 0), P.Nx - 1);  // :472-480
+      const int iy = min(max(lookup_index(ky, fy, P.Ny / 2, 0, 0.f), 0), P.Ny - 1);
+      const int iz = min(max(lookup_index(kz, fz, 0, 0, 0.f), 0), P.Nz - 1);
+      i = (unsigned int)(iz * NyNx + ix * P.Ny + iy);
+      if (!VOX) tiss = __ldg(P.V + i);
+      sleft = M::neglog(rng.first_step(k0, k1));  // HOP (:501-502)
+      depth = 0;
+      Rd_loc = Atot = 0.f;
+      nsc = nsub = 0;
+      if (TRACE) {
+        fate = NMC_FATE_ALIVE;
+        ndet = nev = 0;
+      }
+      st = kAlive | kBflag | kSurf | kHave;
+      dep.idx = 0xFFFFFFFFu;
+      dep.acc = 0.f;
+      adj.idx = 0xFFFFFFFFu;
+    }
+
+    // ---- one voxel sub-step (:505-682).  The same-voxel move (:515-533) and
+    // the step to the nearest face (:534-682) share one straight path; only
+    // the face landing, the voxel lookup and the tissue load are predicated
+    // on the crossing, so the lanes of a warp stay together.
+    const float4 c = VOX ? __ldg(P.vox + i) : s_core[tiss];  // mua, mus, 1/mus, g
+    float s = sleft * c.z;
+    ++nsub;
+    ++depth;
+    // FindVoxelFace2 (helpers.metal:85-114) in cell-local form: path length
+    // to the face ahead on each axis
+    const float rx = M::rcp(fabsf(ux)), ry = M::rcp(fabsf(uy)), rz = M::rcp(fabsf(uz));
+    const float tx = (ux >= 0.f ? P.dx - fx : fx) * rx;
+    const float ty = (uy >= 0.f ? P.dy - fy : fy) * ry;
+    const float tz = (uz >= 0.f ? P.dz - fz : fz) * rz;
+    const int ax = (tx <= ty) ? ((tx <= tz) ? 0 : 2) : ((ty <= tz) ? 1 : 2);
+    // SameVoxel (helpers.metal:27-39): the end point stays in the cell, upper
+    // faces included; a photon on a lower x or y face moving down stays for
+    // up to one cell (the reference compares with the cell below's upper face)
+    // with the properties of the cell above.  Per-voxel media take the
+    // physical rule instead (the photon steps into the cell below at once):
+    // the reference's makes the hop's distribution in the cell below depend
+    // on two cells' mus through a moving support, which the likelihood-ratio
+    // adjoint cannot differentiate.  The two differ only for photons exactly
+    // on a lower face (a beam launched on a voxel face).
+    const float sx = (!VOX && ux < 0.f && fx == 0.f) ? P.dx * rx : tx;
+    const float sy = (!VOX && uy < 0.f && fy == 0.f) ? P.dy * ry : ty;
+    const bool sv = s <= fminf(sx, fminf(sy, tz));
+    if (!sv) s = kLS + fminf(tx, fminf(ty, tz));
+    float s_mus = s;  // adjoint: the hop length whose probability depends on mus
+    const float D_in = D;
+    const bool fixed_before = (st & kFixed) != 0;
+    {
+      const float absorb = M::absorbed(W, c.x * s);
+      W -= absorb;
+      Atot += absorb;
+      if (back) {
+        adj.at(P, i);
+        adj.L = fmaf(D, s, adj.L);
+      } else if (st & kBflag) {
+        dep.add(P.F3D, i, absorb);
+      }
+    }
+    sleft = sv ? 0.f : sleft - s * c.y;
+    if (sleft <= kLS) sleft = 0.f;
+    {
+      bool moved = false;
+      if (!TT && !sv) {  // surface detection (:556-637)
+        const float rel = (float)(P.ksurf - kz) * P.dz + (P.fsurf - fz);  // zsurf - z
+        const float su = s * uz;
+        const bool cross = (P.det_state == NMC_DET_REFLECTANCE && su <= rel && uz < 0.f) ||
+                           (P.det_state == NMC_DET_TRANSMITTANCE && su >= rel && uz > 0.f);
+        if (cross) {
+          const float dl_b = rel / uz;
+          if (back) {
+            if (sv)
+              s_mus = dl_b;
+            else
+              st |= kFixed;  // the rest of this hop is a fixed length
+          }
+          sleft = (s - dl_b) * c.y;
+          if (sleft <= kLS) sleft = 0.f;
+          fx = fmaf(dl_b, ux, fx);
+          fy = fmaf(dl_b, uy, fy);
+          norm_axis(kx, fx, P.dx, P.dxmax);
+          norm_axis(ky, fy, P.dy, P.dymax);
+          kz = P.ksurf;
+          fz = P.fsurf;
+          moved = true;
+          float uz_t = 0.f;
+          const float rsp = rfresnel(P.n1, P.n2, fabsf(uz), &uz_t);
+          if (rsp < 1.f) {
+            bool det = P.det_everything != 0;
+            const float gx = (float)kx * P.dx + fx, gy = (float)ky * P.dy + fy;
+            const float ro = sqrtf(gx * gx + gy * gy);
+            if (!det) {
+              const float th_exit = flt_eq(uz_t, 1.f) ? 0.f : kRAD_DEG * acosf(uz_t);
+              det = (ro >= P.r_min) && (ro <= P.r_max) && (th_exit <= P.na);
+            }
+            if (det) {
+              const float dw = W * (1.f - rsp);
+              const unsigned int rbin = (unsigned int)min((int)(ro * P.rd_idr), P.rd_bins);
+              if (back) {
+                const float e = P.adj_G[rbin] * dw;  // this event's score is now behind the photon
+                D -= e;
+                Dabs += fabsf(e);
+              } else {
+                const int jx = min(max(lookup_index(kx, fx, P.hx, P.ox, P.hdx), 0), P.Nx - 1);
+                const int jy = min(max(lookup_index(ky, fy, P.hy, P.oy, P.hdy), 0), P.Ny - 1);
+                Rd_loc += dw;
+                const unsigned int i2d = (unsigned int)(jx * P.Ny + jy);
+                atomicAdd(P.Rd2D + i2d, to_fix(dw));
+                atomicAdd(P.Det2D + i2d, 1u);
+                if (P.rd_r) atomicAdd(P.rd_r + rbin, to_fix(dw));
+                if (ADJ) {  // record pass: keep (photon, bin, weight) for the backward pass
+                  const unsigned long long k = atomicAdd(P.ev_count, 1ull);
+                  if (k < P.ev_cap) P.ev[k] = AdjEvent{(unsigned int)pidx, rbin, dw, 0.f};
+                }
+              }
+              if (TRACE) ++ndet;
+              uz = -uz;
+              W = W * rsp;
+            }
+          } else {
+            uz = -uz;
+            W = W * rsp;
+          }
+        }
+      }
+      if (!moved) {
+        fx = fmaf(s, ux, fx);
+        fy = fmaf(s, uy, fy);
+        fz = fmaf(s, uz, fz);
+        if (!sv) {
+          // the face the step aims at is crossed by exactly ls*|u| (as in FP64)
+          if (ax == 0) {
+            const bool p = ux >= 0.f;
+            kx += p ? 1 : -1;
+            fx = p ? kLS * ux : fminf(fmaf(kLS, ux, P.dx), P.dxmax);
+          } else if (ax == 1) {
+            const bool p = uy >= 0.f;
+            ky += p ? 1 : -1;
+            fy = p ? kLS * uy : fminf(fmaf(kLS, uy, P.dy), P.dymax);
+          } else {
+            const bool p = uz >= 0.f;
+            kz += p ? 1 : -1;
+            fz = p ? kLS * uz : fminf(fmaf(kLS, uz, P.dz), P.dzmax);
+          }
+        }
+        // offsets leave [0, d) only when a point lands on a face (an upper
+        // face of the same-voxel end point, a tie between faces)
+        if (fx < 0.f || fx >= P.dx || fy < 0.f || fy >= P.dy || fz < 0.f || fz >= P.dz) {
+          norm_axis(kx, fx, P.dx, P.dxmax);
+          norm_axis(ky, fy, P.dy, P.dymax);
+          norm_axis(kz, fz, P.dz, P.dzmax);
+        }
+      }
+    }
+    if (back && !fixed_before) adj.M = fmaf(-D_in, s_mus, adj.M);
+    if (!sv) {
+      // voxel index (:641-643): inside the grid this is the cell plus N/2
+      int ix = P.hx + kx + (P.ox ? (int)(fx >= P.hdx) : 0);
+      int iy = P.hy + ky + (P.oy ? (int)(fy >= P.hdy) : 0);
+      int iz = kz;
+      const bool inside = (unsigned)ix < (unsigned)P.Nx && (unsigned)iy < (unsigned)P.Ny &&
+                          (unsigned)iz < (unsigned)P.Nz;
+      if (!inside) {  // C truncation toward zero outside the grid
+        ix = lookup_index(kx, fx, P.hx, P.ox, P.hdx);
+        iy = lookup_index(ky, fy, P.hy, P.oy, P.hdy);
+        iz = lookup_index(kz, fz, 0, 0, 0.f);
+      }
+      if (TT) {  // :981-993
+        const float zrel = (float)(kz - P.ksurf) * P.dz + (fz - P.fsurf);  // z - zsurf
+        if (zrel < 0.f && (st & kSurf)) {
+          st &= ~kSurf;
+          Rd_loc += W;
+          if (TRACE) ++ndet;
+          const int jx = min(max(ix, 0), P.Nx - 1), jy = min(max(iy, 0), P.Ny - 1);
+          atomicAdd(P.Rd2D + (unsigned int)(jx * P.Ny + jy), to_fix(W));
+        }
+        if (kz < 0) {
+          kill(NMC_FATE_BOUNDARY);
+          sleft = 0.f;
+        }
+        st |= kBflag;
+      }
+      if (!inside) {  // boundary modes (:646-672)
+        const bool xo = (unsigned)ix >= (unsigned)P.Nx, yo = (unsigned)iy >= (unsigned)P.Ny;
+        const bool zlo = iz < 0, zhi = iz >= P.Nz;
+        ix = min(max(ix, 0), P.Nx - 1);
+        iy = min(max(iy, 0), P.Ny - 1);
+        iz = min(max(iz, 0), P.Nz - 1);
+        if (P.boundaryflag == 1) {
+          if (xo || yo || zlo || zhi) {
+            kill(NMC_FATE_BOUNDARY);
+            sleft = 0.f;
+          }
+        } else if (P.boundaryflag == 2 && zlo) {
+          kill(NMC_FATE_BOUNDARY);
+          sleft = 0.f;
+          if (xo || yo || zhi) st &= ~kBflag;
+        } else if (P.boundaryflag == 0 || P.boundaryflag == 2) {
+          if (xo || yo || zlo || zhi) st &= ~kBflag;
+        }
+      }
+      i = (unsigned int)(iz * NyNx + ix * P.Ny + iy);  // :675-679
+      if (!VOX) tiss = __ldg(P.V + i);
+    }
+    if (nsub >= P.step_cap) {  // device-side cap: not a reference behaviour
+      kill(NMC_FATE_STEPCAP);
+      atomicOr(&P.sums->flags, (unsigned int)NMC_DEVFLAG_STEPCAP);
+      continue;
+    }
+    if (depth <= kRAY_DEPTH && sleft > 0.f) continue;  // :685
+
+    // ---- SPIN (:688-731 / :1046-1097), ROULETTE (:733-748), next HOP (:501)
+    const bool need_roul = W < kTHRESHOLD;
+    const SpinDraws d = spin_draws<TT>(rng, need_roul, k0, k1);
+    float costheta;
+    if constexpr (VOX) {
+      const float4 cv = __ldg(P.vox + i);  // the voxel the photon scatters in
+      costheta = hg_from_g<FAST>(cv.w, d.a);
+      if (back) {
+        adj.at(P, i);
+        if (!(st & kFixed)) adj.M = fmaf(D, cv.z, adj.M);  // D / mus: density of the scattering point
+        if (!flt_eq(cv.w, 1.f)) adj.Q = fmaf(D, dlnhg_dg(cv.w, costheta), adj.Q);
+        st &= ~kFixed;
+      }
+    } else {
+      const PhaseConst& ph = s_ph[tiss];
+      costheta = TT ? tt_sample<FAST>(ph, d.a, d.b) : hg_sample<FAST>(ph, d.a);
+    }
+    spin<FAST>(costheta, TT ? d.c : d.b, ux, uy, uz);
+    ++nsc;
+    if (need_roul) {
+      if (d.roul <= kCHANCE)
+        W /= kCHANCE;
+      else
+        kill(NMC_FATE_ROULETTE);
+    }
+    if (hard_kill && (W < kMIN_VALUE || (int)nsc > kMAX_SCATT))
+      kill(W < kMIN_VALUE ? NMC_FATE_MINWEIGHT : NMC_FATE_MAXSCATT);
+    if (TRACE && nev < P.trace.k_events) {
+      P.trace.events[pidx * P.trace.k_events + nev] =
+          make_float4((float)kx * P.dx + fx, (float)ky * P.dy + fy, (float)kz * P.dz + fz, W);
+      ++nev;
+    }
+    sleft = M::neglog(d.step);
+    depth = 0;
+  }
+
+  __syncthreads();
+  if (threadIdx.x < 5 && s_tot[threadIdx.x]) {
+    unsigned long long* dst = threadIdx.x == 0   ? &P.sums->photons
+                              : threadIdx.x == 1 ? &P.sums->substeps
+                              : threadIdx.x == 2 ? &P.sums->scatters
+                              : threadIdx.x == 3 ? &P.sums->A
+                                                 : &P.sums->rd;
+    atomicAdd(dst, s_tot[threadIdx.x]);
+  }
+  if (threadIdx.x == 0 && s_rd2 != 0.0) atomicAdd(&P.sums->rd_sumsq, s_rd2);
+}
+
+}  // namespace
+}  // namespace nmc

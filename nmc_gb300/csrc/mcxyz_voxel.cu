@@ -1,0 +1,52 @@
+// mcxyz_voxel.cu - the voxel transport kernel for media with per-voxel
+// optical properties (no reference counterpart: the reference indexes at most
+// 18 tissue types through a uint8 map, definitions.h:57), forward and
+// perturbation Monte Carlo adjoint.  The kernel itself is in mcxyz_kernel.cuh.
+#include "mcxyz_kernel.cuh"
+
+namespace nmc {
+namespace {
+
+const void* pick_voxel(int mode, bool trace, bool fast) {
+  if (mode == kAdjoint)
+    return fast ? (const void*)mcxyz_kernel<false, PhiloxRng<false>, false, true, kAdjoint>
+                : (const void*)mcxyz_kernel<false, PhiloxRng<false>, false, false, kAdjoint>;
+  if (trace)
+    return fast ? (const void*)mcxyz_kernel<false, PhiloxRng<false>, true, true, kVoxel>
+                : (const void*)mcxyz_kernel<false, PhiloxRng<false>, true, false, kVoxel>;
+  return fast ? (const void*)mcxyz_kernel<false, PhiloxRng<false>, false, true, kVoxel>
+              : (const void*)mcxyz_kernel<false, PhiloxRng<false>, false, false, kVoxel>;
+}
+
+__global__ void adjoint_scores_kernel(const AdjEvent* __restrict__ ev, unsigned int n, const float* __restrict__ G,
+                                      float* __restrict__ D) {
+  for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const AdjEvent e = ev[k];
+    const float v = G[e.bin] * e.w;
+    if (v != 0.f) atomicAdd(D + e.photon, v);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_mcxyz_voxel(const XyzParams& p, int mode, bool trace, int grid, int block,
+                               cudaStream_t stream) {
+  const void* f = pick_voxel(mode, trace, p.fast_math != 0);
+  void* args[] = {(void*)&p};
+  return cudaLaunchKernel(f, dim3(grid), dim3(block), args, 0, stream);
+}
+
+cudaError_t mcxyz_voxel_occupancy(int mode, bool trace, int block, int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pick_voxel(mode, trace, true), block, 0);
+}
+
+cudaError_t launch_adjoint_scores(const AdjEvent* ev, unsigned int n_ev, const float* G, float* D,
+                                  cudaStream_t stream) {
+  if (n_ev == 0) return cudaSuccess;
+  const int block = 256;
+  const unsigned int grid = (n_ev + block - 1) / block < 4096u ? (n_ev + block - 1) / block : 4096u;
+  adjoint_scores_kernel<<<grid, block, 0, stream>>>(ev, n_ev, G, D);
+  return cudaGetLastError();
+}
+
+}  // namespace nmc

@@ -60,6 +60,16 @@ struct nmc_handle {
   uint32_t seen_flags = 0;
   nmc::XyzParams xp{};
   nmc::SubParams sp{};
+  // per-voxel media, radial tally, adjoint
+  bool voxel_mode = false;
+  float4* d_vox = nullptr;
+  int rd_bins = 0;
+  float rd_dr = 0.f;
+  unsigned long long* d_rdr = nullptr;
+  nmc::AdjEvent* d_ev = nullptr;
+  unsigned long long* d_evcount = nullptr;
+  uint64_t ev_cap = 0, ev_limit = 0, adj_first = 0, adj_n = 0;  // allocated / requested events
+  bool adj_ready = false;
 };
 
 namespace {
@@ -94,9 +104,17 @@ void free_buffers(nmc_handle* h) {
   dfree(h->d_J);
   dfree(h->d_F);
   dfree(h->d_stage);
+  dfree(h->d_vox);
+  dfree(h->d_rdr);
+  dfree(h->d_ev);
+  dfree(h->d_evcount);
   if (h->h_stage) cudaFreeHost(h->h_stage);
   h->h_stage = nullptr;
   h->nvox = h->n2d = h->nslots = h->nJ = h->nF = h->stage_elems = 0;
+  h->voxel_mode = false;
+  h->rd_bins = 0;
+  h->ev_cap = 0;
+  h->adj_ready = false;
 }
 
 bool finite_nonneg(float v) { return std::isfinite(v) && v >= 0.f; }
@@ -112,6 +130,10 @@ nmc_status build_xyz(nmc_handle* h) {
   p.rd_slots = h->d_slots;
   p.nslots = h->nslots;
   p.sums = h->d_sums;
+  p.vox = h->d_vox;
+  p.rd_r = h->d_rdr;
+  p.rd_bins = h->rd_bins;
+  p.rd_idr = h->rd_bins > 0 ? (float)(1.0 / h->rd_dr) : 0.f;
   return NMC_OK;
 }
 
@@ -206,10 +228,25 @@ EventPair get_pair(nmc_handle* h) {
   return p;
 }
 
+// Device buffers of one adjoint pass.
+struct AdjArgs {
+  int pass;  // 0 record, 1 backward
+  const float* D;
+  const float* G;
+  double* gL;
+  double* gM;
+  double* gQ;
+};
+
 nmc_status launch(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_record* d_recs,
-                  float4* d_events, uint32_t k_events) {
+                  float4* d_events, uint32_t k_events, const AdjArgs* adj = nullptr) {
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   if (n == 0) return NMC_OK;
+  if (adj && !h->voxel_mode) return fail(h, NMC_ESTATE, "the adjoint needs per-voxel properties");
+  if (h->voxel_mode && h->sim == NMC_SIM_MCXYZ_TT)
+    return fail(h, NMC_EUNSUPPORTED, "per-voxel media use the one-term HG kernel (NMC_SIM_MCXYZ)");
+  if (h->voxel_mode && h->ext.rng != NMC_RNG_PHILOX)
+    return fail(h, NMC_EUNSUPPORTED, "per-voxel media use the Philox streams");
   NMC_CUDA(h, cudaSetDevice(h->device));
   NMC_CUDA(h, cudaMemsetAsync(&h->d_sums->work, 0, sizeof(unsigned long long), h->stream));
   const bool trace = d_recs != nullptr;
@@ -234,14 +271,32 @@ nmc_status launch(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_record* 
     p.first = first;
     p.n = n;
     p.trace = tr;
+    if (adj) {
+      p.adj_pass = adj->pass;
+      p.ev = h->d_ev;
+      p.ev_count = h->d_evcount;
+      p.ev_cap = (unsigned int)std::min(h->ev_cap, h->ev_limit);
+      p.adj_D = adj->D;
+      p.adj_G = adj->G;
+      p.gL = adj->gL;
+      p.gM = adj->gM;
+      p.gQ = adj->gQ;
+    }
     block = h->ext.block_size > 0 ? h->ext.block_size : 256;
     const bool tt = h->sim == NMC_SIM_MCXYZ_TT;
-    NMC_CUDA(h, nmc::mcxyz_occupancy(tt, trace, block, &per_sm));
+    const int mode = adj ? nmc::kAdjoint : nmc::kVoxel;
+    if (h->voxel_mode)
+      NMC_CUDA(h, nmc::mcxyz_voxel_occupancy(mode, trace, block, &per_sm));
+    else
+      NMC_CUDA(h, nmc::mcxyz_occupancy(tt, trace, block, &per_sm));
     if (h->ext.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)h->ext.blocks_per_sm);
     if (per_sm < 1) return fail(h, NMC_EDEVICE, "mcxyz kernel does not fit on an SM with this block size");
     uint64_t grid = (uint64_t)h->nsm * per_sm;
     grid = std::min<uint64_t>(grid, (n + block - 1) / block);
-    NMC_CUDA(h, nmc::launch_mcxyz(p, tt, trace, (int)grid, block, h->stream));
+    if (h->voxel_mode)
+      NMC_CUDA(h, nmc::launch_mcxyz_voxel(p, mode, trace, (int)grid, block, h->stream));
+    else
+      NMC_CUDA(h, nmc::launch_mcxyz(p, tt, trace, (int)grid, block, h->stream));
   }
   NMC_CUDA(h, cudaEventRecord(ev.b, h->stream));
   h->pending.push_back(ev);
@@ -267,6 +322,8 @@ nmc_status sync_all(nmc_handle* h) {
   NMC_CUDA(h, cudaMemcpy(&flags, &h->d_sums->flags, sizeof flags, cudaMemcpyDeviceToHost));
   const unsigned int fresh = flags & ~h->seen_flags;
   h->seen_flags = flags;
+  if (fresh & NMC_DEVFLAG_REPLAY)
+    return fail(h, NMC_EDEVICE, "the adjoint replay did not reproduce the recorded detections");
   if (fresh & NMC_DEVFLAG_STEPCAP)
     return fail(h, NMC_ESTEPCAP, "a photon reached the device step cap and was terminated");
   return NMC_OK;
@@ -431,6 +488,7 @@ nmc_status nmc_reset(nmc_handle* h) {
   if (h->d_Rd2D) NMC_CUDA(h, cudaMemsetAsync(h->d_Rd2D, 0, h->n2d * 8, h->stream));
   if (h->d_Det) NMC_CUDA(h, cudaMemsetAsync(h->d_Det, 0, h->n2d * 4, h->stream));
   if (h->d_slots) NMC_CUDA(h, cudaMemsetAsync(h->d_slots, 0, h->nslots * 8, h->stream));
+  if (h->d_rdr) NMC_CUDA(h, cudaMemsetAsync(h->d_rdr, 0, ((size_t)h->rd_bins + 1) * 8, h->stream));
   h->kernel_ms = 0.0;
   h->launches = 0;
   h->seen_flags = 0;
@@ -506,6 +564,7 @@ size_t nmc_tally_size(nmc_handle* h, int32_t which) {
     case NMC_TALLY_RD2D: return h->n2d;
     case NMC_TALLY_DETPHOT2D: return h->n2d;
     case NMC_TALLY_RD_SLOTS: return h->nslots;
+    case NMC_TALLY_RD_R: return h->rd_bins > 0 ? (size_t)h->rd_bins + 1 : 0;
     default: return 0;
   }
 }
@@ -527,7 +586,8 @@ nmc_status nmc_get_tally_f64(nmc_handle* h, int32_t which, double* out, size_t n
                                   : which == NMC_TALLY_F ? h->d_F
                                   : which == NMC_TALLY_F3D ? h->d_F3D
                                   : which == NMC_TALLY_RD2D ? h->d_Rd2D
-                                                           : h->d_slots;
+                                  : which == NMC_TALLY_RD_R  ? h->d_rdr
+                                                             : h->d_slots;
   std::vector<unsigned long long> tmp(n);
   NMC_CUDA(h, cudaMemcpy(tmp.data(), src, n * 8, cudaMemcpyDeviceToHost));
   for (size_t k = 0; k < n; ++k) out[k] = (double)tmp[k] * nmc::kUnfix;
@@ -729,6 +789,126 @@ nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_set
     o[NMC_SWEEP_RD_SE] = n > 1 ? std::sqrt(std::max(0.0, e2[s] / n - me * me) / n) : 0.0;
   }
   return cleanup(st);
+}
+
+nmc_status nmc_set_voxel_props(nmc_handle* h, const float* mua, const float* mus, const float* g) {
+  if (!h || !mua || !mus) return fail(h, NMC_EINVAL, "null argument");
+  if (h->sim != NMC_SIM_MCXYZ) return fail(h, NMC_EINVAL, "per-voxel media need an NMC_SIM_MCXYZ handle");
+  if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
+  nmc_status st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  std::vector<float4> v(h->nvox);
+  const float g1 = h->tp.gv[1];
+  for (size_t k = 0; k < h->nvox; ++k) {
+    const float a = mua[k], s = mus[k], gg = g ? g[k] : g1;
+    if (!std::isfinite(a) || a < 0.f || !std::isfinite(s) || !(s > 0.f) || !std::isfinite(gg) || !(gg > -1.f) ||
+        !(gg < 1.f)) {
+      char msg[128];
+      std::snprintf(msg, sizeof msg, "voxel %zu: need mua >= 0, mus > 0, -1 < g < 1 (got %g, %g, %g)", k, a, s, gg);
+      return fail(h, NMC_EINVAL, msg);
+    }
+    v[k] = make_float4(a, s, (float)(1.0 / s), gg);
+  }
+  if (!h->d_vox) NMC_CUDA(h, cudaMalloc((void**)&h->d_vox, h->nvox * sizeof(float4)));
+  NMC_CUDA(h, cudaMemcpy(h->d_vox, v.data(), h->nvox * sizeof(float4), cudaMemcpyHostToDevice));
+  h->voxel_mode = true;
+  h->adj_ready = false;
+  return build_xyz(h);
+}
+
+nmc_status nmc_set_radial_tally(nmc_handle* h, int32_t bins, float dr) {
+  if (!h) return NMC_EINVAL;
+  if (h->sim == NMC_SIM_MCSUB) return fail(h, NMC_EINVAL, "the radial tally is for voxel kinds (mcsub has J)");
+  if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
+  if (bins < 1 || bins > 65536 || !(dr > 0.f) || !std::isfinite(dr))
+    return fail(h, NMC_EINVAL, "radial tally needs 1 <= bins <= 65536 and dr > 0");
+  nmc_status st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  dfree(h->d_rdr);
+  NMC_CUDA(h, cudaMalloc((void**)&h->d_rdr, ((size_t)bins + 1) * 8));
+  NMC_CUDA(h, cudaMemset(h->d_rdr, 0, ((size_t)bins + 1) * 8));
+  h->rd_bins = bins;
+  h->rd_dr = dr;
+  return build_xyz(h);
+}
+
+nmc_status nmc_adjoint_forward(nmc_handle* h, uint64_t first, uint64_t n, uint64_t event_capacity) {
+  if (!h) return NMC_EINVAL;
+  if (!h->prepared || !h->voxel_mode) return fail(h, NMC_ESTATE, "the adjoint needs nmc_set_voxel_props");
+  if (h->rd_bins < 1) return fail(h, NMC_ESTATE, "the adjoint differentiates the radial tally: nmc_set_radial_tally");
+  if (n >= 0xFFFFFFFFull || event_capacity == 0 || event_capacity >= 0xFFFFFFFFull)
+    return fail(h, NMC_EINVAL, "adjoint runs need n < 2^32 photons and 0 < event_capacity < 2^32");
+  nmc_status st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  if (h->ev_cap < event_capacity) {
+    dfree(h->d_ev);
+    NMC_CUDA(h, cudaMalloc((void**)&h->d_ev, event_capacity * sizeof(nmc::AdjEvent)));
+    h->ev_cap = event_capacity;
+  }
+  h->ev_limit = event_capacity;
+  if (!h->d_evcount) NMC_CUDA(h, cudaMalloc((void**)&h->d_evcount, sizeof(unsigned long long)));
+  NMC_CUDA(h, cudaMemsetAsync(h->d_evcount, 0, sizeof(unsigned long long), h->stream));
+  AdjArgs a{0, nullptr, nullptr, nullptr, nullptr, nullptr};
+  st = launch(h, first, n, nullptr, nullptr, 0, &a);
+  if (st == NMC_OK) st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  unsigned long long cnt = 0;
+  NMC_CUDA(h, cudaMemcpy(&cnt, h->d_evcount, sizeof cnt, cudaMemcpyDeviceToHost));
+  if (cnt > h->ev_limit) {
+    h->adj_ready = false;
+    char msg[128];
+    std::snprintf(msg, sizeof msg, "%llu detection events exceed event_capacity %llu", cnt,
+                  (unsigned long long)h->ev_limit);
+    return fail(h, NMC_EINVAL, msg);
+  }
+  h->adj_first = first;
+  h->adj_n = n;
+  h->adj_ready = true;
+  return st;
+}
+
+nmc_status nmc_adjoint_backward(nmc_handle* h, const float* grad_rd_r, double* grad_mua, double* grad_mus,
+                                double* grad_g) {
+  if (!h || !grad_rd_r) return fail(h, NMC_EINVAL, "null argument");
+  if (!h->adj_ready) return fail(h, NMC_ESTATE, "nmc_adjoint_forward has not completed");
+  nmc_status st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  unsigned long long cnt = 0;
+  NMC_CUDA(h, cudaMemcpy(&cnt, h->d_evcount, sizeof cnt, cudaMemcpyDeviceToHost));
+  const size_t nb = (size_t)h->rd_bins + 1, nv = h->nvox;
+  char* base = nullptr;
+  const size_t bD = h->adj_n * 4, bG = nb * 4, bg = nv * 8;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  NMC_CUDA(h, cudaMalloc((void**)&base, al(bD) + al(bG) + 3 * al(bg)));
+  float* D = (float*)base;
+  float* G = (float*)(base + al(bD));
+  double* gL = (double*)(base + al(bD) + al(bG));
+  double* gM = (double*)((char*)gL + al(bg));
+  double* gQ = (double*)((char*)gM + al(bg));
+  auto done = [&](nmc_status s) {
+    cudaFree(base);
+    return s;
+  };
+  if (cudaMemsetAsync(D, 0, bD, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync(G, grad_rd_r, bG, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+      cudaMemsetAsync(gL, 0, 3 * al(bg), h->stream) != cudaSuccess ||
+      nmc::launch_adjoint_scores(h->d_ev, (unsigned int)cnt, G, D, h->stream) != cudaSuccess)
+    return done(fail(h, NMC_EDEVICE, "adjoint set-up"));
+  AdjArgs a{1, D, G, gL, gM, gQ};
+  st = launch(h, h->adj_first, h->adj_n, nullptr, nullptr, 0, &a);
+  if (st == NMC_OK) st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return done(st);
+  std::vector<double> L(nv), M(nv), Q(nv);
+  if (cudaMemcpy(L.data(), gL, bg, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(M.data(), gM, bg, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(Q.data(), gQ, bg, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return done(fail(h, NMC_EDEVICE, "adjoint results"));
+  for (size_t k = 0; k < nv; ++k) {
+    if (grad_mua) grad_mua[k] = -L[k];
+    if (grad_mus) grad_mus[k] = M[k];
+    if (grad_g) grad_g[k] = Q[k];
+  }
+  return done(st);
 }
 
 void* nmc_stream(nmc_handle* h) { return h ? (void*)h->stream : nullptr; }

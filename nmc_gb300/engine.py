@@ -66,10 +66,15 @@ def lib() -> C.CDLL:
         L.nmc_probe_issue_peaks.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.nmc_run_sweep.argtypes = [H, C.POINTER(abi.SweepSet), C.c_int32, _P, _P]
         L.nmc_run_sweep.restype = C.c_int
+        L.nmc_set_voxel_props.argtypes = [H, _P, _P, _P]
+        L.nmc_set_radial_tally.argtypes = [H, C.c_int32, C.c_float]
+        L.nmc_adjoint_forward.argtypes = [H, C.c_uint64, C.c_uint64, C.c_uint64]
+        L.nmc_adjoint_backward.argtypes = [H, _P, _P, _P, _P]
         for name in ("nmc_create", "nmc_prepare", "nmc_set_ext", "nmc_set_num_runs_seed",
                      "nmc_send_compute_command", "nmc_run", "nmc_run_async", "nmc_synchronize",
                      "nmc_run_traced", "nmc_get_compute_results", "nmc_get_summary",
-                     "nmc_get_tally_f64", "nmc_reset"):
+                     "nmc_get_tally_f64", "nmc_reset", "nmc_set_voxel_props", "nmc_set_radial_tally",
+                     "nmc_adjoint_forward", "nmc_adjoint_backward"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -204,6 +209,38 @@ class Engine:
         if with_J:
             res["J"] = J
         return res
+
+    # -- per-voxel media and the perturbation Monte Carlo adjoint
+    def set_voxel_props(self, mua, mus, g=None):
+        """Per-voxel mua, mus (1/cm) and HG g, arrays of Nz x Nx x Ny (the
+        engine's voxel order iz*Ny*Nx + ix*Ny + iy) or flat."""
+        a = np.ascontiguousarray(mua, dtype=np.float32).ravel()
+        s = np.ascontiguousarray(mus, dtype=np.float32).ravel()
+        gg = None if g is None else np.ascontiguousarray(g, dtype=np.float32).ravel()
+        n = self.rp.Nx * self.rp.Ny * self.rp.Nz
+        if a.size != n or s.size != n or (gg is not None and gg.size != n):
+            raise ValueError(f"per-voxel arrays need {n} values")
+        self._check(self._L.nmc_set_voxel_props(self._h, _ptr(a), _ptr(s), _ptr(gg)), "nmc_set_voxel_props")
+
+    def set_radial_tally(self, bins: int, dr: float):
+        self._check(self._L.nmc_set_radial_tally(self._h, int(bins), float(dr)), "nmc_set_radial_tally")
+
+    def adjoint_forward(self, first: int, n: int, event_capacity: int | None = None):
+        cap = int(event_capacity) if event_capacity else max(1 << 20, 4 * int(n))
+        self._check(self._L.nmc_adjoint_forward(self._h, int(first), int(n), cap), "nmc_adjoint_forward")
+
+    def adjoint_backward(self, grad_rd_r):
+        """(grad_mua, grad_mus, grad_g) per voxel for the upstream gradient of
+        the un-normalised radial tally (bins + 1 values)."""
+        G = np.ascontiguousarray(grad_rd_r, dtype=np.float32).ravel()
+        nb = self._L.nmc_tally_size(self._h, abi.TALLY_RD_R)
+        if G.size != nb:
+            raise ValueError(f"grad_rd_r needs {nb} values")
+        n = self.rp.Nx * self.rp.Ny * self.rp.Nz
+        ga, gs, gg = (np.zeros(n, np.float64) for _ in range(3))
+        self._check(self._L.nmc_adjoint_backward(self._h, _ptr(G), _ptr(ga), _ptr(gs), _ptr(gg)),
+                    "nmc_adjoint_backward")
+        return ga, gs, gg
 
     @property
     def stream(self) -> int:

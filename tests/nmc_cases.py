@@ -130,3 +130,38 @@ def spectral_sweep_sets(n_wavelengths: int = 351, seed: int = 2024, budget_lo: f
         sets.append(abi.SweepSet(mua=float(mua[i]), mus=float(mus[i]), g=g_eff, gf=gf, af=af, gb=gb, ab=ab,
                                  cc=cc, n1=n1, n2=n2, pad=0, photons=int(budgets[i])))
     return lam, sets
+
+
+def smooth_noise(shape, seed: int, sigma: float) -> np.ndarray:
+    """Seeded white noise smoothed by a periodic Gaussian of `sigma` voxels
+    (FFT), rescaled to [0, 1]."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal(shape)
+    k = [np.fft.fftfreq(n) for n in shape]
+    kk = sum(np.meshgrid(*[(2 * np.pi * f) ** 2 for f in k], indexing="ij"))
+    s = np.real(np.fft.ifftn(np.fft.fftn(w) * np.exp(-0.5 * sigma ** 2 * kk)))
+    return (s - s.min()) / (s.max() - s.min())
+
+
+def adjoint_case(N: int = 64, d: float = 0.01, seed: int = 7, sigma: float = 4.0, bins: int = 128,
+                 dr: float = 0.005):
+    """Per-voxel medium for the adjoint: N^3 voxels of d cm; mua log-uniform
+    over smoothed seeded noise in [0.1, 5] /cm, mus linear in [50, 300] /cm
+    (an independent noise field), g = 0.85 everywhere; tissue n = 1.4 under
+    air; normal pencil beam at the origin of the top face (launchflag 1);
+    photons leaving the grid are killed (boundaryflag 1); Rd(r) in `bins`
+    bins of `dr` cm plus overflow.  Returns (rp, tp, v, ext, mua, mus, g,
+    bins, dr) with the property arrays shaped [iz, ix, iy]."""
+    rp = abi.run_params(myname="adjoint", Nx=N, Ny=N, Nz=N, dx=d, dy=d, dz=d, mcflag=0, launchflag=1,
+                        boundaryflag=1, xs=0.0, ys=0.0, zs=0.0, xfocus=0.0, yfocus=0.0, zfocus=float("inf"),
+                        ux0=0.0, uy0=0.0, uz0=1.0, radius=0.0, waist=0.0, zsurf=0.0, det_radius=15.0, xd=0.0,
+                        n1=1.4, n2=1.0, na=90.0, det_state=0, mckernelflag=abi.SIM_MCXYZ, Nt=1)
+    tp = abi.tissue_params(mua=[1.0], mus=[100.0], g=[0.85])
+    v = np.ones(N * N * N, np.uint8)
+    ext = abi.ext_defaults(rng=abi.RNG_PHILOX, seed=seed)
+    ua = smooth_noise((N, N, N), seed, sigma)
+    us = smooth_noise((N, N, N), seed + 1, sigma)
+    mua = (0.1 * 50.0 ** ua).astype(np.float32)
+    mus = (50.0 + 250.0 * us).astype(np.float32)
+    g = np.full((N, N, N), 0.85, np.float32)
+    return rp, tp, v, ext, mua, mus, g, bins, dr

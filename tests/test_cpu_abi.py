@@ -3,6 +3,8 @@ import ctypes as C
 import os
 import re
 
+import numpy as np
+
 import pytest
 
 from nmc_gb300 import abi
@@ -76,3 +78,15 @@ def test_null_handle_calls_do_not_crash(engine_lib):
     assert L.nmc_reset(None) == 1
     assert L.nmc_last_error(None) == b"null handle"
     L.nmc_destroy(None)
+
+
+def test_adjoint_case_and_autograd_module_import():
+    import nmc_cases as cases
+    from nmc_gb300 import autograd
+
+    rp, tp, v, ext, mua, mus, g, bins, dr = cases.adjoint_case(N=16)
+    assert mua.shape == (16, 16, 16) and mua.dtype == np.float32
+    assert 0.1 - 1e-6 <= mua.min() and mua.max() <= 5.0 + 1e-5
+    assert 50.0 - 1e-4 <= mus.min() and mus.max() <= 300.0 + 1e-3
+    assert np.all(g == np.float32(0.85))
+    assert callable(autograd.radial_reflectance)

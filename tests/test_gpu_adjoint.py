@@ -1,0 +1,200 @@
+"""Per-voxel media and the perturbation Monte Carlo adjoint of Rd(r).
+
+The adjoint's gradients are checked against central finite differences with
+common random numbers (the same photon streams at mu -/+ delta) on 32 voxels
+around the beam entry of a 64^3 heterogeneous medium, batch by batch, so that
+each comparison carries its own standard error.  mua is pathwise (the
+trajectories do not depend on it) and must agree to 1e-3 relative; mus and g
+are likelihood-ratio estimates and must agree within 4.5 standard errors of
+the batch means, voxel by voxel and summed.
+"""
+import time
+
+import numpy as np
+import pytest
+
+from nmc_gb300 import abi
+import nmc_cases as cases
+
+pytestmark = pytest.mark.gpu
+
+VOXELS = [(iz, ix, iy) for iz in range(4) for ix in (30, 31, 32, 33) for iy in (31, 32)]
+
+
+def _engine(gpu, case):
+    rp, tp, v, ext, mua, mus, g, bins, dr = case
+    e = gpu.Engine(abi.SIM_MCXYZ, 0, ext)
+    e.prepare_data(rp, tp, v)
+    e.set_radial_tally(bins, dr)
+    e.set_voxel_props(mua, mus, g)
+    return e
+
+
+@pytest.fixture(scope="module")
+def case():
+    return cases.adjoint_case()
+
+
+def _upstream(bins):
+    G = np.random.default_rng(3).uniform(0.5, 1.5, bins + 1).astype(np.float32)
+    G[-1] = 0.0  # overflow bin carries no loss
+    return G
+
+
+def test_adjoint_matches_crn_finite_differences(gpu, case):
+    rp, tp, v, ext, mua, mus, g, bins, dr = case
+    N = rp.Nx
+    flat = np.array([iz * N * N + ix * N + iy for iz, ix, iy in VOXELS])
+    G = _upstream(bins)
+    B, nb = 16, 500_000
+    with _engine(gpu, case) as e:
+        pm = {k: np.zeros((B, len(flat))) for k in "asg"}
+        for b in range(B):
+            e.reset()
+            e.adjoint_forward(b * nb, nb)
+            ga, gs, gg = e.adjoint_backward(G)
+            pm["a"][b], pm["s"][b], pm["g"][b] = ga[flat], gs[flat], gg[flat]
+        fd = {k: np.zeros((B, len(flat))) for k in "asg"}
+        for k, arr, step in (("a", mua, lambda x: 0.02 * x), ("s", mus, lambda x: 0.02 * x),
+                             ("g", g, lambda x: 0.01)):
+            for j, fi in enumerate(flat):
+                base = float(arr.ravel()[fi])
+                h = step(base)
+                sides = []
+                for sgn in (1.0, -1.0):
+                    a2 = arr.copy().ravel()
+                    a2[fi] = base + sgn * h
+                    props = {"a": (a2, mus, g), "s": (mua, a2, g), "g": (mua, mus, a2)}[k]
+                    e.set_voxel_props(*[p.ravel() for p in props])
+                    sc = []
+                    for b in range(B):
+                        e.reset()
+                        e.run(b * nb, nb)
+                        sc.append(float(G.astype(np.float64) @ e.tally(abi.TALLY_RD_R)))
+                    sides.append(np.array(sc))
+                fd[k][:, j] = (sides[0] - sides[1]) / (2.0 * h)
+    for k in "asg":
+        d = pm[k] - fd[k]
+        se = d.std(0, ddof=1) / np.sqrt(B)
+        P, F = pm[k].mean(0), fd[k].mean(0)
+        t = d.mean(0) / se
+        tot = d.sum(1)
+        t_tot = tot.mean() / (tot.std(ddof=1) / np.sqrt(B))
+        print(f"{k}: corr {np.corrcoef(P, F)[0, 1]:.4f} max|t| {np.abs(t).max():.2f} total t {t_tot:.2f}")
+        if k == "a":
+            # pathwise: same trajectories, differences are the fast exp's
+            # slope and roulette flips
+            assert np.all(np.abs(P - F) <= np.maximum(4.5 * se, 1e-3 * np.abs(F))), (P, F)
+        else:
+            assert np.all(np.abs(t) <= 4.5), (k, t)
+            assert abs(t_tot) <= 4.5
+            assert np.corrcoef(P, F)[0, 1] >= 0.98
+
+
+def test_adjoint_is_linear_in_the_upstream_gradient(gpu, case):
+    bins = case[7]
+    G1 = _upstream(bins)
+    G2 = np.zeros(bins + 1, np.float32)
+    G2[5:40] = 1.0
+    with _engine(gpu, case) as e:
+        e.adjoint_forward(0, 200_000)
+        r1 = e.adjoint_backward(G1)
+        r2 = e.adjoint_backward(G2)
+        r12 = e.adjoint_backward(G1 + G2)
+    for a, b, c in zip(r1, r2, r12):
+        scale = np.abs(a).max() + np.abs(b).max()
+        np.testing.assert_allclose(a + b, c, rtol=0, atol=1e-4 * scale)
+
+
+def test_radial_tally_and_events(gpu, case):
+    with _engine(gpu, case) as e:
+        n = 200_000
+        e.adjoint_forward(0, n)
+        rd = e.tally(abi.TALLY_RD_R)
+        sm = e.summary()
+        assert rd.size == case[7] + 1
+        # the radial bins hold every detected weight
+        assert rd.sum() == pytest.approx(sm["rd_sum"], rel=1e-5)
+        # the record pass tallies like a plain run of the same photons (the
+        # two kernels are compiled apart: a rare photon may round differently)
+        e.reset()
+        e.run(0, n)
+        plain = e.tally(abi.TALLY_RD_R)
+        print("record vs plain: max bin difference", np.abs(plain - rd).max() / rd.max())
+        np.testing.assert_allclose(plain, rd, rtol=0, atol=1e-3 * rd.max())
+        # too small an event list is an error, and the handle stays usable
+        e.reset()
+        with pytest.raises(gpu.NMCError):
+            e.adjoint_forward(0, n, event_capacity=100)
+        with pytest.raises(gpu.NMCError):
+            e.adjoint_backward(_upstream(case[7]))
+        e.adjoint_forward(0, 1000)
+        e.adjoint_backward(_upstream(case[7]))
+
+
+def test_voxel_media_match_the_tissue_map(gpu):
+    # the same medium given as a tissue map and as per-voxel properties; a
+    # beam of finite radius (no photon starts exactly on a voxel face, where
+    # the two modes' same-voxel rules differ)
+    rp, tp, v, ext = cases.skin_vessel_case(N=64, d=0.005)
+    gv = [0.9, 0.9, 0.9, 0.9]
+    mua_t, mus_t = [0.0001, 20.0, 0.5, 230.0], [1.0, 300.0, 200.0, 200.0]
+    tp = abi.tissue_params(mua=mua_t, mus=mus_t, g=gv)
+    vi = v.astype(np.int64) - 1
+    mua = np.asarray(mua_t, np.float32)[vi]
+    mus = np.asarray(mus_t, np.float32)[vi]
+    g = np.asarray(gv, np.float32)[vi]
+    n = 20_000
+    with gpu.Engine(abi.SIM_MCXYZ, 0, ext) as e:
+        e.prepare_data(rp, tp, v)
+        recs_t, _ = e.run_traced(0, n)
+        e.set_voxel_props(mua, mus, g)
+        recs_v, _ = e.run_traced(0, n)
+    frac, _ = cases.match_fraction(recs_t, recs_v)
+    print("per-photon agreement", frac)
+    assert frac >= 0.97
+
+
+def test_autograd_function(gpu, case):
+    torch = pytest.importorskip("torch")
+    from nmc_gb300.autograd import radial_reflectance
+
+    rp, tp, v, ext, mua, mus, g, bins, dr = case
+    n = 200_000
+    w = torch.linspace(1.0, 0.0, bins + 1, dtype=torch.float64)
+    with _engine(gpu, case) as e:
+        ta = torch.tensor(mua, dtype=torch.float64, requires_grad=True)
+        ts = torch.tensor(mus, dtype=torch.float64, requires_grad=True)
+        tg = torch.tensor(g, dtype=torch.float64, requires_grad=True)
+        rd = radial_reflectance(ta, ts, tg, e, 0, n)
+        assert rd.shape == (bins + 1,)
+        # another forward on the same handle before backward: the first is
+        # recorded again
+        radial_reflectance(ta * 1.1, ts, tg, e, 0, n)
+        (rd * w).sum().backward()
+        e.set_voxel_props(mua, mus, g)
+        e.reset()
+        e.adjoint_forward(0, n)
+        ga, gs, gg = e.adjoint_backward((w.numpy() / n).astype(np.float32))
+        rd_direct = e.tally(abi.TALLY_RD_R) / n
+    np.testing.assert_allclose(rd.detach().numpy(), rd_direct, rtol=1e-6)
+    for t, ref in ((ta, ga), (ts, gs), (tg, gg)):
+        np.testing.assert_allclose(t.grad.numpy().ravel(), ref, rtol=1e-5, atol=1e-9 * np.abs(ref).max())
+
+
+def test_adjoint_costs_at_most_three_forwards(gpu, case):
+    G = _upstream(case[7])
+    n = 2_000_000
+    with _engine(gpu, case) as e:
+        e.run(0, n)  # warm-up
+        e.adjoint_forward(0, n)
+        e.adjoint_backward(G)
+        t0 = time.perf_counter()
+        e.run(0, n)
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        e.adjoint_forward(0, n)
+        e.adjoint_backward(G)
+        t_adj = time.perf_counter() - t0
+    print(f"forward {t_fwd * 1e3:.1f} ms, record + backward {t_adj * 1e3:.1f} ms, ratio {t_adj / t_fwd:.2f}")
+    assert t_adj <= 3.0 * t_fwd
