@@ -349,6 +349,14 @@ nmc_status nmc_set_radial_tally(nmc_handle* h, int32_t bins, float dr);
 nmc_status nmc_adjoint_forward(nmc_handle* h, uint64_t first, uint64_t n, uint64_t event_capacity);
 nmc_status nmc_adjoint_backward(nmc_handle* h, const float* grad_rd_r, double* grad_mua,
                                 double* grad_mus, double* grad_g);
+/* As nmc_adjoint_backward, with the upstream gradient of the absorbed-weight
+ * tally too (NMC_TALLY_F3D of the forward's photons, Nx*Ny*Nz floats; the
+ * fluence is that tally / (mua * photons * voxel volume), whose chain rule
+ * stays with the caller).  Either gradient may be NULL, not both.  With a
+ * deposit gradient the detected photons are not enough: every photon is
+ * replayed twice (its total score first, then the accumulation). */
+nmc_status nmc_adjoint_backward_ex(nmc_handle* h, const float* grad_rd_r, const float* grad_absorbed,
+                                   double* grad_mua, double* grad_mus, double* grad_g);
 
 /* ------------------------------------------------------- batched sweeps */
 /* One parameter set of a batched sweep (e.g. one wavelength) on the mcsub

@@ -1,14 +1,19 @@
-"""Differentiable radial reflectance for per-voxel media.
+"""Differentiable transport through per-voxel media.
 
-``radial_reflectance(mua, mus, g, engine, first, n)`` returns Rd(r) — the
-weight detected at the detection plane per launched photon, binned by the
-distance from the z axis (``engine.set_radial_tally`` bins plus one overflow
-bin) — as a torch tensor whose gradient with respect to the per-voxel
-absorption ``mua``, scattering ``mus`` and anisotropy ``g`` is the
-perturbation Monte Carlo adjoint of the same photons (``nmc_adjoint_forward``
-/ ``nmc_adjoint_backward`` in include/nmc_abi.h):
+``transport(mua, mus, g, engine, first, n)`` runs photons [first, first+n)
+and returns, per launched photon,
 
-* d/dmua: pathwise, the detected weight carries exp(-sum mua * path);
+* ``rd_r``: the weight detected at the detection plane binned by the distance
+  from the z axis (``engine.set_radial_tally`` bins plus one overflow bin);
+* ``absorbed``: the weight deposited in each voxel (NMC_TALLY_F3D, shaped
+  like ``mua``); ``fluence(absorbed, mua, dV)`` turns it into fluence;
+
+as torch tensors whose gradients with respect to the per-voxel absorption
+``mua``, scattering ``mus`` and anisotropy ``g`` are the perturbation Monte
+Carlo adjoint of the same photons (``nmc_adjoint_forward`` /
+``nmc_adjoint_backward_ex`` in include/nmc_abi.h):
+
+* d/dmua: pathwise, the weight carries exp(-sum mua * path);
 * d/dmus, d/dg: likelihood ratio of the sampled scattering points and angles.
 
 The reference has no gradient path (it tallies forward only, kernels.metal
@@ -26,7 +31,7 @@ from . import abi
 from .engine import Engine
 
 
-class _RadialReflectance(torch.autograd.Function):
+class _Transport(torch.autograd.Function):
     @staticmethod
     def forward(ctx, mua, mus, g, engine: Engine, first: int, n: int, event_capacity: int | None):
         ctx.engine, ctx.first, ctx.n, ctx.cap = engine, int(first), int(n), event_capacity
@@ -35,10 +40,12 @@ class _RadialReflectance(torch.autograd.Function):
         _forward(engine, mua, mus, g, first, n, event_capacity)
         ctx.token = engine._adj_token
         rd = engine.tally(abi.TALLY_RD_R) / float(n)
-        return torch.as_tensor(rd, dtype=mua.dtype, device=mua.device)
+        ab = engine.tally(abi.TALLY_F3D) / float(n)
+        kw = dict(dtype=mua.dtype, device=mua.device)
+        return torch.as_tensor(rd, **kw), torch.as_tensor(ab.reshape(ctx.shape), **kw)
 
     @staticmethod
-    def backward(ctx, grad_rd):
+    def backward(ctx, grad_rd, grad_ab):
         e: Engine = ctx.engine
         if getattr(e, "_adj_token", None) != ctx.token:
             # the handle ran another forward since: record this one again
@@ -46,16 +53,27 @@ class _RadialReflectance(torch.autograd.Function):
             mua, mus, g = ctx.saved_tensors
             _forward(e, mua, mus, g, ctx.first, ctx.n, ctx.cap)
             ctx.token = e._adj_token
-        G = grad_rd.detach().to("cpu", torch.float64).numpy() / float(ctx.n)
-        ga, gs, gg = e.adjoint_backward(G.astype(np.float32))
-        mua = ctx.saved_tensors[0]
 
-        def out(a, need):
-            if not need:
+        def host(t):
+            if t is None:
+                return None
+            a = t.detach().to("cpu", torch.float64).numpy().ravel() / float(ctx.n)
+            return a.astype(np.float32) if np.any(a) else None
+
+        G, GF = host(grad_rd), host(grad_ab)
+        mua = ctx.saved_tensors[0]
+        need = ctx.needs_input_grad
+        if G is None and GF is None:
+            z = torch.zeros_like(mua)
+            return (z if need[0] else None, z if need[1] else None, z if need[2] else None,
+                    None, None, None, None)
+        ga, gs, gg = e.adjoint_backward(G, GF)
+
+        def out(a, want):
+            if not want:
                 return None
             return torch.as_tensor(a.reshape(ctx.shape), dtype=mua.dtype, device=mua.device)
 
-        need = ctx.needs_input_grad
         return out(ga, need[0]), out(gs, need[1]), out(gg, need[2]), None, None, None, None
 
 
@@ -69,13 +87,27 @@ def _forward(e: Engine, mua, mus, g, first, n, cap):
     e._adj_token = getattr(e, "_adj_token", 0) + 1
 
 
-def radial_reflectance(mua: torch.Tensor, mus: torch.Tensor, g: torch.Tensor, engine: Engine,
-                       first: int = 0, n: int = 1_000_000, event_capacity: int | None = None) -> torch.Tensor:
-    """Rd(r) per launched photon (bins + 1 values, last = overflow) of photons
-    [first, first + n) through per-voxel media (arrays of Nz x Nx x Ny or flat,
-    engine voxel order), differentiable in mua, mus and g.  `engine` is an
-    NMC_SIM_MCXYZ Engine after prepare_data and set_radial_tally; its other
-    tallies hold this forward's photons afterwards."""
+def transport(mua: torch.Tensor, mus: torch.Tensor, g: torch.Tensor, engine: Engine, first: int = 0,
+              n: int = 1_000_000, event_capacity: int | None = None):
+    """(rd_r, absorbed) per launched photon for photons [first, first + n)
+    through per-voxel media (arrays of Nz x Nx x Ny or flat, engine voxel
+    order), differentiable in mua, mus and g.  `engine` is an NMC_SIM_MCXYZ
+    Engine after prepare_data and set_radial_tally; its other tallies hold
+    this forward's photons afterwards."""
     if engine.sim_type != abi.SIM_MCXYZ:
-        raise ValueError("radial_reflectance needs an NMC_SIM_MCXYZ engine")
-    return _RadialReflectance.apply(mua, mus, g, engine, first, n, event_capacity)
+        raise ValueError("transport needs an NMC_SIM_MCXYZ engine")
+    return _Transport.apply(mua, mus, g, engine, first, n, event_capacity)
+
+
+def radial_reflectance(mua, mus, g, engine: Engine, first: int = 0, n: int = 1_000_000,
+                       event_capacity: int | None = None) -> torch.Tensor:
+    """Rd(r) per launched photon (bins + 1 values, last = overflow)."""
+    return transport(mua, mus, g, engine, first, n, event_capacity)[0]
+
+
+def fluence(absorbed: torch.Tensor, mua: torch.Tensor, voxel_volume: float) -> torch.Tensor:
+    """Fluence per launched photon (1/cm^2) from the absorbed weight per
+    voxel: absorbed / (mua * voxel volume), the normalisation the reference
+    applies to F3D before writing _F.bin (main.m:271-281).  Voxels with
+    mua = 0 give 0."""
+    return torch.where(mua > 0, absorbed / (mua.clamp_min(1e-30) * voxel_volume), torch.zeros_like(absorbed))

@@ -57,12 +57,14 @@ struct XyzParams {
   int rd_bins;
   float rd_idr;
   // perturbation Monte Carlo adjoint
-  int adj_pass;               // 0: record detection events, 1: backward replay
+  int adj_pass;               // 0: record detection events, 1: accumulating replay, 2: score replay
   AdjEvent* ev;
   unsigned long long* ev_count;
   unsigned int ev_cap;
-  const float* adj_D;         // per photon detected score (backward)
-  const float* adj_G;         // upstream gradient per radial bin (backward)
+  const float* adj_D;         // per photon score (accumulating replay)
+  float* adj_Dw;              // per photon score (written by the score replay)
+  const float* adj_G;         // upstream gradient per radial bin (replays)
+  const float* adj_GF;        // upstream gradient per voxel of F3D, or null (replays)
   double* gL;                 // per voxel: sum D * charged path length (absorption)
   double* gM;                 // per voxel: d ln p(path)/dmus terms weighted by D
   double* gQ;                 // per voxel: sum D * dln p_HG / dg over scatterings

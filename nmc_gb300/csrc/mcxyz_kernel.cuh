@@ -239,7 +239,10 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
 
   const uint32_t k0 = P.rng.k0, k1 = P.rng.k1;
   const bool hard_kill = !(P.flags & NMC_FLAG_NO_HARD_KILL);
-  const bool back = ADJ && P.adj_pass == 1;  // backward replay: no tallies
+  const bool back = ADJ && P.adj_pass == 1;   // accumulating replay
+  const bool score = ADJ && P.adj_pass == 2;  // score replay: D[photon] = its total score
+  const bool replay = back || score;          // replays write no tallies
+  const float* __restrict__ GF = ADJ ? P.adj_GF : nullptr;
   const int NyNx = P.Ny * P.Nx;
 
   RNG rng;
@@ -266,7 +269,8 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
         // the rounding of the two summation orders
         if (!(fabsf(D) <= 1e-4f * Dabs)) atomicOr(&P.sums->flags, (unsigned int)NMC_DEVFLAG_REPLAY);
       }
-      if ((st & kHave) && !back) {  // retire the finished photon
+      if (score && (st & kHave)) P.adj_Dw[pidx] = D;
+      if ((st & kHave) && !replay) {  // retire the finished photon
         dep.flush(P.F3D);
         if (Rd_loc > 0.f) atomicAdd(P.rd_slots + slot, to_fix(Rd_loc));  // :753
         atomicAdd(&s_tot[0], 1ull);
@@ -292,7 +296,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
       }
       pidx = next_photon(&P.sums->work);
       if (pidx >= P.n) break;
-      if (back) {  // only photons with a detected score contribute
+      if (back) {  // only photons with a score contribute
         D = P.adj_D[pidx];
         Dabs = 0.f;
         if (D == 0.f) {
@@ -300,6 +304,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
           continue;
         }
       }
+      if (score) D = 0.f;
       const unsigned long long pid = P.first + pidx;
       slot = (unsigned int)(pid % P.nslots);
       float x, y, z;
@@ -365,13 +370,25 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
     float s_mus = s;  // adjoint: the hop length whose probability depends on mus
     const float D_in = D;
     const bool fixed_before = (st & kFixed) != 0;
+    float e_dep = 0.f;  // adjoint: score of this sub-step's deposit
     {
       const float absorb = M::absorbed(W, c.x * s);
       W -= absorb;
       Atot += absorb;
-      if (back) {
-        adj.at(P, i);
-        adj.L = fmaf(D, s, adj.L);
+      if (replay) {
+        const float gf = (GF && (st & kBflag)) ? __ldg(GF + i) : 0.f;
+        e_dep = gf * absorb;
+        if (score) {
+          D += e_dep;
+        } else {
+          adj.at(P, i);
+          // later scores carry exp(-mua s); this deposit's own derivative is
+          // d[W (1 - exp(-mua s))]/dmua = s * W_after
+          adj.L = fmaf(D - e_dep, s, adj.L);
+          if (gf != 0.f) adj.L = fmaf(-gf * s, W, adj.L);
+          D -= e_dep;
+          Dabs += fabsf(e_dep);
+        }
       } else if (st & kBflag) {
         dep.add(P.F3D, i, absorb);
       }
@@ -415,10 +432,14 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
             if (det) {
               const float dw = W * (1.f - rsp);
               const unsigned int rbin = (unsigned int)min((int)(ro * P.rd_idr), P.rd_bins);
-              if (back) {
+              if (replay) {
                 const float e = P.adj_G[rbin] * dw;  // this event's score is now behind the photon
-                D -= e;
-                Dabs += fabsf(e);
+                if (score) {
+                  D += e;
+                } else {
+                  D -= e;
+                  Dabs += fabsf(e);
+                }
               } else {
                 const int jx = min(max(lookup_index(kx, fx, P.hx, P.ox, P.hdx), 0), P.Nx - 1);
                 const int jy = min(max(lookup_index(ky, fy, P.hy, P.oy, P.hdy), 0), P.Ny - 1);
@@ -537,7 +558,9 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
       costheta = hg_from_g<FAST>(cv.w, d.a);
       if (back) {
         adj.at(P, i);
-        if (!(st & kFixed)) adj.M = fmaf(D, cv.z, adj.M);  // D / mus: density of the scattering point
+        // D / mus: density of the scattering point, which also places this
+        // hop's last deposit
+        if (!(st & kFixed)) adj.M = fmaf(D + e_dep, cv.z, adj.M);
         if (!flt_eq(cv.w, 1.f)) adj.Q = fmaf(D, dlnhg_dg(cv.w, costheta), adj.Q);
         st &= ~kFixed;
       }

@@ -230,9 +230,10 @@ EventPair get_pair(nmc_handle* h) {
 
 // Device buffers of one adjoint pass.
 struct AdjArgs {
-  int pass;  // 0 record, 1 backward
-  const float* D;
+  int pass;  // 0 record, 1 accumulating replay, 2 score replay
+  float* D;
   const float* G;
+  const float* GF;
   double* gL;
   double* gM;
   double* gQ;
@@ -277,7 +278,9 @@ nmc_status launch(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_record* 
       p.ev_count = h->d_evcount;
       p.ev_cap = (unsigned int)std::min(h->ev_cap, h->ev_limit);
       p.adj_D = adj->D;
+      p.adj_Dw = adj->D;
       p.adj_G = adj->G;
+      p.adj_GF = adj->GF;
       p.gL = adj->gL;
       p.gM = adj->gM;
       p.gQ = adj->gQ;
@@ -848,7 +851,7 @@ nmc_status nmc_adjoint_forward(nmc_handle* h, uint64_t first, uint64_t n, uint64
   h->ev_limit = event_capacity;
   if (!h->d_evcount) NMC_CUDA(h, cudaMalloc((void**)&h->d_evcount, sizeof(unsigned long long)));
   NMC_CUDA(h, cudaMemsetAsync(h->d_evcount, 0, sizeof(unsigned long long), h->stream));
-  AdjArgs a{0, nullptr, nullptr, nullptr, nullptr, nullptr};
+  AdjArgs a{0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   st = launch(h, first, n, nullptr, nullptr, 0, &a);
   if (st == NMC_OK) st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
@@ -867,34 +870,46 @@ nmc_status nmc_adjoint_forward(nmc_handle* h, uint64_t first, uint64_t n, uint64
   return st;
 }
 
-nmc_status nmc_adjoint_backward(nmc_handle* h, const float* grad_rd_r, double* grad_mua, double* grad_mus,
-                                double* grad_g) {
-  if (!h || !grad_rd_r) return fail(h, NMC_EINVAL, "null argument");
+nmc_status nmc_adjoint_backward_ex(nmc_handle* h, const float* grad_rd_r, const float* grad_absorbed,
+                                   double* grad_mua, double* grad_mus, double* grad_g) {
+  if (!h || (!grad_rd_r && !grad_absorbed)) return fail(h, NMC_EINVAL, "null argument");
   if (!h->adj_ready) return fail(h, NMC_ESTATE, "nmc_adjoint_forward has not completed");
   nmc_status st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
   unsigned long long cnt = 0;
   NMC_CUDA(h, cudaMemcpy(&cnt, h->d_evcount, sizeof cnt, cudaMemcpyDeviceToHost));
   const size_t nb = (size_t)h->rd_bins + 1, nv = h->nvox;
-  char* base = nullptr;
-  const size_t bD = h->adj_n * 4, bG = nb * 4, bg = nv * 8;
+  const size_t bD = h->adj_n * 4, bG = nb * 4, bF = grad_absorbed ? nv * 4 : 0, bg = nv * 8;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  NMC_CUDA(h, cudaMalloc((void**)&base, al(bD) + al(bG) + 3 * al(bg)));
+  char* base = nullptr;
+  NMC_CUDA(h, cudaMalloc((void**)&base, al(bD) + al(bG) + al(bF) + 3 * al(bg)));
   float* D = (float*)base;
   float* G = (float*)(base + al(bD));
-  double* gL = (double*)(base + al(bD) + al(bG));
+  float* GF = grad_absorbed ? (float*)(base + al(bD) + al(bG)) : nullptr;
+  double* gL = (double*)(base + al(bD) + al(bG) + al(bF));
   double* gM = (double*)((char*)gL + al(bg));
   double* gQ = (double*)((char*)gM + al(bg));
   auto done = [&](nmc_status s) {
     cudaFree(base);
     return s;
   };
-  if (cudaMemsetAsync(D, 0, bD, h->stream) != cudaSuccess ||
-      cudaMemcpyAsync(G, grad_rd_r, bG, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
-      cudaMemsetAsync(gL, 0, 3 * al(bg), h->stream) != cudaSuccess ||
-      nmc::launch_adjoint_scores(h->d_ev, (unsigned int)cnt, G, D, h->stream) != cudaSuccess)
-    return done(fail(h, NMC_EDEVICE, "adjoint set-up"));
-  AdjArgs a{1, D, G, gL, gM, gQ};
+  bool ok = cudaMemsetAsync(gL, 0, 3 * al(bg), h->stream) == cudaSuccess;
+  ok = ok && (grad_rd_r ? cudaMemcpyAsync(G, grad_rd_r, bG, cudaMemcpyHostToDevice, h->stream)
+                        : cudaMemsetAsync(G, 0, bG, h->stream)) == cudaSuccess;
+  if (GF) ok = ok && cudaMemcpyAsync(GF, grad_absorbed, bF, cudaMemcpyHostToDevice, h->stream) == cudaSuccess;
+  if (!ok) return done(fail(h, NMC_EDEVICE, "adjoint set-up"));
+  if (GF) {
+    // deposits score too: a first replay gives every photon its total score
+    AdjArgs a{2, D, G, GF, nullptr, nullptr, nullptr};
+    st = launch(h, h->adj_first, h->adj_n, nullptr, nullptr, 0, &a);
+    if (st != NMC_OK) return done(st);
+  } else {
+    // detection scores only: from the events the record pass kept
+    if (cudaMemsetAsync(D, 0, bD, h->stream) != cudaSuccess ||
+        nmc::launch_adjoint_scores(h->d_ev, (unsigned int)cnt, G, D, h->stream) != cudaSuccess)
+      return done(fail(h, NMC_EDEVICE, "adjoint scores"));
+  }
+  AdjArgs a{1, D, G, GF, gL, gM, gQ};
   st = launch(h, h->adj_first, h->adj_n, nullptr, nullptr, 0, &a);
   if (st == NMC_OK) st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return done(st);
@@ -909,6 +924,12 @@ nmc_status nmc_adjoint_backward(nmc_handle* h, const float* grad_rd_r, double* g
     if (grad_g) grad_g[k] = Q[k];
   }
   return done(st);
+}
+
+nmc_status nmc_adjoint_backward(nmc_handle* h, const float* grad_rd_r, double* grad_mua, double* grad_mus,
+                                double* grad_g) {
+  if (!h || !grad_rd_r) return fail(h, NMC_EINVAL, "null argument");
+  return nmc_adjoint_backward_ex(h, grad_rd_r, nullptr, grad_mua, grad_mus, grad_g);
 }
 
 void* nmc_stream(nmc_handle* h) { return h ? (void*)h->stream : nullptr; }

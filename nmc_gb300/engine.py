@@ -70,11 +70,12 @@ def lib() -> C.CDLL:
         L.nmc_set_radial_tally.argtypes = [H, C.c_int32, C.c_float]
         L.nmc_adjoint_forward.argtypes = [H, C.c_uint64, C.c_uint64, C.c_uint64]
         L.nmc_adjoint_backward.argtypes = [H, _P, _P, _P, _P]
+        L.nmc_adjoint_backward_ex.argtypes = [H, _P, _P, _P, _P, _P]
         for name in ("nmc_create", "nmc_prepare", "nmc_set_ext", "nmc_set_num_runs_seed",
                      "nmc_send_compute_command", "nmc_run", "nmc_run_async", "nmc_synchronize",
                      "nmc_run_traced", "nmc_get_compute_results", "nmc_get_summary",
                      "nmc_get_tally_f64", "nmc_reset", "nmc_set_voxel_props", "nmc_set_radial_tally",
-                     "nmc_adjoint_forward", "nmc_adjoint_backward"):
+                     "nmc_adjoint_forward", "nmc_adjoint_backward", "nmc_adjoint_backward_ex"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -229,17 +230,24 @@ class Engine:
         cap = int(event_capacity) if event_capacity else max(1 << 20, 4 * int(n))
         self._check(self._L.nmc_adjoint_forward(self._h, int(first), int(n), cap), "nmc_adjoint_forward")
 
-    def adjoint_backward(self, grad_rd_r):
-        """(grad_mua, grad_mus, grad_g) per voxel for the upstream gradient of
-        the un-normalised radial tally (bins + 1 values)."""
-        G = np.ascontiguousarray(grad_rd_r, dtype=np.float32).ravel()
-        nb = self._L.nmc_tally_size(self._h, abi.TALLY_RD_R)
-        if G.size != nb:
-            raise ValueError(f"grad_rd_r needs {nb} values")
+    def adjoint_backward(self, grad_rd_r=None, grad_absorbed=None):
+        """(grad_mua, grad_mus, grad_g) per voxel for the upstream gradients of
+        the un-normalised radial tally (bins + 1 values) and of the absorbed
+        weight per voxel (NMC_TALLY_F3D); either may be None, not both."""
         n = self.rp.Nx * self.rp.Ny * self.rp.Nz
+        G = GF = None
+        if grad_rd_r is not None:
+            G = np.ascontiguousarray(grad_rd_r, dtype=np.float32).ravel()
+            nb = self._L.nmc_tally_size(self._h, abi.TALLY_RD_R)
+            if G.size != nb:
+                raise ValueError(f"grad_rd_r needs {nb} values")
+        if grad_absorbed is not None:
+            GF = np.ascontiguousarray(grad_absorbed, dtype=np.float32).ravel()
+            if GF.size != n:
+                raise ValueError(f"grad_absorbed needs {n} values")
         ga, gs, gg = (np.zeros(n, np.float64) for _ in range(3))
-        self._check(self._L.nmc_adjoint_backward(self._h, _ptr(G), _ptr(ga), _ptr(gs), _ptr(gg)),
-                    "nmc_adjoint_backward")
+        self._check(self._L.nmc_adjoint_backward_ex(self._h, _ptr(G), _ptr(GF), _ptr(ga), _ptr(gs), _ptr(gg)),
+                    "nmc_adjoint_backward_ex")
         return ga, gs, gg
 
     @property

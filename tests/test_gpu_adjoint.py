@@ -6,7 +6,9 @@ around the beam entry of a 64^3 heterogeneous medium, batch by batch, so that
 each comparison carries its own standard error.  mua is pathwise (the
 trajectories do not depend on it) and must agree to 1e-3 relative; mus and g
 are likelihood-ratio estimates and must agree within 4.5 standard errors of
-the batch means, voxel by voxel and summed.
+the batch means, voxel by voxel and summed.  Two losses: one on Rd(r) alone
+(the detected photons are replayed once) and one on Rd(r) plus the absorbed
+weight of a block of voxels (every photon is replayed twice).
 """
 import time
 
@@ -41,18 +43,27 @@ def _upstream(bins):
     return G
 
 
-def test_adjoint_matches_crn_finite_differences(gpu, case):
+def _crn_check(gpu, case, voxels, G, GF, B, nb):
+    """pMC gradients of G . Rd(r) + GF . absorbed against CRN central
+    differences, per batch of nb photons (B batches)."""
     rp, tp, v, ext, mua, mus, g, bins, dr = case
     N = rp.Nx
-    flat = np.array([iz * N * N + ix * N + iy for iz, ix, iy in VOXELS])
-    G = _upstream(bins)
-    B, nb = 16, 500_000
+    flat = np.array([iz * N * N + ix * N + iy for iz, ix, iy in voxels])
+    G64 = G.astype(np.float64)
+    GF64 = None if GF is None else GF.astype(np.float64)
+
+    def loss(e):
+        out = float(G64 @ e.tally(abi.TALLY_RD_R))
+        if GF64 is not None:
+            out += float(GF64 @ e.tally(abi.TALLY_F3D))
+        return out
+
     with _engine(gpu, case) as e:
         pm = {k: np.zeros((B, len(flat))) for k in "asg"}
         for b in range(B):
             e.reset()
             e.adjoint_forward(b * nb, nb)
-            ga, gs, gg = e.adjoint_backward(G)
+            ga, gs, gg = e.adjoint_backward(G, GF)
             pm["a"][b], pm["s"][b], pm["g"][b] = ga[flat], gs[flat], gg[flat]
         fd = {k: np.zeros((B, len(flat))) for k in "asg"}
         for k, arr, step in (("a", mua, lambda x: 0.02 * x), ("s", mus, lambda x: 0.02 * x),
@@ -70,7 +81,7 @@ def test_adjoint_matches_crn_finite_differences(gpu, case):
                     for b in range(B):
                         e.reset()
                         e.run(b * nb, nb)
-                        sc.append(float(G.astype(np.float64) @ e.tally(abi.TALLY_RD_R)))
+                        sc.append(loss(e))
                     sides.append(np.array(sc))
                 fd[k][:, j] = (sides[0] - sides[1]) / (2.0 * h)
     for k in "asg":
@@ -88,7 +99,20 @@ def test_adjoint_matches_crn_finite_differences(gpu, case):
         else:
             assert np.all(np.abs(t) <= 4.5), (k, t)
             assert abs(t_tot) <= 4.5
-            assert np.corrcoef(P, F)[0, 1] >= 0.98
+            assert np.corrcoef(P, F)[0, 1] >= 0.97
+
+
+def test_adjoint_rd_matches_crn_finite_differences(gpu, case):
+    _crn_check(gpu, case, VOXELS, _upstream(case[7]), None, B=16, nb=500_000)
+
+
+def test_adjoint_rd_and_fluence_match_crn_finite_differences(gpu, case):
+    # loss on Rd(r) and on the absorbed weight of a block under the beam
+    N = case[0].Nx
+    GF = np.zeros((N, N, N), np.float32)
+    GF[2:8, 28:36, 28:36] = 1.0
+    voxels = [(iz, ix, iy) for iz in range(0, 8, 2) for ix in (30, 31, 32, 33) for iy in (31, 32)]
+    _crn_check(gpu, case, voxels, _upstream(case[7]), GF.ravel(), B=16, nb=250_000)
 
 
 def test_adjoint_is_linear_in_the_upstream_gradient(gpu, case):
@@ -157,29 +181,40 @@ def test_voxel_media_match_the_tissue_map(gpu):
 
 def test_autograd_function(gpu, case):
     torch = pytest.importorskip("torch")
-    from nmc_gb300.autograd import radial_reflectance
+    from nmc_gb300.autograd import fluence, radial_reflectance, transport
 
     rp, tp, v, ext, mua, mus, g, bins, dr = case
+    N = rp.Nx
     n = 200_000
     w = torch.linspace(1.0, 0.0, bins + 1, dtype=torch.float64)
+    wf = torch.zeros((N, N, N), dtype=torch.float64)
+    wf[1:6, 30:34, 30:34] = 1.0
     with _engine(gpu, case) as e:
         ta = torch.tensor(mua, dtype=torch.float64, requires_grad=True)
         ts = torch.tensor(mus, dtype=torch.float64, requires_grad=True)
         tg = torch.tensor(g, dtype=torch.float64, requires_grad=True)
-        rd = radial_reflectance(ta, ts, tg, e, 0, n)
-        assert rd.shape == (bins + 1,)
+        rd, ab = transport(ta, ts, tg, e, 0, n)
+        assert rd.shape == (bins + 1,) and ab.shape == (N, N, N)
         # another forward on the same handle before backward: the first is
         # recorded again
         radial_reflectance(ta * 1.1, ts, tg, e, 0, n)
-        (rd * w).sum().backward()
+        ((rd * w).sum() + (ab * wf).sum()).backward()
         e.set_voxel_props(mua, mus, g)
         e.reset()
         e.adjoint_forward(0, n)
-        ga, gs, gg = e.adjoint_backward((w.numpy() / n).astype(np.float32))
         rd_direct = e.tally(abi.TALLY_RD_R) / n
+        ab_direct = e.tally(abi.TALLY_F3D) / n
+        ga, gs, gg = e.adjoint_backward((w.numpy() / n).astype(np.float32),
+                                        (wf.numpy().ravel() / n).astype(np.float32))
     np.testing.assert_allclose(rd.detach().numpy(), rd_direct, rtol=1e-6)
+    np.testing.assert_allclose(ab.detach().numpy().ravel(), ab_direct, rtol=1e-6)
     for t, ref in ((ta, ga), (ts, gs), (tg, gg)):
         np.testing.assert_allclose(t.grad.numpy().ravel(), ref, rtol=1e-5, atol=1e-9 * np.abs(ref).max())
+    # the fluence normalisation differentiates through torch
+    ta2 = torch.tensor(mua, dtype=torch.float64, requires_grad=True)
+    phi = fluence(ab.detach(), ta2, 0.01 ** 3)
+    phi.sum().backward()
+    assert torch.all(ta2.grad <= 0)
 
 
 def test_adjoint_costs_at_most_three_forwards(gpu, case):
@@ -196,5 +231,12 @@ def test_adjoint_costs_at_most_three_forwards(gpu, case):
         e.adjoint_forward(0, n)
         e.adjoint_backward(G)
         t_adj = time.perf_counter() - t0
-    print(f"forward {t_fwd * 1e3:.1f} ms, record + backward {t_adj * 1e3:.1f} ms, ratio {t_adj / t_fwd:.2f}")
+        GF = np.ones(case[0].Nx ** 3, np.float32)
+        t0 = time.perf_counter()
+        e.adjoint_forward(0, n)
+        e.adjoint_backward(G, GF)
+        t_adj_f = time.perf_counter() - t0
+    print(f"forward {t_fwd * 1e3:.1f} ms; record + backward: Rd {t_adj * 1e3:.1f} ms ({t_adj / t_fwd:.2f}x), "
+          f"Rd + absorbed {t_adj_f * 1e3:.1f} ms ({t_adj_f / t_fwd:.2f}x)")
     assert t_adj <= 3.0 * t_fwd
+    assert t_adj_f <= 4.0 * t_fwd  # every photon replayed twice
