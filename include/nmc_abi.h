@@ -247,6 +247,12 @@ nmc_status nmc_create(int32_t sim_type, int32_t device, nmc_handle** out);
 nmc_status nmc_prepare(nmc_handle* h, const nmc_run_params* rp,
                        const nmc_tissue_params* tp, const uint8_t* v);
 
+/* Swaps the tissue table of a prepared handle (e.g. the next wavelength)
+ * without re-sending the map; tallies are kept (nmc_reset clears them).
+ * The tissues the map uses must have finite mua >= 0, mus > 0 and phase
+ * terms, as in nmc_prepare. */
+nmc_status nmc_set_tissue_params(nmc_handle* h, const nmc_tissue_params* tp);
+
 /* Extension knobs (RNG, phase function, mcsub bins and beam, launch shape).
  * Call before nmc_prepare or between runs; defaults from nmc_ext_defaults. */
 nmc_status nmc_set_ext(nmc_handle* h, const nmc_ext* ext);
@@ -396,6 +402,21 @@ enum {
  * escaping flux J[ir] per set (un-normalised). */
 nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_sets, double* out,
                          double* J);
+
+/* Batched sweep on a voxel tissue map: set s runs photons[s] photons with
+ * its own tissue table tables[s] (all 19 entries as in nmc_prepare; the
+ * handle's map, geometry, beam and kernel kind stay) in one persistent
+ * launch on a handle made with NMC_SIM_MCXYZ or NMC_SIM_MCXYZ_TT.  Photons
+ * of set s are ids first_photon[s] .. first_photon[s] + photons[s] - 1
+ * (first_photon may be NULL: all 0) under Philox key (seed lo, seed hi + s),
+ * so set s reproduces a plain run of those ids with seed + (s << 32).
+ * Replaces one `nmc` process per wavelength on the skin-vessel map
+ * (NMC-samples/example3.ipynb cell 5).  `out` holds n_sets *
+ * NMC_SWEEP_FIELDS doubles: HOPS counts voxel sub-steps, S is 0, E the
+ * detected weight, RD = E / photons (the run's Total Rd, main.m:294-305).
+ * No map tallies (F3D, Rd2D) are kept. */
+nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables, const uint64_t* photons,
+                                 const uint64_t* first_photon, int32_t n_sets, double* out);
 
 /* Measurement support (no counterpart in the reference): FP32 FMA lanes per
  * second and MUFU (ex2) lanes per second sustained on `device`, the issue

@@ -22,6 +22,12 @@ struct AdjEvent {
 // Voxel kernels (MCXYZKernel kernels.metal:321-754 and MCXYZKernelTT
 // :757-1118).  Photon positions are kept as an integer voxel-lattice cell
 // (k = floor(x / d), unbounded) plus an FP32 offset inside the cell.
+// Per-set sums of a voxel sweep (u64 fixed point 2^-32 for weights).
+struct XyzSweepSums {
+  unsigned long long photons, substeps, scatters, A, rd;
+  double rd2;
+};
+
 struct XyzParams {
   int Nx, Ny, Nz;
   float dx, dy, dz, idx, idy, idz;
@@ -68,9 +74,16 @@ struct XyzParams {
   double* gL;                 // per voxel: sum D * charged path length (absorption)
   double* gM;                 // per voxel: d ln p(path)/dmus terms weighted by D
   double* gQ;                 // per voxel: sum D * dln p_HG / dg over scatterings
+  // batched sweep over tissue tables (one table per set, e.g. per wavelength)
+  const float4* sw_core;               // n_sets * NMC_NTISS (mua, mus, 1/mus, g)
+  const PhaseConst* sw_phase;          // n_sets * NMC_NTISS
+  const unsigned long long* sw_prefix; // n_sets + 1 budget prefix sums
+  const unsigned long long* sw_first;  // id of each set's first photon
+  XyzSweepSums* sw_sums;               // n_sets
+  int sw_nsets;
 };
 
-enum XyzMode { kTissue = 0, kVoxel = 1, kAdjoint = 2 };
+enum XyzMode { kTissue = 0, kVoxel = 1, kAdjoint = 2, kSweep = 3 };
 
 // Layered semi-infinite kernel (MCSubKernel kernels.metal:59-319).
 struct SubParams {
@@ -140,6 +153,8 @@ cudaError_t launch_mcxyz_voxel(const XyzParams& p, int mode, bool trace, int gri
                                cudaStream_t stream);
 cudaError_t mcxyz_voxel_occupancy(int mode, bool trace, int block, int* blocks_per_sm);
 // D[photon] += G[bin] * w over recorded events
+cudaError_t launch_mcxyz_sweep(const XyzParams& p, bool two_term, int grid, int block, cudaStream_t stream);
+cudaError_t mcxyz_sweep_occupancy(bool two_term, int block, int* blocks_per_sm);
 cudaError_t launch_adjoint_scores(const AdjEvent* ev, unsigned int n_ev, const float* G, float* D,
                                   cudaStream_t stream);
 

@@ -221,13 +221,14 @@ __device__ __forceinline__ float dlnhg_dg(float g, float mu) {
 template <bool TT, class RNG, bool TRACE, bool FAST, int MODE>
 __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(const XyzParams P) {
   using M = Math<FAST>;
-  constexpr bool VOX = MODE != kTissue;
+  constexpr bool SW = MODE == kSweep;  // many tissue tables, one per set
+  constexpr bool VOX = MODE == kVoxel || MODE == kAdjoint;
   constexpr bool ADJ = MODE == kAdjoint;
   __shared__ float4 s_core[NMC_NTISS];
   __shared__ PhaseConst s_ph[NMC_NTISS];
   __shared__ unsigned long long s_tot[5];  // photons, substeps, scatters, A, rd
   __shared__ double s_rd2;
-  if (!VOX) {
+  if (!VOX && !SW) {
     for (int t = threadIdx.x; t < NMC_NTISS; t += blockDim.x) {
       s_core[t] = P.core[t];
       s_ph[t] = P.phase[t];
@@ -237,7 +238,8 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
   if (threadIdx.x == 0) s_rd2 = 0.0;
   __syncthreads();
 
-  const uint32_t k0 = P.rng.k0, k1 = P.rng.k1;
+  const uint32_t k0 = P.rng.k0;
+  uint32_t k1 = P.rng.k1;  // a sweep set s draws from key (k0, k1 + s)
   const bool hard_kill = !(P.flags & NMC_FLAG_NO_HARD_KILL);
   const bool back = ADJ && P.adj_pass == 1;   // accumulating replay
   const bool score = ADJ && P.adj_pass == 2;  // score replay: D[photon] = its total score
@@ -251,6 +253,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
   float W = 0.f, sleft = 0.f, Rd_loc = 0.f, Atot = 0.f;
   float D = 0.f, Dabs = 0.f;  // adjoint: remaining detected score, sum of |event scores| replayed
   unsigned int i = 0, slot = 0, nsc = 0, nsub = 0, st = 0;
+  unsigned int set = 0, sbase = 0;  // sweep: the photon's set and its table offset
   unsigned long long pidx = 0;
   uint32_t fate = NMC_FATE_ALIVE, ndet = 0, nev = 0;  // trace only
   Deposit dep{0xFFFFFFFFu, 0.f};
@@ -270,7 +273,18 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
         if (!(fabsf(D) <= 1e-4f * Dabs)) atomicOr(&P.sums->flags, (unsigned int)NMC_DEVFLAG_REPLAY);
       }
       if (score && (st & kHave)) P.adj_Dw[pidx] = D;
-      if ((st & kHave) && !replay) {  // retire the finished photon
+      if (SW && (st & kHave)) {  // per-set sums
+        XyzSweepSums* q = P.sw_sums + set;
+        atomicAdd(&q->photons, 1ull);
+        atomicAdd(&q->substeps, (unsigned long long)nsub);
+        atomicAdd(&q->scatters, (unsigned long long)nsc);
+        atomicAdd(&q->A, to_fix(Atot));
+        if (Rd_loc > 0.f) {
+          atomicAdd(&q->rd, to_fix(Rd_loc));
+          atomicAdd(&q->rd2, (double)Rd_loc * (double)Rd_loc);
+        }
+      }
+      if ((st & kHave) && !replay && !SW) {  // retire the finished photon
         dep.flush(P.F3D);
         if (Rd_loc > 0.f) atomicAdd(P.rd_slots + slot, to_fix(Rd_loc));  // :753
         atomicAdd(&s_tot[0], 1ull);
@@ -305,7 +319,18 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
         }
       }
       if (score) D = 0.f;
-      const unsigned long long pid = P.first + pidx;
+      unsigned long long pid = P.first + pidx;
+      if (SW) {  // the set whose budget holds this photon: last s with prefix[s] <= pidx
+        unsigned int lo = 0, hi = (unsigned int)P.sw_nsets;
+        while (hi - lo > 1) {
+          const unsigned int mid = (lo + hi) >> 1;
+          if (__ldg(P.sw_prefix + mid) <= pidx) lo = mid; else hi = mid;
+        }
+        set = lo;
+        sbase = set * NMC_NTISS;
+        pid = __ldg(P.sw_first + set) + (pidx - __ldg(P.sw_prefix + set));
+        k1 = P.rng.k1 + set;
+      }
       slot = (unsigned int)(pid % P.nslots);
       float x, y, z;
       if constexpr (std::is_same<RNG, TausRng>::value) {
@@ -343,7 +368,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
     // the step to the nearest face (:534-682) share one straight path; only
     // the face landing, the voxel lookup and the tissue load are predicated
     // on the crossing, so the lanes of a warp stay together.
-    const float4 c = VOX ? __ldg(P.vox + i) : s_core[tiss];  // mua, mus, 1/mus, g
+    const float4 c = VOX ? __ldg(P.vox + i) : (SW ? __ldg(P.sw_core + sbase + tiss) : s_core[tiss]);  // mua, mus, 1/mus, g
     float s = sleft * c.z;
     ++nsub;
     ++depth;
@@ -389,7 +414,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
           D -= e_dep;
           Dabs += fabsf(e_dep);
         }
-      } else if (st & kBflag) {
+      } else if (!SW && (st & kBflag)) {
         dep.add(P.F3D, i, absorb);
       }
     }
@@ -444,10 +469,12 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
                 const int jx = min(max(lookup_index(kx, fx, P.hx, P.ox, P.hdx), 0), P.Nx - 1);
                 const int jy = min(max(lookup_index(ky, fy, P.hy, P.oy, P.hdy), 0), P.Ny - 1);
                 Rd_loc += dw;
-                const unsigned int i2d = (unsigned int)(jx * P.Ny + jy);
-                atomicAdd(P.Rd2D + i2d, to_fix(dw));
-                atomicAdd(P.Det2D + i2d, 1u);
-                if (P.rd_r) atomicAdd(P.rd_r + rbin, to_fix(dw));
+                if (!SW) {
+                  const unsigned int i2d = (unsigned int)(jx * P.Ny + jy);
+                  atomicAdd(P.Rd2D + i2d, to_fix(dw));
+                  atomicAdd(P.Det2D + i2d, 1u);
+                  if (P.rd_r) atomicAdd(P.rd_r + rbin, to_fix(dw));
+                }
                 if (ADJ) {  // record pass: keep (photon, bin, weight) for the backward pass
                   const unsigned long long k = atomicAdd(P.ev_count, 1ull);
                   if (k < P.ev_cap) P.ev[k] = AdjEvent{(unsigned int)pidx, rbin, dw, 0.f};
@@ -511,8 +538,10 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
           st &= ~kSurf;
           Rd_loc += W;
           if (TRACE) ++ndet;
-          const int jx = min(max(ix, 0), P.Nx - 1), jy = min(max(iy, 0), P.Ny - 1);
-          atomicAdd(P.Rd2D + (unsigned int)(jx * P.Ny + jy), to_fix(W));
+          if (!SW) {
+            const int jx = min(max(ix, 0), P.Nx - 1), jy = min(max(iy, 0), P.Ny - 1);
+            atomicAdd(P.Rd2D + (unsigned int)(jx * P.Ny + jy), to_fix(W));
+          }
         }
         if (kz < 0) {
           kill(NMC_FATE_BOUNDARY);
@@ -565,7 +594,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
         st &= ~kFixed;
       }
     } else {
-      const PhaseConst& ph = s_ph[tiss];
+      const PhaseConst& ph = SW ? P.sw_phase[sbase + tiss] : s_ph[tiss];
       costheta = TT ? tt_sample<FAST>(ph, d.a, d.b) : hg_sample<FAST>(ph, d.a);
     }
     spin<FAST>(costheta, TT ? d.c : d.b, ux, uy, uz);

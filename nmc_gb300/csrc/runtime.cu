@@ -37,6 +37,7 @@ struct nmc_handle {
   nmc_run_params rp{};
   nmc_tissue_params tp{};
   bool prepared = false;
+  uint32_t tiss_used = 0;  // bit t: tissue t occurs in the map
   std::string err;
   int32_t run = 1;
   cudaStream_t stream = nullptr;
@@ -147,6 +148,27 @@ nmc_status build_sub(nmc_handle* h) {
   return NMC_OK;
 }
 
+// The optical properties of every tissue in `mask` (bit t = tissue t) must be
+// usable: finite mua >= 0, finite mus > 0, finite g.  `set` >= 0 names the
+// sweep set in the message.
+nmc_status check_tissues(nmc_handle* h, const nmc_tissue_params* tp, uint32_t mask, int set) {
+  for (int t = 0; t < NMC_NTISS; ++t) {
+    if (!(mask >> t & 1u)) continue;
+    if (!finite_nonneg(tp->muav[t]) || !(tp->musv[t] > 0.f) || !std::isfinite(tp->musv[t]) ||
+        !std::isfinite(tp->gv[t]) || !std::isfinite(tp->gf[t]) || !std::isfinite(tp->af[t]) ||
+        !std::isfinite(tp->gb[t]) || !std::isfinite(tp->ab[t]) || !std::isfinite(tp->CC[t])) {
+      char msg[128];
+      if (set >= 0)
+        std::snprintf(msg, sizeof msg, "sweep set %d, tissue %d needs finite mua >= 0, mus > 0 and phase terms",
+                      set, t);
+      else
+        std::snprintf(msg, sizeof msg, "tissue %d needs finite mua >= 0, mus > 0 and phase terms", t);
+      return fail(h, NMC_EINVAL, msg);
+    }
+  }
+  return NMC_OK;
+}
+
 nmc_status validate(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue_params* tp,
                     const uint8_t* v) {
   const nmc_ext& e = h->ext;
@@ -181,16 +203,12 @@ nmc_status validate(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue_pa
     }
     used[v[k]] = true;
   }
-  for (int t = 0; t < NMC_NTISS; ++t) {
-    if (!used[t]) continue;
-    if (!finite_nonneg(tp->muav[t]) || !(tp->musv[t] > 0.f) || !std::isfinite(tp->musv[t]) ||
-        !std::isfinite(tp->gv[t])) {
-      char msg[96];
-      std::snprintf(msg, sizeof msg, "tissue %d needs finite mua >= 0, mus > 0 and g", t);
-      return fail(h, NMC_EINVAL, msg);
-    }
-  }
-  return NMC_OK;
+  uint32_t mask = 0;
+  for (int t = 0; t < NMC_NTISS; ++t)
+    if (used[t]) mask |= 1u << t;
+  nmc_status st = check_tissues(h, tp, mask, -1);
+  if (st == NMC_OK) h->tiss_used = mask;
+  return st;
 }
 
 nmc_status wait_event(nmc_handle* h, cudaEvent_t ev) {
@@ -476,6 +494,23 @@ nmc_status nmc_prepare(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue
   h->prepared = true;
   st = nmc_reset(h);
   if (st != NMC_OK) return st;
+  return h->sim == NMC_SIM_MCSUB ? build_sub(h) : build_xyz(h);
+}
+
+nmc_status nmc_set_tissue_params(nmc_handle* h, const nmc_tissue_params* tp) {
+  if (!h || !tp) return fail(h, NMC_EINVAL, "null argument");
+  if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
+  nmc_status st;
+  if (h->sim == NMC_SIM_MCSUB) {
+    const float mua = tp->muav[1], mus = tp->musv[1];
+    if (!finite_nonneg(mua) || !finite_nonneg(mus) || !(mua + mus > 0.f))
+      return fail(h, NMC_EINVAL, "tissue 1 needs finite mua, mus >= 0 with mua + mus > 0");
+  } else if ((st = check_tissues(h, tp, h->tiss_used, -1)) != NMC_OK) {
+    return st;
+  }
+  st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  h->tp = *tp;
   return h->sim == NMC_SIM_MCSUB ? build_sub(h) : build_xyz(h);
 }
 
@@ -790,6 +825,102 @@ nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_set
     const double me = n > 0 ? o[NMC_SWEEP_E] / n : 0.0;
     o[NMC_SWEEP_RD] = n > 0 ? (o[NMC_SWEEP_S] + o[NMC_SWEEP_E]) / n : 0.0;
     o[NMC_SWEEP_RD_SE] = n > 1 ? std::sqrt(std::max(0.0, e2[s] / n - me * me) / n) : 0.0;
+  }
+  return cleanup(st);
+}
+
+nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables, const uint64_t* photons,
+                                 const uint64_t* first_photon, int32_t n_sets, double* out) {
+  if (!h || !tables || !photons || !out) return fail(h, NMC_EINVAL, "null argument");
+  if (h->sim != NMC_SIM_MCXYZ && h->sim != NMC_SIM_MCXYZ_TT)
+    return fail(h, NMC_EINVAL, "tissue sweeps run on an NMC_SIM_MCXYZ or NMC_SIM_MCXYZ_TT handle");
+  if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
+  if (n_sets < 1 || n_sets > 65536) return fail(h, NMC_EINVAL, "n_sets must be in [1, 65536]");
+  if (h->ext.rng != NMC_RNG_PHILOX) return fail(h, NMC_EINVAL, "sweeps use the Philox streams");
+  if (h->voxel_mode) return fail(h, NMC_ESTATE, "tissue sweeps read the tissue map, not per-voxel properties");
+  nmc_status st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  const size_t nt = (size_t)n_sets * NMC_NTISS;
+  std::vector<float4> core(nt);
+  std::vector<nmc::PhaseConst> phase(nt);
+  std::vector<unsigned long long> prefix(n_sets + 1, 0ull), first(n_sets, 0ull);
+  for (int s = 0; s < n_sets; ++s) {
+    if ((st = check_tissues(h, &tables[s], h->tiss_used, s)) != NMC_OK) return st;
+    nmc::XyzParams tmp{};
+    nmc::fill_xyz(tmp, h->rp, tables[s], h->ext, h->sim);
+    for (int t = 0; t < NMC_NTISS; ++t) {
+      core[(size_t)s * NMC_NTISS + t] = tmp.core[t];
+      phase[(size_t)s * NMC_NTISS + t] = tmp.phase[t];
+    }
+    if (first_photon) first[s] = first_photon[s];
+    prefix[s + 1] = prefix[s] + photons[s];
+  }
+  nmc::XyzParams p = h->xp;
+  const size_t b_core = sizeof(float4) * nt, b_ph = sizeof(nmc::PhaseConst) * nt, b_pre = 8 * (n_sets + 1),
+               b_first = 8 * (size_t)n_sets, b_sums = sizeof(nmc::XyzSweepSums) * n_sets;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  char* base = nullptr;
+  NMC_CUDA(h, cudaMalloc((void**)&base, al(b_core) + al(b_ph) + al(b_pre) + al(b_first) + al(b_sums)));
+  char* cur = base;
+  auto take = [&](size_t b) {
+    char* r = cur;
+    cur += al(b);
+    return r;
+  };
+  p.sw_core = (const float4*)take(b_core);
+  p.sw_phase = (const nmc::PhaseConst*)take(b_ph);
+  p.sw_prefix = (const unsigned long long*)take(b_pre);
+  p.sw_first = (const unsigned long long*)take(b_first);
+  p.sw_sums = (nmc::XyzSweepSums*)take(b_sums);
+  p.sw_nsets = n_sets;
+  p.first = 0;
+  p.n = prefix[n_sets];
+  p.trace = nmc::TraceParams{nullptr, nullptr, 0u};
+  auto cleanup = [&](nmc_status s) {
+    cudaFree(base);
+    return s;
+  };
+  if (cudaMemcpyAsync((void*)p.sw_core, core.data(), b_core, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync((void*)p.sw_phase, phase.data(), b_ph, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync((void*)p.sw_prefix, prefix.data(), b_pre, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync((void*)p.sw_first, first.data(), b_first, cudaMemcpyHostToDevice, h->stream) !=
+          cudaSuccess ||
+      cudaMemsetAsync(p.sw_sums, 0, b_sums, h->stream) != cudaSuccess ||
+      cudaMemsetAsync(&h->d_sums->work, 0, sizeof(unsigned long long), h->stream) != cudaSuccess)
+    return cleanup(fail(h, NMC_EDEVICE, "sweep buffer set-up"));
+  const bool tt = h->sim == NMC_SIM_MCXYZ_TT;
+  const int block = h->ext.block_size > 0 ? h->ext.block_size : 256;
+  int per_sm = 0;
+  if (nmc::mcxyz_sweep_occupancy(tt, block, &per_sm) != cudaSuccess || per_sm < 1)
+    return cleanup(fail(h, NMC_EDEVICE, "sweep kernel does not fit on an SM"));
+  if (h->ext.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)h->ext.blocks_per_sm);
+  uint64_t grid = (uint64_t)h->nsm * per_sm;
+  grid = std::max<uint64_t>(1, std::min<uint64_t>(grid, (p.n + block - 1) / block));
+  EventPair ev = get_pair(h);
+  cudaEventRecord(ev.a, h->stream);
+  if (p.n > 0 && nmc::launch_mcxyz_sweep(p, tt, (int)grid, block, h->stream) != cudaSuccess)
+    return cleanup(fail(h, NMC_EDEVICE, "sweep launch"));
+  cudaEventRecord(ev.b, h->stream);
+  h->pending.push_back(ev);
+  ++h->launches;
+  st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return cleanup(st);
+  std::vector<nmc::XyzSweepSums> sums(n_sets);
+  if (cudaMemcpy(sums.data(), p.sw_sums, b_sums, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return cleanup(fail(h, NMC_EDEVICE, "sweep results"));
+  for (int s = 0; s < n_sets; ++s) {
+    double* o = out + (size_t)s * NMC_SWEEP_FIELDS;
+    const nmc::XyzSweepSums& u = sums[s];
+    const double n = (double)u.photons;
+    o[NMC_SWEEP_PHOTONS] = n;
+    o[NMC_SWEEP_HOPS] = (double)u.substeps;
+    o[NMC_SWEEP_S] = 0.0;
+    o[NMC_SWEEP_A] = (double)u.A * nmc::kUnfix;
+    o[NMC_SWEEP_E] = (double)u.rd * nmc::kUnfix;
+    o[NMC_SWEEP_E2] = u.rd2;
+    const double me = n > 0 ? o[NMC_SWEEP_E] / n : 0.0;
+    o[NMC_SWEEP_RD] = me;
+    o[NMC_SWEEP_RD_SE] = n > 1 ? std::sqrt(std::max(0.0, u.rd2 / n - me * me) / n) : 0.0;
   }
   return cleanup(st);
 }

@@ -46,6 +46,7 @@ def lib() -> C.CDLL:
         L.nmc_create.argtypes = [C.c_int32, C.c_int32, C.POINTER(H)]
         L.nmc_prepare.argtypes = [H, C.POINTER(abi.RunParams), C.POINTER(abi.TissueParams), _P]
         L.nmc_set_ext.argtypes = [H, C.POINTER(abi.Ext)]
+        L.nmc_set_tissue_params.argtypes = [H, C.POINTER(abi.TissueParams)]
         L.nmc_set_num_runs_seed.argtypes = [H, C.c_int32, C.c_float]
         L.nmc_send_compute_command.argtypes = [H]
         L.nmc_run.argtypes = [H, C.c_uint64, C.c_uint64]
@@ -66,12 +67,14 @@ def lib() -> C.CDLL:
         L.nmc_probe_issue_peaks.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.nmc_run_sweep.argtypes = [H, C.POINTER(abi.SweepSet), C.c_int32, _P, _P]
         L.nmc_run_sweep.restype = C.c_int
+        L.nmc_run_sweep_tissues.argtypes = [H, C.POINTER(abi.TissueParams), _P, _P, C.c_int32, _P]
+        L.nmc_run_sweep_tissues.restype = C.c_int
         L.nmc_set_voxel_props.argtypes = [H, _P, _P, _P]
         L.nmc_set_radial_tally.argtypes = [H, C.c_int32, C.c_float]
         L.nmc_adjoint_forward.argtypes = [H, C.c_uint64, C.c_uint64, C.c_uint64]
         L.nmc_adjoint_backward.argtypes = [H, _P, _P, _P, _P]
         L.nmc_adjoint_backward_ex.argtypes = [H, _P, _P, _P, _P, _P]
-        for name in ("nmc_create", "nmc_prepare", "nmc_set_ext", "nmc_set_num_runs_seed",
+        for name in ("nmc_create", "nmc_prepare", "nmc_set_ext", "nmc_set_tissue_params", "nmc_set_num_runs_seed",
                      "nmc_send_compute_command", "nmc_run", "nmc_run_async", "nmc_synchronize",
                      "nmc_run_traced", "nmc_get_compute_results", "nmc_get_summary",
                      "nmc_get_tally_f64", "nmc_reset", "nmc_set_voxel_props", "nmc_set_radial_tally",
@@ -140,6 +143,10 @@ class Engine:
         self.rp = rp
         vv = None if v is None else np.ascontiguousarray(v, dtype=np.uint8).ravel()
         self._check(self._L.nmc_prepare(self._h, C.byref(rp), C.byref(tp), _ptr(vv)), "nmc_prepare")
+
+    def set_tissue_params(self, tp: abi.TissueParams):
+        """Swap the tissue table (e.g. the next wavelength) keeping the map."""
+        self._check(self._L.nmc_set_tissue_params(self._h, C.byref(tp)), "nmc_set_tissue_params")
 
     def set_num_runs_seed(self, run: int, time_seed: float = 0.0):
         self._check(self._L.nmc_set_num_runs_seed(self._h, int(run), float(time_seed)), "nmc_set_num_runs_seed")
@@ -210,6 +217,21 @@ class Engine:
         if with_J:
             res["J"] = J
         return res
+
+    def run_sweep_tissues(self, tables, photons, first_photon=None) -> dict:
+        """Batched sweep on a voxel tissue map (mcxyz handle): set s runs
+        photons[s] photons with tissue table tables[s] (abi.TissueParams).
+        Returns per-set arrays named as abi.SWEEP_FIELDS."""
+        n = len(tables)
+        arr = (abi.TissueParams * n)(*tables)
+        ph = np.ascontiguousarray(photons, dtype=np.uint64)
+        fp = None if first_photon is None else np.ascontiguousarray(first_photon, dtype=np.uint64)
+        if ph.size != n or (fp is not None and fp.size != n):
+            raise ValueError("one photon budget (and first photon) per table")
+        out = np.zeros((n, len(abi.SWEEP_FIELDS)), np.float64)
+        self._check(self._L.nmc_run_sweep_tissues(self._h, arr, _ptr(ph), _ptr(fp), n, _ptr(out)),
+                    "nmc_run_sweep_tissues")
+        return {k: out[:, i] for i, k in enumerate(abi.SWEEP_FIELDS)}
 
     # -- per-voxel media and the perturbation Monte Carlo adjoint
     def set_voxel_props(self, mua, mus, g=None):

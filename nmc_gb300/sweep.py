@@ -1,9 +1,11 @@
-"""Batched parameter sweeps on the mcsub geometry (one persistent launch for
-many wavelengths or tissue sets), with an optional target standard error.
+"""Batched parameter sweeps (one persistent launch for many wavelengths or
+tissue sets), with an optional target standard error.
 
-The reference sweeps wavelengths by rewriting its input files and running
-one `nmc` process per wavelength (NMC-samples/example3.ipynb cell 5); here a
-whole sweep is one call.
+Two geometries: the mcsub semi-infinite medium (sets are abi.SweepSet) and a
+voxel tissue map (sets are TissueSet: one 19-entry tissue table per set on
+the handle's map).  The reference sweeps wavelengths by rewriting its input
+files and running one `nmc` process per wavelength on the skin-vessel map
+(NMC-samples/example3.ipynb cell 5); here a whole sweep is one call.
 """
 from __future__ import annotations
 
@@ -15,11 +17,27 @@ import numpy as np
 from . import abi
 
 
-def _copy(s: abi.SweepSet, **kw) -> abi.SweepSet:
+class TissueSet:
+    """One set of a voxel sweep: a tissue table and its photon budget."""
+
+    def __init__(self, tp: abi.TissueParams, photons: int, first_photon: int = 0):
+        self.tp = tp
+        self.photons = int(photons)
+        self.first_photon = int(first_photon)
+
+
+def _copy(s, **kw):
     c = copy.copy(s)
     for k, v in kw.items():
         setattr(c, k, v)
     return c
+
+
+def _run(engine, sets) -> dict:
+    if engine.sim_type == abi.SIM_MCSUB:
+        return engine.run_sweep(list(sets))
+    return engine.run_sweep_tissues([s.tp for s in sets], [s.photons for s in sets],
+                                    [s.first_photon for s in sets])
 
 
 def _combine(parts: list[dict]) -> dict:
@@ -34,7 +52,8 @@ def _combine(parts: list[dict]) -> dict:
 
 def sweep(engine, sets, target_rel_se: float | None = None, pilot: int = 20_000,
           safety: float = 1.15) -> dict:
-    """Runs `sets` (abi.SweepSet) on an mcsub Engine.
+    """Runs `sets` (abi.SweepSet on an mcsub Engine, TissueSet on an mcxyz
+    Engine).
 
     Without a target every set runs its full budget in one launch.  With
     `target_rel_se`, a pilot launch of min(pilot, budget) photons per set
@@ -44,28 +63,24 @@ def sweep(engine, sets, target_rel_se: float | None = None, pilot: int = 20_000,
     (abi.SWEEP_FIELDS) and "launches".
     """
     if target_rel_se is None:
-        r = engine.run_sweep(list(sets))
+        r = _run(engine, sets)
         r["launches"] = 1
         return r
     pil = [_copy(s, photons=min(int(pilot), int(s.photons)), first_photon=0) for s in sets]
-    r1 = engine.run_sweep(pil)
+    r1 = _run(engine, pil)
     n1 = r1["photons"]
     me = r1["E"] / np.maximum(n1, 1)
     var = np.maximum(r1["E2"] / np.maximum(n1, 1) - me * me, 1e-30)
     need = np.ceil(safety * var / (target_rel_se * np.maximum(r1["Rd"], 1e-30)) ** 2)
     budget = np.array([s.photons for s in sets], dtype=np.float64)
     extra = np.clip(np.minimum(need, budget) - n1, 0, None).astype(np.int64)
-    idx = [i for i in range(len(sets)) if extra[i] > 0]
     parts = [r1]
     launches = 1
-    if idx:
-        top = [_copy(sets[i], photons=int(extra[i]), first_photon=int(n1[i])) for i in idx]
-        r2 = engine.run_sweep(top)
-        full = {k: np.zeros(len(sets)) for k in r2}
-        for j, i in enumerate(idx):
-            for k in r2:
-                full[k][i] = r2[k][j]
-        parts.append(full)
+    if np.any(extra > 0):
+        # every set keeps its index (its key) and continues its stream; sets
+        # already precise enough get an empty budget
+        top = [_copy(s, photons=int(extra[i]), first_photon=int(n1[i])) for i, s in enumerate(sets)]
+        parts.append(_run(engine, top))
         launches = 2
     out = _combine(parts)
     out["launches"] = launches

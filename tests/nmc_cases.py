@@ -165,3 +165,48 @@ def adjoint_case(N: int = 64, d: float = 0.01, seed: int = 7, sigma: float = 4.0
     mus = (50.0 + 250.0 * us).astype(np.float32)
     g = np.full((N, N, N), 0.85, np.float32)
     return rp, tp, v, ext, mua, mus, g, bins, dr
+
+
+# Two-term phase function of the spectral sweeps: forward HG lobe g_f = 0.9,
+# backward lobe g_b = 0.3 sampled and negated (mean cosine -0.3), HG shape
+# (alpha = 0.5) per lobe, forward weight 0.9.
+TT_SWEEP = dict(gf=0.9, af=0.5, gb=0.3, ab=0.5, cc=0.9)
+# seeded absorption amplitude ranges (1/cm) per tissue of the skin-vessel map
+SWEEP_MUA_RANGE = {EPIDERMIS: (1.0, 20.0), DERMIS: (0.05, 2.0), BLOOD: (10.0, 250.0)}
+
+
+def skin_vessel_spectral_tables(n_wavelengths: int = 351, seed: int = 2024, budget_lo: float = 1e5,
+                                budget_hi: float = 1e7):
+    """Spectral sweep on the skin-vessel map: wavelengths 400-750 nm; per
+    tissue (epidermis, dermis, blood) mus' = a (lambda / 500 nm)^-b with a in
+    [10, 40] /cm and b in [0.8, 2.0], and mua a sum of 3-6 Gaussians (centres
+    400-750 nm, widths 10-60 nm, amplitudes in SWEEP_MUA_RANGE) over 0.01 /cm,
+    all seeded; two-term phase TT_SWEEP with mus = mus' / (1 - g_eff),
+    g_eff = 0.9*0.9 - 0.1*0.3 = 0.78; air mua 1e-4, mus 1; budgets
+    log-uniform in [budget_lo, budget_hi].  Returns (wavelengths, list of
+    abi.TissueParams, budgets)."""
+    rng = np.random.default_rng(seed)
+    lam = np.linspace(400.0, 750.0, n_wavelengths)
+    g_eff = TT_SWEEP["cc"] * TT_SWEEP["gf"] - (1 - TT_SWEEP["cc"]) * TT_SWEEP["gb"]
+    mua = {}
+    mus = {}
+    for t in (EPIDERMIS, DERMIS, BLOOD):
+        a = rng.uniform(10.0, 40.0)
+        b = rng.uniform(0.8, 2.0)
+        k = int(rng.integers(3, 7))
+        lo, hi = SWEEP_MUA_RANGE[t]
+        amp = rng.uniform(lo, hi, k)
+        cen = rng.uniform(400.0, 750.0, k)
+        wid = rng.uniform(10.0, 60.0, k)
+        mua[t] = 0.01 + (amp[None, :] * np.exp(-((lam[:, None] - cen[None, :]) ** 2)
+                                                / (2 * wid[None, :] ** 2))).sum(1)
+        mus[t] = a * (lam / 500.0) ** (-b) / (1.0 - g_eff)
+    budgets = np.exp(rng.uniform(np.log(budget_lo), np.log(budget_hi), n_wavelengths)).astype(np.int64)
+    tables = []
+    for i in range(n_wavelengths):
+        tables.append(abi.tissue_params(
+            mua=[1e-4, mua[EPIDERMIS][i], mua[DERMIS][i], mua[BLOOD][i]],
+            mus=[1.0, mus[EPIDERMIS][i], mus[DERMIS][i], mus[BLOOD][i]],
+            g=[1.0, g_eff, g_eff, g_eff],
+            **{k: [v] * 4 for k, v in TT_SWEEP.items()}))
+    return lam, tables, budgets

@@ -65,3 +65,69 @@ def test_sweep_rd_against_oracle(gpu, oracle):
         z = (sw["Rd"][s] - rd_o) / np.hypot(sw["Rd_se"][s], se_o)
         print(f"set {s}: mua {q.mua:.3f} mus {q.mus:.1f} Rd gpu {sw['Rd'][s]:.5f} oracle {rd_o:.5f} z={z:.2f}")
         assert abs(z) <= 3.0
+
+
+# ---- voxel sweeps: many tissue tables on one skin-vessel map
+
+
+def _sv_engine(gpu, N=64, seed=11):
+    rp, tp, v, ext = cases.skin_vessel_case(N=N, d=0.005, seed=seed)
+    e = gpu.Engine(abi.SIM_MCXYZ_TT, 0, ext)
+    e.prepare_data(rp, tp, v)
+    return e, rp, v, ext
+
+
+def test_tissue_sweep_sets_equal_plain_runs(gpu):
+    lam, tables, budgets = cases.skin_vessel_spectral_tables(n_wavelengths=12, budget_lo=2e3, budget_hi=3e4)
+    e, rp, v, ext = _sv_engine(gpu)
+    with e:
+        sw = e.run_sweep_tissues(tables, budgets)
+    for s in (0, 5, 11):
+        ext_s = cases.skin_vessel_case(N=64, d=0.005, seed=11)[3]
+        ext_s.seed = ext.seed + (s << 32)
+        with gpu.Engine(abi.SIM_MCXYZ_TT, 0, ext_s) as p:
+            p.prepare_data(rp, tables[s], v)
+            p.run(0, int(budgets[s]))
+            sm = p.summary()
+        assert sw["photons"][s] == budgets[s] == sm["photons"]
+        assert sw["hops"][s] == sm["substeps"], s
+        assert sw["A"][s] == pytest.approx(sm["A"], rel=1e-6)
+        assert sw["E"][s] == pytest.approx(sm["rd_sum"], rel=1e-6)
+
+
+def test_tissue_sweep_rd_against_oracle(gpu, oracle):
+    lam, tables, budgets = cases.skin_vessel_spectral_tables(n_wavelengths=351)
+    pick = [0, 200]
+    e, rp, v, ext = _sv_engine(gpu)
+    with e:
+        sw = e.run_sweep_tissues([tables[i] for i in pick], [200_000] * len(pick))
+    for j, i in enumerate(pick):
+        ext_o = cases.skin_vessel_case(N=64, d=0.005)[3]
+        ext_o.seed = 777 + j  # independent streams
+        n_o = 30_000
+        o = oracle.run(abi.SIM_MCXYZ_TT, rp, tables[i], v, ext=ext_o, n=n_o, tallies=False)
+        rd_o = o["rd_sum"] / n_o
+        se_o = np.sqrt(max(o["rd_sumsq"] / n_o - rd_o ** 2, 0) / n_o)
+        z = (sw["Rd"][j] - rd_o) / np.hypot(sw["Rd_se"][j], se_o)
+        print(f"{lam[i]:.0f} nm: Rd gpu {sw['Rd'][j]:.5f} +- {sw['Rd_se'][j]:.5f} oracle {rd_o:.5f} +- {se_o:.5f} z={z:.2f}")
+        assert abs(z) <= 3.0
+
+
+def test_tissue_sweep_to_target_continues_each_stream(gpu):
+    from nmc_gb300.sweep import TissueSet, sweep
+
+    lam, tables, budgets = cases.skin_vessel_spectral_tables(n_wavelengths=24, budget_lo=1e4, budget_hi=4e5)
+    sets = [TissueSet(t, b) for t, b in zip(tables, budgets)]
+    e, rp, v, ext = _sv_engine(gpu)
+    with e:
+        r = sweep(e, sets, target_rel_se=0.01, pilot=5000)
+        # the pilot and the top-up are one stream per set: a single launch of
+        # the same counts gives the same photons
+        one = e.run_sweep_tissues(tables, r["photons"].astype(np.int64))
+    assert r["launches"] == 2
+    np.testing.assert_array_equal(one["photons"], r["photons"])
+    np.testing.assert_array_equal(one["hops"], r["hops"])
+    np.testing.assert_allclose(one["E"], r["E"], rtol=1e-9)
+    rel = r["Rd_se"] / r["Rd"]
+    capped = r["photons"] >= budgets
+    assert np.all((rel <= 0.0105) | capped), rel
