@@ -391,6 +391,155 @@ def run_sweep_workload(args) -> dict:
     }
 
 
+def run_sweep_mcsub_workload(args) -> dict:
+    """351-wavelength batched sweep on the mcsub geometry (the C1 medium; two-term phase
+    function, budgets log-uniform in 1e5-1e7).  Two comparisons on the same
+    photon streams: (1) every set's full budget in one persistent launch
+    against 351 plain per-wavelength runs; (2) time until every set reaches
+    1% relative standard error in Rd (pilot + top-up), batched (2 launches)
+    against plain (2 runs per wavelength)."""
+    import numpy as np
+    import torch
+
+    import nmc_cases as cases
+    from nmc_gb300 import abi, build, engine
+    from nmc_gb300 import sweep as nsweep
+
+    build.build()
+    torch.cuda.set_device(0)
+    lam, sets = cases.spectral_sweep_sets()
+    total = int(sum(s.photons for s in sets))
+    flags = abi.FLAG_SKIP_FLUENCE  # both sides tally Rd, J and totals only
+
+    def ext_for(seed):
+        return abi.ext_defaults(phase=abi.PHASE_TWO_TERM, sub_bins=101, sub_dr=0.01, sub_dz=0.01, seed=seed,
+                                flags=flags)
+
+    rp, tp, _ = cases.mcsub_case(tt=(0.9, 0.5, 0.3, 0.5, 0.9))
+    e = engine.Engine(abi.SIM_MCSUB, 0, ext_for(11))
+    e.prepare_data(rp, tp)
+    warm = [nsweep._copy(s, photons=20000) for s in sets[:8]]
+    e.run_sweep(warm)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    res, batched_s = timed(lambda: e.run_sweep(sets))
+    tgt, batched_tgt_s = timed(lambda: nsweep.sweep(e, sets, target_rel_se=0.01))
+
+    def plain(target):
+        rd = np.zeros(len(sets))
+        rse = np.zeros(len(sets))
+        photons = 0
+        for i, q in enumerate(sets):
+            e.set_ext(ext_for(11 + (i << 32)))
+            tps = abi.tissue_params(mua=[q.mua], mus=[q.mus], g=[q.g], gf=[q.gf], af=[q.af], gb=[q.gb],
+                                    ab=[q.ab], cc=[q.cc])
+            rp.n1, rp.n2 = q.n1, q.n2
+            e.prepare_data(rp, tps)
+            if target is None:
+                e.run(0, q.photons)
+            else:  # same pilot + top-up rule as the batched sweep
+                n1 = min(20000, q.photons)
+                e.run(0, n1)
+                s1 = e.summary()
+                me = s1["E"] / n1
+                var = max(s1["rd_sumsq"] / n1 - me * me, 1e-30)
+                rd1 = (s1["S"] + s1["E"]) / n1
+                need = int(np.ceil(1.15 * var / (target * max(rd1, 1e-30)) ** 2))
+                extra = max(min(need, q.photons) - n1, 0)
+                if extra:
+                    e.run(n1, extra)
+            sm = e.summary()
+            n = sm["photons"]
+            photons += n
+            me = sm["E"] / n
+            rd[i] = (sm["S"] + sm["E"]) / n
+            rse[i] = np.sqrt(max(sm["rd_sumsq"] / n - me * me, 0) / n) / rd[i]
+        return rd, rse, photons
+
+    (plain_rd, _, _), plain_s = timed(lambda: plain(None))
+    (plain_tgt_rd, plain_tgt_rse, plain_tgt_n), plain_tgt_s = timed(lambda: plain(0.01))
+    e.close()
+    rel_se = res["Rd_se"] / res["Rd"]
+    tgt_rel = tgt["Rd_se"] / tgt["Rd"]
+    return {
+        "metric": "photons/s, 351-wavelength batched sweep vs plain per-wavelength runs", "unit": "photons/s",
+        "value": total / batched_s, "plain_value": total / plain_s, "speedup": plain_s / batched_s,
+        "photons": total, "batched_s": batched_s, "plain_s": plain_s, "n_sets": len(sets),
+        "sets_at_1pct_se": int((rel_se <= 0.01).sum()), "max_rel_se": float(rel_se.max()),
+        "rd_matches_plain": float(np.max(np.abs(plain_rd - res["Rd"]) / res["Rd"])),
+        "to_1pct_se": {"batched_s": batched_tgt_s, "plain_s": plain_tgt_s, "speedup": plain_tgt_s / batched_tgt_s,
+                       "photons": int(tgt["photons"].sum()), "plain_photons": int(plain_tgt_n),
+                       "launches": tgt["launches"], "max_rel_se": float(tgt_rel.max()),
+                       "plain_max_rel_se": float(plain_tgt_rse.max())},
+        "hops_per_photon": float(res["hops"].sum() / total), "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "mcsub semi-infinite, 351 wavelengths 400-750 nm, two-term HG, budgets 1e5-1e7",
+                   "rng": "philox4x32-10", "tallies": "Rd, J(r), S/A/E per set (no F(r,z) on either side)"},
+    }
+
+
+def run_adjoint_workload(args) -> dict:
+    """Forward + pMC adjoint on the 64^3 per-voxel medium (smoothed seeded
+    noise mua in [0.1, 5], mus in [50, 300] /cm, g 0.85, n 1.4, pencil beam,
+    Rd(r) 128 x 0.005 cm), 1e7 photons: a plain forward against forward +
+    adjoint for a loss on Rd(r), and for a loss on Rd(r) plus the absorbed
+    weight per voxel."""
+    import numpy as np
+    import torch
+
+    import nmc_cases as cases
+    from nmc_gb300 import abi, build, engine
+
+    build.build()
+    torch.cuda.set_device(0)
+    rp, tp, v, ext, mua, mus, g, bins, dr = cases.adjoint_case()
+    n = args.photons if args.photons != PHOTONS_PER_STEP else 10_000_000
+    e = engine.Engine(abi.SIM_MCXYZ, 0, ext)
+    e.prepare_data(rp, tp, v)
+    e.set_radial_tally(bins, dr)
+    e.set_voxel_props(mua, mus, g)
+    G = np.random.default_rng(3).uniform(0.5, 1.5, bins + 1).astype(np.float32)
+    GF = np.ones(rp.Nx * rp.Ny * rp.Nz, np.float32)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    fwd = lambda: (e.reset(), e.run(0, n))
+    adj = lambda: (e.reset(), e.adjoint_forward(0, n, 8 * n), e.adjoint_backward(G))
+    adj_f = lambda: (e.reset(), e.adjoint_forward(0, n, 8 * n), e.adjoint_backward(G, GF))
+    for f in (fwd, adj, adj_f):
+        for _ in range(max(args.warmup, 1)):
+            f()
+    K = max(args.steps, 1)
+    t_fwd = min(timed(fwd) for _ in range(K))
+    t_adj = min(timed(adj) for _ in range(K))
+    t_adj_f = min(timed(adj_f) for _ in range(K))
+    sm = e.summary()
+    rd = e.tally(abi.TALLY_RD_R).sum() / n
+    e.close()
+    return {
+        "metric": "photons/s, forward + pMC adjoint vs plain forward, 64^3 per-voxel medium",
+        "unit": "photons/s", "value": n / t_adj, "plain_value": n / t_fwd,
+        "cost_ratio_rd": t_adj / t_fwd, "cost_ratio_rd_fluence": t_adj_f / t_fwd,
+        "forward_s": t_fwd, "adjoint_rd_s": t_adj, "adjoint_rd_fluence_s": t_adj_f, "photons": n,
+        "rd": rd, "substeps_per_photon": sm["substeps"] / max(sm["photons"], 1), "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "64^3 x 0.01 cm per-voxel medium, mua 0.1-5, mus 50-300 /cm (smoothed seeded "
+                               "noise), g 0.85, n 1.4, pencil beam, Rd(r) 128 x 0.005 cm",
+                   "timing": f"best of {K} after {max(args.warmup, 1)} warm-up, host clock around "
+                             "synchronised calls (includes the event list and gradient copies)"},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -401,10 +550,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warm-up and timed transport launches (for ncu)")
-    ap.add_argument("--workload", default="skinvessel", choices=["skinvessel", "sweep"])
+    ap.add_argument("--workload", default="skinvessel", choices=["skinvessel", "sweep", "sweep_mcsub", "adjoint"])
     args = ap.parse_args()
     if args.workload == "sweep":
         out = run_sweep_workload(args)
+    elif args.workload == "sweep_mcsub":
+        out = run_sweep_mcsub_workload(args)
+    elif args.workload == "adjoint":
+        out = run_adjoint_workload(args)
     else:
         out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if out:

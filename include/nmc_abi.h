@@ -148,7 +148,10 @@ enum {
   NMC_FLAG_PRECISE_MATH = 1u << 2,
   /* Skip the fluence tally (mcsub F(r,z)) when only Rd, J and the totals
    * are wanted. */
-  NMC_FLAG_SKIP_FLUENCE = 1u << 3
+  NMC_FLAG_SKIP_FLUENCE = 1u << 3,
+  /* mcsub: deposit F(r,z) and J(r) straight into the global u64 tallies
+   * instead of privatising them per block in shared memory. */
+  NMC_FLAG_GLOBAL_TALLIES = 1u << 4
 };
 
 typedef struct nmc_ext {
@@ -363,6 +366,30 @@ nmc_status nmc_adjoint_backward(nmc_handle* h, const float* grad_rd_r, double* g
  * replayed twice (its total score first, then the accumulation). */
 nmc_status nmc_adjoint_backward_ex(nmc_handle* h, const float* grad_rd_r, const float* grad_absorbed,
                                    double* grad_mua, double* grad_mus, double* grad_g);
+
+/* -------------------------------------------------------------- autotune */
+/* One launch configuration the autotuner timed. */
+typedef struct nmc_tune_entry {
+  int32_t block_size, blocks_per_sm;
+  uint32_t flags; /* NMC_FLAG_GLOBAL_TALLIES or 0 */
+  float ms;       /* kernel time of the tuning run */
+} nmc_tune_entry;
+
+typedef struct nmc_tune_result {
+  nmc_tune_entry best, fallback; /* chosen; the defaults (block 0 / blocks 0) */
+  int32_t n_tried;
+  nmc_tune_entry tried[48];
+} nmc_tune_result;
+
+/* Times the handle's kernel on photons [0, photons) under each candidate
+ * launch configuration (block size; resident blocks per SM, i.e. photons in
+ * flight per SM; for mcsub, tallies privatised in shared memory or not), keeps
+ * the fastest in the handle's nmc_ext (block_size, blocks_per_sm, flags) and
+ * clears the tallies.  Results do not depend on the configuration: every
+ * photon's stream is a function of its id only.  No reference counterpart
+ * (the reference dispatches 1e4 threads in threadgroups of the pipeline's
+ * maximum, MetalMC.m:485-495). */
+nmc_status nmc_autotune(nmc_handle* h, uint64_t photons, nmc_tune_result* out);
 
 /* ------------------------------------------------------- batched sweeps */
 /* One parameter set of a batched sweep (e.g. one wavelength) on the mcsub

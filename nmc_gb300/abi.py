@@ -41,6 +41,7 @@ FLAG_TT_REPLAY_RUN1 = 1 << 0
 FLAG_NO_HARD_KILL = 1 << 1
 FLAG_PRECISE_MATH = 1 << 2
 FLAG_SKIP_FLUENCE = 1 << 3
+FLAG_GLOBAL_TALLIES = 1 << 4
 
 FATE_ALIVE, FATE_ESCAPED, FATE_ROULETTE, FATE_MINWEIGHT, FATE_MAXSCATT, FATE_BOUNDARY, FATE_STEPCAP = range(7)
 
@@ -144,6 +145,18 @@ class Ext(C.Structure):
         ("timeout_s", C.c_double),
         ("reserved", C.c_uint32 * 8),
     ]
+
+
+class TuneEntry(C.Structure):
+    """nmc_tune_entry."""
+
+    _fields_ = [("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("flags", C.c_uint32), ("ms", C.c_float)]
+
+
+class TuneResult(C.Structure):
+    """nmc_tune_result."""
+
+    _fields_ = [("best", TuneEntry), ("fallback", TuneEntry), ("n_tried", C.c_int32), ("tried", TuneEntry * 48)]
 
 
 class Summary(C.Structure):

@@ -96,6 +96,7 @@ struct SubParams {
   int phase_kind;    // SubPhase
   int fast_math;
   int skip_F;        // no F(r,z) tally
+  int global_tallies;  // F(r,z), J(r) straight to global memory (no shared-memory privatisation)
   unsigned long long* J;  // fixed point 2^-32, BINS+1
   unsigned long long* F;  // (BINS+1)^2
   DevSums* sums;

@@ -280,7 +280,7 @@ size_t mcsub_smem_bytes(int bins) {
 static bool smem_fits(int bins) { return mcsub_smem_bytes(bins) <= 200 * 1024; }
 
 static cudaError_t prepare(const SubParams& p, bool trace, const void** f, size_t* sh) {
-  const bool smem = !p.skip_F && smem_fits(p.bins);
+  const bool smem = !p.skip_F && !p.global_tallies && smem_fits(p.bins);
   *f = p.fast_math ? pick2<true>(p, trace, smem) : pick2<false>(p, trace, smem);
   *sh = smem ? mcsub_smem_bytes(p.bins) : 0;
   if (*sh > 48 * 1024)

@@ -160,6 +160,7 @@ void fill_sub(SubParams& p, const nmc_run_params& rp, const nmc_tissue_params& t
                                                       : kPhaseHG;
   p.fast_math = (e.flags & NMC_FLAG_PRECISE_MATH) ? 0 : 1;
   p.skip_F = (e.flags & NMC_FLAG_SKIP_FLUENCE) ? 1 : 0;
+  p.global_tallies = (e.flags & NMC_FLAG_GLOBAL_TALLIES) ? 1 : 0;
   p.rng = rng_params(e, NMC_SIM_MCSUB);
   p.step_cap = 10000000u;
 }

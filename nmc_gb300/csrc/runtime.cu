@@ -30,6 +30,18 @@ struct EventPair {
   cudaEvent_t a = nullptr, b = nullptr;
 };
 
+// Regions of the result staging buffer (floats): the tallies
+// nmc_get_compute_results can return, converted on the device.
+enum StageRegion { kStJ, kStF, kStF3D, kStSlots, kStRd2D, kStDet, kStSums, kStN };
+
+// A CUDA graph that converts and copies one combination of regions (mask of
+// 1 << StageRegion): captured once per handle and combination, replayed by
+// every nmc_get_compute_results.
+struct ReduceGraph {
+  unsigned mask;
+  cudaGraphExec_t exec;
+};
+
 struct nmc_handle {
   int sim = 0;
   int device = 0;
@@ -54,6 +66,8 @@ struct nmc_handle {
   float* d_stage = nullptr;  // conversion buffer for results (floats)
   float* h_stage = nullptr;  // pinned host copy
   size_t stage_elems = 0;
+  size_t st_off[kStN] = {}, st_len[kStN] = {};
+  std::vector<ReduceGraph> graphs;
   std::vector<EventPair> pending;
   std::vector<EventPair> pool;
   double kernel_ms = 0.0;
@@ -109,6 +123,8 @@ void free_buffers(nmc_handle* h) {
   dfree(h->d_rdr);
   dfree(h->d_ev);
   dfree(h->d_evcount);
+  for (ReduceGraph& g : h->graphs) cudaGraphExecDestroy(g.exec);
+  h->graphs.clear();
   if (h->h_stage) cudaFreeHost(h->h_stage);
   h->h_stage = nullptr;
   h->nvox = h->n2d = h->nslots = h->nJ = h->nF = h->stage_elems = 0;
@@ -365,21 +381,49 @@ __global__ void u32_to_f32(const unsigned int* __restrict__ s, float* __restrict
     d[k] = __uint_as_float(s[k]);
 }
 
-// Converts a device tally into h->h_stage as floats (u32 counts are passed
-// through bit-exactly and reinterpreted by the caller).
-nmc_status stage_tally(nmc_handle* h, const void* dsrc, size_t n, bool counts) {
-  if (n > h->stage_elems) return fail(h, NMC_EINVAL, "staging buffer too small");
-  const int block = 256;
-  const int grid = (int)std::min<size_t>((n + block - 1) / block, (size_t)h->nsm * 8);
-  if (counts)
-    u32_to_f32<<<grid, block, 0, h->stream>>>((const unsigned int*)dsrc, h->d_stage, n);
-  else
-    unfix_f32<<<grid, block, 0, h->stream>>>((const unsigned long long*)dsrc, h->d_stage, n,
-                                             nmc::kUnfix);
-  NMC_CUDA(h, cudaGetLastError());
-  NMC_CUDA(h, cudaMemcpyAsync(h->h_stage, h->d_stage, n * sizeof(float), cudaMemcpyDeviceToHost,
-                              h->stream));
-  return wait_stream(h);
+// The reduction graph for `mask` (regions of StageRegion), captured on first
+// use: per region a conversion kernel (u64 fixed point -> float, or u32 count
+// bits) into the device staging buffer, then its copy to pinned host memory.
+nmc_status reduce_graph(nmc_handle* h, unsigned mask, cudaGraphExec_t* out) {
+  for (const ReduceGraph& g : h->graphs)
+    if (g.mask == mask) {
+      *out = g.exec;
+      return NMC_OK;
+    }
+  const void* src[kStN] = {h->d_J, h->d_F, h->d_F3D, h->d_slots, h->d_Rd2D, h->d_Det, h->d_sums};
+  NMC_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < kStN && e == cudaSuccess; ++k) {
+    if (!(mask >> k & 1u) || h->st_len[k] == 0) continue;
+    const size_t n = h->st_len[k];
+    float* dst = h->d_stage + h->st_off[k];
+    if (k == kStSums) {
+      e = cudaMemcpyAsync(dst, src[k], sizeof(DevSums), cudaMemcpyDeviceToDevice, h->stream);
+    } else {
+      const int block = 256;
+      const int grid = (int)std::min<size_t>((n + block - 1) / block, (size_t)h->nsm * 8);
+      if (k == kStDet)
+        u32_to_f32<<<grid, block, 0, h->stream>>>((const unsigned int*)src[k], dst, n);
+      else
+        unfix_f32<<<grid, block, 0, h->stream>>>((const unsigned long long*)src[k], dst, n, nmc::kUnfix);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h->h_stage + h->st_off[k], dst, n * sizeof(float), cudaMemcpyDeviceToHost, h->stream);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return cuda_fail(h, e != cudaSuccess ? e : e2, "capturing the result reduction");
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(h, e, "instantiating the result reduction");
+  h->graphs.push_back(ReduceGraph{mask, exec});
+  *out = exec;
+  return NMC_OK;
 }
 
 }  // namespace
@@ -469,13 +513,11 @@ nmc_status nmc_prepare(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue
   h->prepared = false;
   h->rp = *rp;
   h->tp = *tp;
-  size_t stage = 4096;
   if (h->sim == NMC_SIM_MCSUB) {
     h->nJ = (size_t)h->ext.sub_bins + 1;
     h->nF = h->nJ * h->nJ;
     NMC_CUDA(h, cudaMalloc((void**)&h->d_J, h->nJ * 8));
     NMC_CUDA(h, cudaMalloc((void**)&h->d_F, h->nF * 8));
-    stage = std::max(stage, h->nF);
   } else {
     h->nvox = (size_t)rp->Nx * rp->Ny * rp->Nz;
     h->n2d = (size_t)rp->Nx * rp->Ny;
@@ -486,7 +528,15 @@ nmc_status nmc_prepare(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue
     NMC_CUDA(h, cudaMalloc((void**)&h->d_Rd2D, h->n2d * 8));
     NMC_CUDA(h, cudaMalloc((void**)&h->d_Det, h->n2d * 4));
     NMC_CUDA(h, cudaMalloc((void**)&h->d_slots, h->nslots * 8));
-    stage = std::max({stage, h->nvox, h->n2d, h->nslots});
+  }
+  // one region per tally, 256-byte aligned
+  const size_t lens[kStN] = {h->nJ, h->nF, h->nvox, h->nslots, h->n2d,
+                             h->sim == NMC_SIM_MCXYZ ? h->n2d : 0, (sizeof(DevSums) + 3) / 4};
+  size_t stage = 0;
+  for (int k = 0; k < kStN; ++k) {
+    h->st_off[k] = stage;
+    h->st_len[k] = lens[k];
+    stage += (lens[k] + 63) & ~(size_t)63;
   }
   h->stage_elems = stage;
   NMC_CUDA(h, cudaMalloc((void**)&h->d_stage, stage * sizeof(float)));
@@ -593,6 +643,84 @@ nmc_status nmc_run_traced(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_
   return st;
 }
 
+nmc_status nmc_autotune(nmc_handle* h, uint64_t photons, nmc_tune_result* out) {
+  if (!h || !out) return fail(h, NMC_EINVAL, "null argument");
+  if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
+  if (photons == 0) return fail(h, NMC_EINVAL, "photons must be > 0");
+  nmc_status st = sync_all(h);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  std::memset(out, 0, sizeof *out);
+  const nmc_ext saved = h->ext;
+  const bool sub = h->sim == NMC_SIM_MCSUB;
+  const bool tt = h->sim == NMC_SIM_MCXYZ_TT;
+  auto apply = [&](int block, int bps, uint32_t priv) {
+    h->ext = saved;
+    h->ext.block_size = block;
+    h->ext.blocks_per_sm = bps;
+    h->ext.flags = (saved.flags & ~(uint32_t)NMC_FLAG_GLOBAL_TALLIES) | priv;
+    return sub ? build_sub(h) : build_xyz(h);
+  };
+  auto restore = [&](nmc_status s) {
+    h->ext = saved;
+    const nmc_status b = sub ? build_sub(h) : build_xyz(h);
+    return s != NMC_OK ? s : b;
+  };
+  auto time_run = [&](float* ms) -> nmc_status {
+    const double before = h->kernel_ms;
+    nmc_status s = launch(h, 0, photons, nullptr, nullptr, 0);
+    if (s == NMC_OK) s = sync_all(h);
+    if (s != NMC_OK && s != NMC_ESTEPCAP) return s;
+    *ms = (float)(h->kernel_ms - before);
+    return NMC_OK;
+  };
+  auto max_resident = [&](int block, int* bps) -> nmc_status {
+    cudaError_t e;
+    if (sub)
+      e = nmc::mcsub_occupancy(h->sp, false, block, bps);
+    else if (h->voxel_mode)
+      e = nmc::mcxyz_voxel_occupancy(nmc::kVoxel, false, block, bps);
+    else
+      e = nmc::mcxyz_occupancy(tt, false, block, bps);
+    return e == cudaSuccess ? NMC_OK : cuda_fail(h, e, "occupancy query");
+  };
+  // the defaults, run twice (the first also warms the caches)
+  const uint32_t priv0 = saved.flags & NMC_FLAG_GLOBAL_TALLIES;
+  float ms = 0.f;
+  if ((st = apply(0, 0, priv0)) != NMC_OK || (st = time_run(&ms)) != NMC_OK || (st = time_run(&ms)) != NMC_OK)
+    return restore(st);
+  out->fallback = nmc_tune_entry{0, 0, priv0, ms};
+  out->best = out->fallback;
+  const std::vector<int> blocks = sub ? std::vector<int>{128, 256, 512} : std::vector<int>{64, 128, 256};
+  std::vector<uint32_t> privs{0u};
+  if (sub && !(saved.flags & NMC_FLAG_SKIP_FLUENCE) && nmc::mcsub_smem_bytes(saved.sub_bins) <= 200 * 1024)
+    privs.push_back((uint32_t)NMC_FLAG_GLOBAL_TALLIES);
+  for (int block : blocks) {
+    for (uint32_t priv : privs) {
+      if ((st = apply(block, 0, priv)) != NMC_OK) return restore(st);
+      int maxb = 0;
+      if ((st = max_resident(block, &maxb)) != NMC_OK) return restore(st);
+      if (maxb < 1) continue;
+      std::vector<int> cands{maxb, std::max(1, (3 * maxb) / 4), std::max(1, maxb / 2)};
+      std::sort(cands.begin(), cands.end());
+      cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
+      for (int bps : cands) {
+        if (out->n_tried >= (int)(sizeof out->tried / sizeof out->tried[0])) break;
+        if ((st = apply(block, bps, priv)) != NMC_OK || (st = time_run(&ms)) != NMC_OK) return restore(st);
+        const nmc_tune_entry t{block, bps, priv, ms};
+        out->tried[out->n_tried++] = t;
+        if (ms < out->best.ms) out->best = t;
+      }
+    }
+  }
+  h->ext = saved;
+  h->ext.block_size = out->best.block_size;
+  h->ext.blocks_per_sm = out->best.blocks_per_sm;
+  h->ext.flags = (saved.flags & ~(uint32_t)NMC_FLAG_GLOBAL_TALLIES) | out->best.flags;
+  st = sub ? build_sub(h) : build_xyz(h);
+  if (st != NMC_OK) return st;
+  return nmc_reset(h);
+}
+
 size_t nmc_tally_size(nmc_handle* h, int32_t which) {
   if (!h || !h->prepared) return 0;
   switch (which) {
@@ -642,35 +770,43 @@ nmc_status nmc_get_compute_results(nmc_handle* h, float* J, float* F, float* F3D
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   nmc_status st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
-  auto add_f = [&](float* dst, const void* src, size_t n, bool counts) -> nmc_status {
-    if (!dst || !src || n == 0) return NMC_OK;
-    nmc_status s = stage_tally(h, src, n, counts);
-    if (s != NMC_OK) return s;
-    if (counts) {
-      const unsigned int* c = reinterpret_cast<const unsigned int*>(h->h_stage);
-      for (size_t k = 0; k < n; ++k) reinterpret_cast<int32_t*>(dst)[k] += (int32_t)c[k];
-    } else {
-      for (size_t k = 0; k < n; ++k) dst[k] += h->h_stage[k];
-    }
-    return NMC_OK;
-  };
+  float* dst[kStN] = {nullptr};
   if (h->sim == NMC_SIM_MCSUB) {
-    if ((st = add_f(J, h->d_J, h->nJ, false)) != NMC_OK) return st;
-    if ((st = add_f(F, h->d_F, h->nF, false)) != NMC_OK) return st;
-    if (SAE) {
+    dst[kStJ] = J;
+    dst[kStF] = F;
+    dst[kStSums] = SAE;
+  } else {
+    dst[kStF3D] = F3D;
+    dst[kStSlots] = Rd;
+    dst[kStRd2D] = Rd2D;
+    if (h->sim == NMC_SIM_MCXYZ) dst[kStDet] = reinterpret_cast<float*>(DetPhot2D);
+  }
+  unsigned mask = 0;
+  for (int k = 0; k < kStN; ++k)
+    if (dst[k] && h->st_len[k]) mask |= 1u << k;
+  if (!mask) return NMC_OK;
+  cudaGraphExec_t exec = nullptr;
+  if ((st = reduce_graph(h, mask, &exec)) != NMC_OK) return st;
+  NMC_CUDA(h, cudaGraphLaunch(exec, h->stream));
+  if ((st = wait_stream(h)) != NMC_OK) return st;
+  for (int k = 0; k < kStN; ++k) {
+    if (!(mask >> k & 1u)) continue;
+    const float* src = h->h_stage + h->st_off[k];
+    const size_t n = h->st_len[k];
+    if (k == kStSums) {
       DevSums s;
-      NMC_CUDA(h, cudaMemcpy(&s, h->d_sums, sizeof s, cudaMemcpyDeviceToHost));
+      std::memcpy(&s, src, sizeof s);
       SAE[0] += (float)(s.S * nmc::kUnfix);
       SAE[1] += (float)(s.A * nmc::kUnfix);
       SAE[2] += (float)(s.E * nmc::kUnfix);
+    } else if (k == kStDet) {
+      const unsigned int* c = reinterpret_cast<const unsigned int*>(src);
+      for (size_t i = 0; i < n; ++i) DetPhot2D[i] += (int32_t)c[i];
+    } else {
+      float* d = dst[k];
+      for (size_t i = 0; i < n; ++i) d[i] += src[i];
     }
-    return NMC_OK;
   }
-  if ((st = add_f(F3D, h->d_F3D, h->nvox, false)) != NMC_OK) return st;
-  if ((st = add_f(Rd, h->d_slots, h->nslots, false)) != NMC_OK) return st;
-  if ((st = add_f(Rd2D, h->d_Rd2D, h->n2d, false)) != NMC_OK) return st;
-  if (h->sim == NMC_SIM_MCXYZ)
-    if ((st = add_f(reinterpret_cast<float*>(DetPhot2D), h->d_Det, h->n2d, true)) != NMC_OK) return st;
   return NMC_OK;
 }
 

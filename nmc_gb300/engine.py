@@ -67,6 +67,8 @@ def lib() -> C.CDLL:
         L.nmc_probe_issue_peaks.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.nmc_run_sweep.argtypes = [H, C.POINTER(abi.SweepSet), C.c_int32, _P, _P]
         L.nmc_run_sweep.restype = C.c_int
+        L.nmc_autotune.argtypes = [H, C.c_uint64, C.POINTER(abi.TuneResult)]
+        L.nmc_autotune.restype = C.c_int
         L.nmc_run_sweep_tissues.argtypes = [H, C.POINTER(abi.TissueParams), _P, _P, C.c_int32, _P]
         L.nmc_run_sweep_tissues.restype = C.c_int
         L.nmc_set_voxel_props.argtypes = [H, _P, _P, _P]
@@ -217,6 +219,20 @@ class Engine:
         if with_J:
             res["J"] = J
         return res
+
+    def autotune(self, photons: int = 200_000) -> dict:
+        """Times the kernel under candidate launch shapes on photons
+        [0, photons), keeps the fastest in the handle and clears the tallies."""
+        r = abi.TuneResult()
+        self._check(self._L.nmc_autotune(self._h, int(photons), C.byref(r)), "nmc_autotune")
+
+        def d(t):
+            return {"block_size": t.block_size, "blocks_per_sm": t.blocks_per_sm, "flags": t.flags, "ms": t.ms}
+
+        self.ext.block_size = r.best.block_size
+        self.ext.blocks_per_sm = r.best.blocks_per_sm
+        self.ext.flags = (self.ext.flags & ~abi.FLAG_GLOBAL_TALLIES) | r.best.flags
+        return {"best": d(r.best), "default": d(r.fallback), "tried": [d(r.tried[i]) for i in range(r.n_tried)]}
 
     def run_sweep_tissues(self, tables, photons, first_photon=None) -> dict:
         """Batched sweep on a voxel tissue map (mcxyz handle): set s runs

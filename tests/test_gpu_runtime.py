@@ -1,0 +1,83 @@
+"""Runtime pieces around the kernels: the autotuner and the graph-captured
+result reduction.
+
+Every photon's random stream is a function of its id only, so a launch
+shape chosen by the autotuner must leave every integer tally unchanged; and
+the reduction graph must return exactly the device tallies, accumulated
+(+=) into the caller's arrays as the reference's getComputeResults does
+(MetalMC.m:508-538).
+"""
+import numpy as np
+import pytest
+
+from nmc_gb300 import abi
+import nmc_cases as cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _tallies(e, which):
+    return {w: e.tally(w) for w in which}
+
+
+@pytest.mark.parametrize("kind", ["mcsub", "mcxyz"])
+def test_autotune_keeps_results(gpu, kind):
+    if kind == "mcsub":
+        rp, tp, ext = cases.mcsub_case()
+        sim, v, which, n = abi.SIM_MCSUB, None, (abi.TALLY_J, abi.TALLY_F), 100_000
+    else:
+        rp, tp, v, ext = cases.skin_vessel_case(N=64)
+        sim, which, n = abi.SIM_MCXYZ, (abi.TALLY_F3D, abi.TALLY_RD2D, abi.TALLY_DETPHOT2D), 50_000
+    with gpu.Engine(sim, 0, ext) as e:
+        e.prepare_data(rp, tp, v)
+        e.run(0, n)
+        before = _tallies(e, which)
+        s0 = e.summary()
+        r = e.autotune(50_000)
+        print(kind, "default", r["default"], "best", r["best"], "tried", len(r["tried"]))
+        assert len(r["tried"]) >= 3
+        assert r["best"]["ms"] <= r["default"]["ms"]
+        assert e.summary()["photons"] == 0  # tallies cleared
+        e.run(0, n)
+        after = _tallies(e, which)
+        s1 = e.summary()
+    for w in which:
+        np.testing.assert_array_equal(before[w], after[w])
+    for k in ("photons", "substeps", "scatters", "S", "A", "E", "rd_sum"):
+        assert s0[k] == s1[k], k
+
+
+@pytest.mark.parametrize("kind", ["mcsub", "mcxyz"])
+def test_reduction_graph_returns_the_tallies(gpu, kind):
+    if kind == "mcsub":
+        rp, tp, ext = cases.mcsub_case()
+        sim, v, n = abi.SIM_MCSUB, None, 50_000
+    else:
+        rp, tp, v, ext = cases.skin_vessel_case(N=64)
+        sim, n = abi.SIM_MCXYZ, 20_000
+    with gpu.Engine(sim, 0, ext) as e:
+        e.prepare_data(rp, tp, v)
+        e.run(0, n)
+        r1 = e.get_compute_results()
+        r2 = e.get_compute_results()  # the graph replayed
+        if kind == "mcsub":
+            ref = {"J": e.tally(abi.TALLY_J), "F": e.tally(abi.TALLY_F)}
+            sm = e.summary()
+            np.testing.assert_allclose(r1["SAE"], np.float32([sm["S"], sm["A"], sm["E"]]), rtol=1e-6)
+        else:
+            ref = {"F3D": e.tally(abi.TALLY_F3D), "Rd2D": e.tally(abi.TALLY_RD2D),
+                   "DetPhot2D": e.tally(abi.TALLY_DETPHOT2D)}
+        for k, want in ref.items():
+            np.testing.assert_array_equal(r1[k], want.astype(np.float32).astype(r1[k].dtype))
+            np.testing.assert_array_equal(r2[k], r1[k])
+        # accumulation into the caller's arrays: a second call adds again
+        acc = {k: np.array(r1[k]) for k in r1}
+        L = e._L
+        if kind == "mcxyz":
+            args = [None, None, acc["F3D"], None, acc["Rd"], acc["Rd2D"], acc["DetPhot2D"]] + [None] * 9
+        else:
+            args = [acc["J"], acc["F"], None, acc["SAE"], None, None, None] + [None] * 9
+        from nmc_gb300.engine import _ptr
+        e._check(L.nmc_get_compute_results(e._h, *[_ptr(a) for a in args]), "nmc_get_compute_results")
+        for k in acc:
+            np.testing.assert_allclose(acc[k], 2 * r1[k], rtol=1e-6)
