@@ -164,6 +164,7 @@ def run_ours(args) -> dict:
     rp, tp, v, ext = cases.skin_vessel_case(N=200)
     e = engine.Engine(abi.SIM_MCXYZ, local, ext)
     e.prepare_data(rp, tp, v)
+    tuned = e.autotune(args.tune) if args.tune > 0 else None
     stream = torch.cuda.ExternalStream(e.stream)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")  # > L2 (129 MB)
     base = rank * 10 ** 12  # disjoint photon ids per rank
@@ -263,7 +264,9 @@ def run_ours(args) -> dict:
                    "l2": "256 MB buffer written before each timed step", "rng": "philox4x32-10",
                    "rd": rd_mean, "rd_rel_se": rd_se / rd_mean if rd_mean else None,
                    "substeps_per_photon": substeps / max(P * args.steps, 1),
-                   "parallelism": f"replicas{world}"},
+                   "parallelism": f"replicas{world}",
+                   "launch": ({"autotuned_on_photons": args.tune, **tuned["best"]} if tuned
+                              else {"block_size": 256, "blocks_per_sm": "max resident"})},
         "e2e": {"value": e2e_value, "unit": "photons/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "fp32_issue", "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
@@ -548,6 +551,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--photons", type=int, default=PHOTONS_PER_STEP)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--tune", type=int, default=0,
+                    help="autotune the launch shape on this many photons before the warm-up (0: defaults)")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warm-up and timed transport launches (for ncu)")
     ap.add_argument("--workload", default="skinvessel", choices=["skinvessel", "sweep", "sweep_mcsub", "adjoint"])

@@ -367,6 +367,87 @@ nmc_status nmc_adjoint_backward(nmc_handle* h, const float* grad_rd_r, double* g
 nmc_status nmc_adjoint_backward_ex(nmc_handle* h, const float* grad_rd_r, const float* grad_absorbed,
                                    double* grad_mua, double* grad_mus, double* grad_g);
 
+/* ---------------------------------- polarised E-field, CBS cone and Raman */
+/* The reference's NMC_SIM_POLARIZATION_CBS_ELECTRIC_FIELDS and NMC_SIM_RAMAN
+ * kernels are empty (kernels.metal:1122-1202); nmc_create still refuses those
+ * kinds.  These entry points are this engine's own polarised transport for a
+ * semi-infinite slab of spheres; the per-pixel outputs mirror the buffers the
+ * reference host allocates for that kind (MetalMC.m:206-328: PolXX/XY/YX/YY,
+ * Rd2D, DetPhot2D, Phase0-3 maps and PolVsScatt[4][MAX_SCATT_POL]). */
+
+/* Mie amplitudes of a homogeneous sphere (size parameter x = 2 pi n_medium a
+ * / lambda, relative index m = m_re + i m_im): S is n_angles x 4 floats
+ * (Re S1, Im S1, Re S2, Im S2) at theta_j = j pi / (n_angles - 1); efficiencies
+ * and the asymmetry g.  Any output may be NULL. */
+nmc_status nmc_mie(double x, double m_re, double m_im, int32_t n_angles, float* S, double* q_ext,
+                   double* q_sca, double* g);
+
+typedef struct nmc_efield_config {
+  float mua, mus;             /* primary wavelength, cm^-1 */
+  float wavelength_cm;        /* primary vacuum wavelength */
+  float raman_mua, raman_mus; /* at the Raman wavelength, cm^-1 */
+  float raman_wavelength_cm;
+  float mu_raman;             /* conversion coefficient, cm^-1 (0: none) */
+  float n_medium, n_outside;  /* refractive indices */
+  int32_t n_angles;           /* rows of both S tables (>= 2) */
+  int32_t cone_n;             /* backscattering cone grid, cone_n x cone_n (2..1024) */
+  float cone_half_angle;      /* rad, in air */
+  int32_t sep_n;              /* first-to-last scattering separation histogram, bins per axis (2..4096) */
+  float sep_half_width;       /* cm */
+  int32_t map_n;              /* exit maps, map_n x map_n pixels centred on the beam (1..1024) */
+  float map_dx;               /* cm per pixel */
+  int32_t depth_bins;         /* Raman conversion depth histogram (1..4096) */
+  float depth_dz;             /* cm per bin */
+  uint64_t seed;
+  uint32_t flags;             /* NMC_FLAG_PRECISE_MATH */
+  uint32_t pad;
+} nmc_efield_config;
+
+typedef struct nmc_efield_setting {
+  float pol_angle;         /* azimuth of the incident linear polarisation (rad, from x) */
+  float theta_in, phi_in;  /* incidence direction in air (rad; 0 = normal) */
+  uint32_t pad;
+  uint64_t photons;
+} nmc_efield_setting;
+#ifdef __cplusplus
+static_assert(sizeof(nmc_efield_config) == 88, "nmc_efield_config layout");
+static_assert(sizeof(nmc_efield_setting) == 24, "nmc_efield_setting layout");
+#endif
+
+/* Per-setting results of nmc_efield_run, NMC_EF_FIELDS doubles per setting.
+ * "co" / "cross": analyser parallel / perpendicular to the incident
+ * polarisation; "multi": photons scattered at least twice, the part that
+ * interferes with its time-reversed path; "interf": the interference term at
+ * exact backscattering, sum of w Re(E conj(E_reversed)). */
+enum {
+  NMC_EF_PHOTONS = 0, NMC_EF_SPECULAR, NMC_EF_RD, NMC_EF_RD2, NMC_EF_CO, NMC_EF_CROSS,
+  NMC_EF_MULTI_CO, NMC_EF_MULTI_CROSS, NMC_EF_INTERF_CO, NMC_EF_INTERF_CROSS, NMC_EF_SEP_OUTSIDE,
+  NMC_EF_RAMAN_N, NMC_EF_RAMAN_RD, NMC_EF_RAMAN_CO, NMC_EF_RAMAN_CROSS, NMC_EF_SCATTERS,
+  NMC_EF_FIELDS
+};
+/* Exit maps, map_n^2 floats each, index ix*map_n + iy. */
+enum {
+  NMC_EF_MAP_XX = 0, NMC_EF_MAP_XY, NMC_EF_MAP_YX, NMC_EF_MAP_YY, NMC_EF_MAP_RD, NMC_EF_MAP_DET,
+  NMC_EF_MAP_PHASE0, NMC_EF_MAP_PHASE1, NMC_EF_MAP_PHASE2, NMC_EF_MAP_PHASE3, NMC_EF_MAPS
+};
+#define NMC_EF_MAX_ORDER 150 /* PolVsScatt orders 0..150, MAX_SCATT_POL (definitions.h:25) */
+
+/* Runs every setting's photons in one persistent launch on `device`.
+ * S_primary / S_raman: n_angles x 4 Mie tables at the two wavelengths.
+ * Outputs (any but `out` may be NULL), per setting s:
+ *   out[s*NMC_EF_FIELDS + k];
+ *   cone[((s*2 + c)*cone_n + i)*cone_n + j] as complex (2 floats): the
+ *     interference field of channel c (0 co, 1 cross) at angles
+ *     (theta_x, theta_y) = (-h + (i + 0.5) 2h/cone_n, -h + (j + 0.5) 2h/cone_n);
+ *     the cone intensity is multi + Re(cone);
+ *   pol_vs_scatt[(s*4 + ch)*(NMC_EF_MAX_ORDER+1) + n]: XX, XY, YX, YY
+ *     intensity escaping after n scatterings (n capped);
+ *   maps[(s*NMC_EF_MAPS + m)*map_n*map_n + ...];
+ *   raman_depth[s*depth_bins + b]: weight converted at depth b*dz. */
+nmc_status nmc_efield_run(int32_t device, const nmc_efield_config* cfg, const float* S_primary,
+                          const float* S_raman, const nmc_efield_setting* settings, int32_t n_settings,
+                          double* out, float* cone, double* pol_vs_scatt, float* maps, double* raman_depth);
+
 /* -------------------------------------------------------------- autotune */
 /* One launch configuration the autotuner timed. */
 typedef struct nmc_tune_entry {

@@ -147,6 +147,31 @@ class Ext(C.Structure):
     ]
 
 
+class EfieldConfig(C.Structure):
+    """nmc_efield_config."""
+
+    _fields_ = [("mua", C.c_float), ("mus", C.c_float), ("wavelength_cm", C.c_float),
+                ("raman_mua", C.c_float), ("raman_mus", C.c_float), ("raman_wavelength_cm", C.c_float),
+                ("mu_raman", C.c_float), ("n_medium", C.c_float), ("n_outside", C.c_float),
+                ("n_angles", C.c_int32), ("cone_n", C.c_int32), ("cone_half_angle", C.c_float),
+                ("sep_n", C.c_int32), ("sep_half_width", C.c_float), ("map_n", C.c_int32), ("map_dx", C.c_float),
+                ("depth_bins", C.c_int32), ("depth_dz", C.c_float), ("seed", C.c_uint64), ("flags", C.c_uint32),
+                ("pad", C.c_uint32)]
+
+
+class EfieldSetting(C.Structure):
+    """nmc_efield_setting."""
+
+    _fields_ = [("pol_angle", C.c_float), ("theta_in", C.c_float), ("phi_in", C.c_float), ("pad", C.c_uint32),
+                ("photons", C.c_uint64)]
+
+
+EF_FIELDS = ("photons", "specular", "Rd", "Rd2", "co", "cross", "multi_co", "multi_cross", "interf_co",
+             "interf_cross", "sep_outside", "raman_n", "raman_Rd", "raman_co", "raman_cross", "scatters")
+EF_MAPS = ("XX", "XY", "YX", "YY", "Rd", "Det", "Phase0", "Phase1", "Phase2", "Phase3")
+EF_MAX_ORDER = 150
+
+
 class TuneEntry(C.Structure):
     """nmc_tune_entry."""
 

@@ -18,7 +18,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libnmc_gb300.so")
-SOURCES = ["mcxyz.cu", "mcxyz_voxel.cu", "mcxyz_sweep.cu", "mcsub.cu", "sweep.cu", "runtime.cu", "params.cu", "probe.cu", "noalloc.cu"]
+SOURCES = ["mcxyz.cu", "mcxyz_voxel.cu", "mcxyz_sweep.cu", "efield.cu", "mie.cu", "mcsub.cu", "sweep.cu", "runtime.cu", "params.cu", "probe.cu", "noalloc.cu"]
 HEADERS = ["nmc_device.cuh", "engine.h", "mcxyz_kernel.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

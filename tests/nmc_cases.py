@@ -210,3 +210,41 @@ def skin_vessel_spectral_tables(n_wavelengths: int = 351, seed: int = 2024, budg
             g=[1.0, g_eff, g_eff, g_eff],
             **{k: [v] * 4 for k, v in TT_SWEEP.items()}))
     return lam, tables, budgets
+
+
+def cbs_case(n_settings: int = 8, photons: int = 12_500_000, cone_n: int = 256, cone_half_angle: float = 5e-3,
+             sep_n: int = 1024, sep_half_width: float = 0.512, mu_raman: float = 1e-4, seed: int = 5):
+    """Polarised E-field / CBS / Raman case: monodisperse spheres a = 0.5 um,
+    n 1.59 in water (1.33), lambda 633 nm, number density for mus = 100 /cm,
+    mua 0.01 /cm; semi-infinite slab under air; Mie S1, S2 on 1801 angles;
+    Raman conversion at mu_raman to 700 nm (the same spheres' table at 700 nm,
+    density unchanged, mua 0.01); backscattering cone on cone_n^2 angles
+    within +-cone_half_angle; settings: linear polarisation at 0, 45, 90,
+    135 degrees, each at normal incidence and at 10 degrees (n_settings of
+    them, photons each).  Returns (config, S_633, S_700, settings)."""
+    from nmc_gb300 import efield
+
+    m633 = efield.sphere_suspension(0.5, 1.59, 1.33, 633.0, 100.0)
+    x700 = 2 * math.pi * 1.33 * 0.5 / 0.700
+    m700 = efield.mie(x700, complex(1.59 / 1.33, 0.0), 1801)
+    mus700 = m633["number_density"] * m700["q_sca"] * math.pi * (0.5e-4) ** 2
+    cfg = abi.EfieldConfig(mua=0.01, mus=100.0, wavelength_cm=633e-7, raman_mua=0.01, raman_mus=mus700,
+                           raman_wavelength_cm=700e-7, mu_raman=mu_raman, n_medium=1.33, n_outside=1.0,
+                           n_angles=1801, cone_n=cone_n, cone_half_angle=cone_half_angle, sep_n=sep_n,
+                           sep_half_width=sep_half_width, map_n=64, map_dx=0.01, depth_bins=100, depth_dz=0.01,
+                           seed=seed, flags=0, pad=0)
+    settings = []
+    for k in range(n_settings):
+        pol = (k % 4) * math.pi / 4
+        th = 0.0 if k < 4 else math.radians(10.0)
+        settings.append(abi.EfieldSetting(pol_angle=pol, theta_in=th, phi_in=0.0, pad=0, photons=photons))
+    return cfg, m633["table"], m700["table"], settings
+
+
+def hg_amplitude_table(g: float, n_angles: int = 1801) -> np.ndarray:
+    """S1 = S2 = sqrt(p_HG(theta)), real: a scatterer whose unpolarised phase
+    function is Henyey-Greenstein (the scalar limit of the E-field kernel)."""
+    th = np.linspace(0.0, math.pi, n_angles)
+    p = (1 - g * g) / (1 + g * g - 2 * g * np.cos(th)) ** 1.5
+    a = np.sqrt(p).astype(np.float32)
+    return np.stack([a, np.zeros_like(a), a, np.zeros_like(a)], axis=1)
