@@ -18,6 +18,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libnmc_gb300.so")
+CLI_SRC = os.path.join(HERE, "cli", "nmc.cpp")
+CLI = os.path.join(OUT, "nmc")
 SOURCES = ["mcxyz.cu", "mcxyz_voxel.cu", "mcxyz_sweep.cu", "efield.cu", "mie.cu", "mcsub.cu", "sweep.cu", "runtime.cu", "params.cu", "probe.cu", "noalloc.cu"]
 HEADERS = ["nmc_device.cuh", "engine.h", "mcxyz_kernel.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
@@ -38,7 +40,7 @@ def _stale(lib: str) -> bool:
         return True
     t = os.path.getmtime(lib)
     deps = [os.path.join(CSRC, s) for s in SOURCES + HEADERS] + [os.path.join(ROOT, "include", "nmc_abi.h"),
-                                                              __file__]
+                                                              __file__, CLI_SRC]
     return any(os.path.getmtime(d) > t for d in deps)
 
 
@@ -53,7 +55,7 @@ def _compile(src: str) -> str:
 
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
-    if not force and not _stale(LIB):
+    if not force and not _stale(LIB) and os.path.exists(CLI):
         return LIB
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(_compile, SOURCES))
@@ -63,9 +65,26 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli()
     if verbose:
         print(f"built {LIB}")
     return LIB
+
+
+def build_cli() -> str:
+    """The `nmc` program (host C++ over the C ABI), next to the library."""
+    cxx = "g++" if subprocess.run(["which", "g++"], capture_output=True).returncode == 0 else nvcc()
+    tmp = CLI + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", f"-I{os.path.join(ROOT, 'include')}", CLI_SRC, "-o", tmp, f"-L{OUT}",
+           "-lnmc_gb300", "-Wl,-rpath,$ORIGIN"]
+    if cxx != "g++":
+        cmd = [cxx, "-O2", "-std=c++17", f"-I{os.path.join(ROOT, 'include')}", CLI_SRC, "-o", tmp, f"-L{OUT}",
+               "-lnmc_gb300", "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nmc CLI build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CLI)
+    return CLI
 
 
 if __name__ == "__main__":
