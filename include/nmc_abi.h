@@ -400,7 +400,8 @@ typedef struct nmc_efield_config {
   float depth_dz;             /* cm per bin */
   uint64_t seed;
   uint32_t flags;             /* NMC_FLAG_PRECISE_MATH */
-  uint32_t pad;
+  uint32_t speckle_max;       /* speckle records kept per exit-map pixel (0: none; the
+                                 reference's MAX_SPECKLES_PER_PIXEL is 1000) */
 } nmc_efield_config;
 
 typedef struct nmc_efield_setting {
@@ -432,6 +433,16 @@ enum {
 };
 #define NMC_EF_MAX_ORDER 150 /* PolVsScatt orders 0..150, MAX_SCATT_POL (definitions.h:25) */
 
+/* One detected photon at an exit-map pixel, struct SPECKLE of
+ * definitions.h:220-229 (same fields, same order): Phase = arg of the
+ * co-polarised amplitude, Path = path phase 2 pi n L / lambda (wrapped),
+ * Scatt = arg of the cross-polarised amplitude, Total = Phase + Path
+ * (wrapped), XX / XY = intensity of an x-polarised input in the x / y
+ * analyser, Ryx = the photon's weight. */
+typedef struct nmc_speckle {
+  float Phase, Path, Scatt, Total, XX, XY, Ryx;
+} nmc_speckle;
+
 /* Runs every setting's photons in one persistent launch on `device`.
  * S_primary / S_raman: n_angles x 4 Mie tables at the two wavelengths.
  * Outputs (any but `out` may be NULL), per setting s:
@@ -446,7 +457,25 @@ enum {
  *   raman_depth[s*depth_bins + b]: weight converted at depth b*dz. */
 nmc_status nmc_efield_run(int32_t device, const nmc_efield_config* cfg, const float* S_primary,
                           const float* S_raman, const nmc_efield_setting* settings, int32_t n_settings,
-                          double* out, float* cone, double* pol_vs_scatt, float* maps, double* raman_depth);
+                          double* out, float* cone, double* pol_vs_scatt, float* maps, double* raman_depth,
+                          nmc_speckle* speckles, int32_t* speckle_counts);
+/* (speckles: with speckle_max > 0 and maps, records of the first
+ * speckle_max photons reaching each pixel, at
+ * ((s*speckle_max + k)*map_n + ix)*map_n + iy; speckle_counts[s*map_n^2 +
+ * ix*map_n + iy] how many; both may be NULL.) */
+
+/* The reference's speckle mutual-interference post-processing
+ * (MetalMC.m:628-742) on the GPU: for each pixel of an nx x ny map, the
+ * pixel's mean (from the accumulated maps and photon counts) interferes with
+ * each of its `counts[p]` speckle records (records[k*nx*ny + p], p = ix*ny +
+ * iy, k < max_records) with the path-difference coherence envelope
+ * exp(-((path_k - path_mean) lambda / (2 pi lc))^2) (0 when lc <= 0.01);
+ * the mutual sums are added (+=) to out_maps (NMC_EF_MAPS maps of nx*ny,
+ * XX, XY, Rd, Det and Phase0-3 updated as the reference updates them).
+ * `maps` holds the accumulated maps in the same layout.  Host pointers. */
+nmc_status nmc_speckle_mutual(int32_t device, int32_t nx, int32_t ny, const float* maps,
+                              const nmc_speckle* records, const int32_t* counts, int32_t max_records,
+                              float lambda, float lc, float* out_maps);
 
 /* -------------------------------------------------------------- autotune */
 /* One launch configuration the autotuner timed. */

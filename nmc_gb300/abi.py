@@ -156,7 +156,7 @@ class EfieldConfig(C.Structure):
                 ("n_angles", C.c_int32), ("cone_n", C.c_int32), ("cone_half_angle", C.c_float),
                 ("sep_n", C.c_int32), ("sep_half_width", C.c_float), ("map_n", C.c_int32), ("map_dx", C.c_float),
                 ("depth_bins", C.c_int32), ("depth_dz", C.c_float), ("seed", C.c_uint64), ("flags", C.c_uint32),
-                ("pad", C.c_uint32)]
+                ("speckle_max", C.c_uint32)]
 
 
 class EfieldSetting(C.Structure):
@@ -170,6 +170,9 @@ EF_FIELDS = ("photons", "specular", "Rd", "Rd2", "co", "cross", "multi_co", "mul
              "interf_cross", "sep_outside", "raman_n", "raman_Rd", "raman_co", "raman_cross", "scatters")
 EF_MAPS = ("XX", "XY", "YX", "YY", "Rd", "Det", "Phase0", "Phase1", "Phase2", "Phase3")
 EF_MAX_ORDER = 150
+# struct SPECKLE (definitions.h:220-229) / nmc_speckle
+SPECKLE_DTYPE = np.dtype([("Phase", "<f4"), ("Path", "<f4"), ("Scatt", "<f4"), ("Total", "<f4"), ("XX", "<f4"),
+                          ("XY", "<f4"), ("Ryx", "<f4")])
 
 
 class TuneEntry(C.Structure):

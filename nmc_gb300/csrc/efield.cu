@@ -107,6 +107,9 @@ struct EfParams {
   unsigned long long* work;
   unsigned int* flags;
   uint32_t step_cap;
+  nmc_speckle* spk;  // nsets * spk_max * map_n^2 records, or null
+  int* spk_count;    // nsets * map_n^2 arrivals
+  uint32_t spk_max;
 };
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
@@ -410,6 +413,13 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
         atomicAdd(m + NMC_EF_MAP_PHASE1 * (size_t)MN, wrap_pi(ph_path));
         atomicAdd(m + NMC_EF_MAP_PHASE2 * (size_t)MN, a_cr);
         atomicAdd(m + NMC_EF_MAP_PHASE3 * (size_t)MN, wrap_pi(a_co + ph_path));
+        if (P.spk) {  // the pixel's speckle record (struct SPECKLE, definitions.h:220-229)
+          const size_t pix = (size_t)ix * P.map_n + iy;
+          const int k = atomicAdd(P.spk_count + (size_t)set * MN + pix, 1);
+          if (k < (int)P.spk_max)
+            P.spk[((size_t)set * P.spk_max + k) * MN + pix] =
+                nmc_speckle{a_co, wrap_pi(ph_path), a_cr, wrap_pi(a_co + ph_path), Ixx, Ixy, w};
+        }
       }
     }
   }
@@ -461,6 +471,66 @@ __global__ void cgemm_kernel(const float2* __restrict__ A, const float2* __restr
   if (row < Mr && col < N) C[(size_t)row * N + col] = acc;
 }
 
+// ---- the reference's speckle mutual interference (MetalMC.m:628-742), one
+// thread per pixel, its records in order.  The variable types follow the
+// reference: float quantities, double sin / cos / atan2 / exp / sqrt of
+// them (C's math functions of float arguments) and double constants.
+__device__ __forceinline__ float keep_finite(float v) { return isfinite(v) ? v : 0.0f; }
+__device__ __forceinline__ float wrap_ref(float a) { return (float)atan2(sin((double)a), cos((double)a)); }
+
+__global__ void speckle_mutual_kernel(int npix, const float* __restrict__ maps, const nmc_speckle* __restrict__ rec,
+                                      const int* __restrict__ counts, int kmax, float lambda, float lc,
+                                      float* __restrict__ out) {
+  const double two = 2.0, pi_ref = 3.1415926;  // MC_TWO, PI (definitions.h:60,77)
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+    const float xx_t = maps[NMC_EF_MAP_XX * (size_t)npix + p], xy_t = maps[NMC_EF_MAP_XY * (size_t)npix + p];
+    const float norm = xx_t + xy_t;
+    const float ndet = maps[NMC_EF_MAP_DET * (size_t)npix + p];
+    const float xx_a = keep_finite(norm > 0.0f ? xx_t / norm : 0.0f);
+    const float xy_a = keep_finite(norm > 0.0f ? xy_t / norm : 0.0f);
+    const float ryx_a = keep_finite(maps[NMC_EF_MAP_RD * (size_t)npix + p] / ndet);
+    const float ph_a = keep_finite(maps[NMC_EF_MAP_PHASE0 * (size_t)npix + p] / ndet);
+    const float path_a = keep_finite(maps[NMC_EF_MAP_PHASE1 * (size_t)npix + p] / ndet);
+    const float sc_a = keep_finite(maps[NMC_EF_MAP_PHASE2 * (size_t)npix + p] / ndet);
+    const float tot_a = keep_finite(maps[NMC_EF_MAP_PHASE3 * (size_t)npix + p] / ndet);
+    float xx_m = xx_a, xy_m = xy_a, ryx_m = ryx_a, ph_m = ph_a, path_m = path_a, sc_m = sc_a, tot_m = tot_a;
+    float n_times = 1.0f;
+    const float path_a_mm = (float)((double)(path_a * lambda) / (two * pi_ref));
+    const int K = min(counts[p], kmax);
+    for (int k = 0; k < K; ++k) {
+      const nmc_speckle r = rec[(size_t)k * npix + p];
+      const float nc = r.XX + r.XY;
+      const float xx_c = keep_finite(nc > 0.0f ? r.XX / nc : 0.0f);
+      const float xy_c = keep_finite(nc > 0.0f ? r.XY / nc : 0.0f);
+      const float ryx_c = keep_finite(r.Ryx);
+      const float ph_c = keep_finite(r.Phase), path_c = keep_finite(r.Path), sc_c = keep_finite(r.Scatt);
+      const float d_path = wrap_ref(path_a - path_c), d_sc = wrap_ref(sc_a - sc_c);
+      const float diff_lin = wrap_ref(d_path + d_sc);
+      const float interf = (float)sin((double)diff_lin);
+      const float path_c_mm = (float)((double)(path_c * lambda) / (two * pi_ref));
+      const float dp = (path_c_mm - path_a_mm) / lc;
+      float env = (float)exp((double)(-dp * dp));
+      env = (!isfinite(env) || lc <= 0.01f) ? 0.0f : env;
+      xx_m += (float)(((double)(xx_a + xx_c) + two * sqrt((double)(xx_a * xx_c)) * interf * env) / 4.0f);
+      xy_m += (float)(((double)(xy_a + xy_c) + two * sqrt((double)(xy_a * xy_c)) * interf * env) / 4.0f);
+      ryx_m += (float)(((double)(ryx_a + ryx_c) + two * sqrt((double)(ryx_a * ryx_c)) * interf * env) / 4.0f);
+      ph_m += ph_c;
+      path_m += path_c;
+      sc_m += sc_c;
+      tot_m += wrap_ref(ph_c + path_c + sc_c);
+      n_times += 1.0f;
+    }
+    out[NMC_EF_MAP_RD * (size_t)npix + p] += ryx_m;
+    out[NMC_EF_MAP_DET * (size_t)npix + p] += n_times;
+    out[NMC_EF_MAP_XX * (size_t)npix + p] += xx_m;
+    out[NMC_EF_MAP_XY * (size_t)npix + p] += xy_m;
+    out[NMC_EF_MAP_PHASE0 * (size_t)npix + p] += ph_m;
+    out[NMC_EF_MAP_PHASE1 * (size_t)npix + p] += path_m;
+    out[NMC_EF_MAP_PHASE2 * (size_t)npix + p] += sc_m;
+    out[NMC_EF_MAP_PHASE3 * (size_t)npix + p] += tot_m;
+  }
+}
+
 cudaError_t cgemm(const float2* A, const float2* B, float2* C, int Mr, int N, int K, bool tb, cudaStream_t st) {
   const dim3 blk(16, 16), grd((N + 15) / 16, (Mr + 15) / 16);
   if (tb)
@@ -508,7 +578,7 @@ bool build_cdf(const float* S, int n, std::vector<float>& cdf) {
 extern "C" nmc_status nmc_efield_run(int32_t device, const nmc_efield_config* cfg, const float* S_primary,
                                      const float* S_raman, const nmc_efield_setting* settings, int32_t n_settings,
                                      double* out, float* cone, double* pol_vs_scatt, float* maps,
-                                     double* raman_depth) {
+                                     double* raman_depth, nmc_speckle* speckles, int32_t* speckle_counts) {
   using namespace nmc;
   if (!cfg || !S_primary || !settings || !out) return NMC_EINVAL;
   const nmc_efield_config& c = *cfg;
@@ -619,8 +689,12 @@ extern "C" nmc_status nmc_efield_run(int32_t device, const nmc_efield_config* cf
   double* dpvs = pol_vs_scatt ? (double*)dalloc(sizeof(double) * 4 * (NMC_EF_MAX_ORDER + 1) * ns) : nullptr;
   float* dmaps = maps ? (float*)dalloc(sizeof(float) * NMC_EF_MAPS * MN * ns) : nullptr;
   double* ddepth = raman_depth ? (double*)dalloc(sizeof(double) * c.depth_bins * ns) : nullptr;
+  const bool spk = maps && c.speckle_max > 0 && (speckles || speckle_counts);
+  if (spk && c.speckle_max > 100000u) return done(NMC_EINVAL);
+  nmc_speckle* dspk = spk ? (nmc_speckle*)dalloc(sizeof(nmc_speckle) * c.speckle_max * MN * ns) : nullptr;
+  int* dspkc = spk ? (int*)dalloc(sizeof(int) * MN * ns) : nullptr;
   if (!dS0 || !dS1 || !dcdf || !dsets || !dpre || !dsums || !dwork || (cone && !dsep) ||
-      (pol_vs_scatt && !dpvs) || (maps && !dmaps) || (raman_depth && !ddepth))
+      (pol_vs_scatt && !dpvs) || (maps && !dmaps) || (raman_depth && !ddepth) || (spk && (!dspk || !dspkc)))
     return done(NMC_ENOMEM);
   if (cudaMemcpyAsync(dS0, S_primary, sizeof(float4) * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(dS1, raman ? S_raman : S_primary, sizeof(float4) * n, cudaMemcpyHostToDevice, st) !=
@@ -672,6 +746,9 @@ extern "C" nmc_status nmc_efield_run(int32_t device, const nmc_efield_config* cf
   P.work = dwork;
   P.flags = (unsigned int*)(dwork + 1);
   P.step_cap = 20000000u;
+  P.spk = dspk;
+  P.spk_count = dspkc;
+  P.spk_max = spk ? c.speckle_max : 0u;
 
   const bool fast = !(c.flags & NMC_FLAG_PRECISE_MATH);
   const void* f = fast ? (const void*)efield_kernel<true> : (const void*)efield_kernel<false>;
@@ -716,8 +793,58 @@ extern "C" nmc_status nmc_efield_run(int32_t device, const nmc_efield_config* cf
       (raman_depth && cudaMemcpyAsync(raman_depth, ddepth, sizeof(double) * c.depth_bins * ns,
                                       cudaMemcpyDeviceToHost, st) != cudaSuccess))
     return done(NMC_EDEVICE);
+  if (spk && ((speckles && cudaMemcpyAsync(speckles, dspk, sizeof(nmc_speckle) * c.speckle_max * MN * ns,
+                                           cudaMemcpyDeviceToHost, st) != cudaSuccess) ||
+              (speckle_counts &&
+               cudaMemcpyAsync(speckle_counts, dspkc, sizeof(int) * MN * ns, cudaMemcpyDeviceToHost, st) !=
+                   cudaSuccess)))
+    return done(NMC_EDEVICE);
   unsigned int flags = 0;
   cudaMemcpyAsync(&flags, P.flags, sizeof flags, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return done(NMC_EDEVICE);
+  if (spk && speckle_counts)  // arrivals -> records kept
+    for (size_t k = 0; k < MN * ns; ++k) speckle_counts[k] = std::min<int32_t>(speckle_counts[k], (int32_t)c.speckle_max);
   return done((flags & NMC_DEVFLAG_STEPCAP) ? NMC_ESTEPCAP : NMC_OK);
+}
+
+extern "C" nmc_status nmc_speckle_mutual(int32_t device, int32_t nx, int32_t ny, const float* maps,
+                                         const nmc_speckle* records, const int32_t* counts, int32_t max_records,
+                                         float lambda, float lc, float* out_maps) {
+  using namespace nmc;
+  if (!maps || !counts || !out_maps || (max_records > 0 && !records)) return NMC_EINVAL;
+  if (nx < 1 || ny < 1 || (size_t)nx * ny > (1u << 24) || max_records < 0 || max_records > 100000 ||
+      !std::isfinite(lambda) || !std::isfinite(lc))
+    return NMC_EINVAL;
+  const size_t np = (size_t)nx * ny, nm = (size_t)NMC_EF_MAPS * np, nr = (size_t)max_records * np;
+  if (cudaSetDevice(device) != cudaSuccess) return NMC_EDEVICE;
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return NMC_EDEVICE;
+  float *dm = nullptr, *dout = nullptr;
+  nmc_speckle* dr = nullptr;
+  int* dc = nullptr;
+  auto done = [&](nmc_status s) {
+    cudaStreamSynchronize(st);
+    cudaFree(dm);
+    cudaFree(dout);
+    cudaFree(dr);
+    cudaFree(dc);
+    cudaStreamDestroy(st);
+    return s;
+  };
+  if (cudaMalloc((void**)&dm, nm * 4) != cudaSuccess || cudaMalloc((void**)&dout, nm * 4) != cudaSuccess ||
+      cudaMalloc((void**)&dc, np * 4) != cudaSuccess ||
+      (nr && cudaMalloc((void**)&dr, nr * sizeof(nmc_speckle)) != cudaSuccess))
+    return done(NMC_ENOMEM);
+  if (cudaMemcpyAsync(dm, maps, nm * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(dout, out_maps, nm * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(dc, counts, np * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      (nr && cudaMemcpyAsync(dr, records, nr * sizeof(nmc_speckle), cudaMemcpyHostToDevice, st) != cudaSuccess))
+    return done(NMC_EDEVICE);
+  const int grid = (int)std::min<size_t>((np + 127) / 128, 65535);
+  speckle_mutual_kernel<<<grid, 128, 0, st>>>((int)np, dm, dr, dc, max_records, lambda, lc, dout);
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpyAsync(out_maps, dout, nm * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return done(NMC_EDEVICE);
+  return done(NMC_OK);
 }

@@ -25,8 +25,11 @@ def _bind():
         L.nmc_mie.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int32, _P, _P, _P, _P]
         L.nmc_mie.restype = C.c_int
         L.nmc_efield_run.argtypes = [C.c_int32, C.POINTER(abi.EfieldConfig), _P, _P, C.POINTER(abi.EfieldSetting),
-                                     C.c_int32, _P, _P, _P, _P, _P]
+                                     C.c_int32, _P, _P, _P, _P, _P, _P, _P]
         L.nmc_efield_run.restype = C.c_int
+        L.nmc_speckle_mutual.argtypes = [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, C.c_int32, C.c_float,
+                                         C.c_float, _P]
+        L.nmc_speckle_mutual.restype = C.c_int
         L._ef_bound = True
     return L
 
@@ -78,8 +81,11 @@ def run(config: abi.EfieldConfig, S_primary, settings, S_raman=None, device: int
     pbuf = np.zeros((n, 4, abi.EF_MAX_ORDER + 1), np.float64) if pol_vs_scatt else None
     mbuf = np.zeros((n, len(abi.EF_MAPS), mn, mn), np.float32) if maps else None
     dbuf = np.zeros((n, config.depth_bins), np.float64) if raman_depth else None
+    spk = maps and config.speckle_max > 0
+    sbuf = np.zeros((n, config.speckle_max, mn, mn), abi.SPECKLE_DTYPE) if spk else None
+    scnt = np.zeros((n, mn, mn), np.int32) if spk else None
     st = L.nmc_efield_run(int(device), C.byref(config), _ptr(S0), _ptr(S1), arr, n, _ptr(out), _ptr(cbuf),
-                          _ptr(pbuf), _ptr(mbuf), _ptr(dbuf))
+                          _ptr(pbuf), _ptr(mbuf), _ptr(dbuf), _ptr(sbuf), _ptr(scnt))
     if st != 0:
         raise NMCError(st, "nmc_efield_run")
     res = {k: out[:, i] for i, k in enumerate(abi.EF_FIELDS)}
@@ -91,4 +97,25 @@ def run(config: abi.EfieldConfig, S_primary, settings, S_raman=None, device: int
         res["maps"] = {k: mbuf[:, i] for i, k in enumerate(abi.EF_MAPS)}
     if raman_depth:
         res["raman_depth"] = dbuf
+    if spk:
+        res["speckles"], res["speckle_counts"] = sbuf, scnt
     return res
+
+
+def speckle_mutual(maps: np.ndarray, records: np.ndarray, counts: np.ndarray, wavelength: float,
+                   coherence_length: float, out: np.ndarray | None = None, device: int = 0) -> np.ndarray:
+    """The reference's speckle mutual-interference post-processing
+    (MetalMC.m:628-742) on the GPU.  maps: (NMC_EF_MAPS, nx, ny) float32 of
+    one setting; records: (kmax, nx, ny) abi.SPECKLE_DTYPE; counts (nx, ny).
+    Returns `out` (zeros if None) with the mutual maps added."""
+    L = _bind()
+    m = np.ascontiguousarray(maps, np.float32)
+    _, nx, ny = m.shape
+    r = np.ascontiguousarray(records, abi.SPECKLE_DTYPE)
+    c = np.ascontiguousarray(counts, np.int32)
+    o = np.zeros_like(m) if out is None else out
+    st = L.nmc_speckle_mutual(int(device), nx, ny, _ptr(m), _ptr(r), _ptr(c), r.shape[0], float(wavelength),
+                              float(coherence_length), _ptr(o))
+    if st != 0:
+        raise NMCError(st, "nmc_speckle_mutual")
+    return o

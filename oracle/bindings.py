@@ -73,6 +73,8 @@ def oracle_lib():
         lib.orc_tt_costheta.argtypes = [C.c_double] * 7
         lib.orc_hg_costheta.restype = C.c_double
         lib.orc_hg_costheta.argtypes = [C.c_double, C.c_double]
+        lib.orc_speckle_mutual.argtypes = [C.c_int, C.c_int, _P, _P, _P, C.c_int, C.c_float, C.c_float, _P]
+        lib.orc_speckle_mutual.restype = None
         _oracle = lib
     return _oracle
 
@@ -221,3 +223,15 @@ def ref_taus(s1, s2, s3, n):
     o = np.zeros(n, np.float32)
     ref_lib().ref_taus_draws(s1, s2, s3, n, _ptr(o))
     return o
+
+
+def speckle_mutual(maps, records, counts, lam, lc, out):
+    """MetalMC.m:628-742 restated: adds the mutual maps into `out` (float32,
+    NMC_EF_MAPS x ny*nx)."""
+    lib = oracle_lib()
+    nmaps, nx, ny = maps.shape
+    kmax = records.shape[0]
+    lib.orc_speckle_mutual(nx, ny, _ptr(np.ascontiguousarray(maps, np.float32)),
+                           _ptr(np.ascontiguousarray(records)), _ptr(np.ascontiguousarray(counts, np.int32)),
+                           kmax, float(lam), float(lc), _ptr(out))
+    return out

@@ -1020,4 +1020,74 @@ double orc_tt_costheta(double gf, double af, double gb, double ab, double cc, do
 
 double orc_hg_costheta(double g, double u) { return hg_costheta<double>(g, u); }
 
+// The speckle mutual-interference post-processing of -[MetalMC
+// getComputeResults:] (MetalMC.m:628-742), restated with the reference's
+// types: float quantities, C's double sin / cos / atan2 / exp / sqrt of them,
+// double constants MC_TWO = 2.0 and PI = 3.1415926 (definitions.h:60,77).
+// The reference's dPhase / phase_total_diff_lg terms feed no output and are
+// left out.  Map layout as nmc_speckle_mutual: NMC_EF_MAPS maps of nx*ny.
+void orc_speckle_mutual(int nx, int ny, const float* maps, const nmc_speckle* rec, const int32_t* counts,
+                        int kmax, float lambda, float lc, float* out) {
+  const size_t np = (size_t)nx * ny;
+  auto fin = [](float v) { return std::isfinite(v) ? v : 0.0f; };
+  auto wrap = [](float a) { return (float)std::atan2(std::sin((double)a), std::cos((double)a)); };
+  const double two = 2.0, pi_ref = 3.1415926;
+  for (size_t p = 0; p < np; ++p) {
+    const float XX_accum_temp = maps[NMC_EF_MAP_XX * np + p];
+    const float XY_accum_temp = maps[NMC_EF_MAP_XY * np + p];
+    const float norm_sum = XX_accum_temp + XY_accum_temp;
+    const float det = maps[NMC_EF_MAP_DET * np + p];
+    const float XX_accum = fin(norm_sum > 0.0f ? XX_accum_temp / norm_sum : 0.0f);
+    const float XY_accum = fin(norm_sum > 0.0f ? XY_accum_temp / norm_sum : 0.0f);
+    const float Ryx_accum = fin(maps[NMC_EF_MAP_RD * np + p] / det);
+    const float Phase_accum = fin(maps[NMC_EF_MAP_PHASE0 * np + p] / det);
+    const float Path_accum = fin(maps[NMC_EF_MAP_PHASE1 * np + p] / det);
+    const float Scatt_accum = fin(maps[NMC_EF_MAP_PHASE2 * np + p] / det);
+    const float Total_accum = fin(maps[NMC_EF_MAP_PHASE3 * np + p] / det);
+    float XX_mutual = XX_accum, XY_mutual = XY_accum, Ryx_mutual = Ryx_accum;
+    float Phase_sum = Phase_accum, Path_sum = Path_accum, Scatt_sum = Scatt_accum, Total_sum = Total_accum;
+    float N_times = 1.0f;
+    const int K = std::min<int>(counts[p], kmax);
+    for (int k = 0; k < K; ++k) {
+      const nmc_speckle& r = rec[(size_t)k * np + p];
+      const float norm_c = r.XX + r.XY;
+      const float XX_current = fin(norm_c > 0.0f ? r.XX / norm_c : 0.0f);
+      const float XY_current = fin(norm_c > 0.0f ? r.XY / norm_c : 0.0f);
+      const float Ryx_current = fin(r.Ryx);
+      const float Phase_current = fin(r.Phase), Path_current = fin(r.Path), Scatt_current = fin(r.Scatt);
+      const float dPath = wrap(Path_accum - Path_current);
+      const float dScatt = wrap(Scatt_accum - Scatt_current);
+      const float diff_linear = wrap(dPath + dScatt);
+      const float interference = (float)std::sin((double)diff_linear);
+      const float path_accum_mm = (float)((double)(Path_accum * lambda) / (two * pi_ref));
+      const float path_current_mm = (float)((double)(Path_current * lambda) / (two * pi_ref));
+      const float delta_path = (path_current_mm - path_accum_mm) / lc;
+      float lc_contribution = (float)std::exp((double)(-delta_path * delta_path));
+      lc_contribution = (!std::isfinite(lc_contribution) || lc <= 0.01f) ? 0.0f : lc_contribution;
+      XX_mutual += (float)(((double)(XX_accum + XX_current) +
+                            two * std::sqrt((double)(XX_accum * XX_current)) * interference * lc_contribution) /
+                           4.0f);
+      XY_mutual += (float)(((double)(XY_accum + XY_current) +
+                            two * std::sqrt((double)(XY_accum * XY_current)) * interference * lc_contribution) /
+                           4.0f);
+      Ryx_mutual += (float)(((double)(Ryx_accum + Ryx_current) +
+                             two * std::sqrt((double)(Ryx_accum * Ryx_current)) * interference * lc_contribution) /
+                            4.0f);
+      Phase_sum += Phase_current;
+      Path_sum += Path_current;
+      Scatt_sum += Scatt_current;
+      Total_sum += wrap(Phase_current + Path_current + Scatt_current);
+      N_times += 1.0f;
+    }
+    out[NMC_EF_MAP_RD * np + p] += Ryx_mutual;
+    out[NMC_EF_MAP_DET * np + p] += N_times;
+    out[NMC_EF_MAP_XX * np + p] += XX_mutual;
+    out[NMC_EF_MAP_XY * np + p] += XY_mutual;
+    out[NMC_EF_MAP_PHASE0 * np + p] += Phase_sum;
+    out[NMC_EF_MAP_PHASE1 * np + p] += Path_sum;
+    out[NMC_EF_MAP_PHASE2 * np + p] += Scatt_sum;
+    out[NMC_EF_MAP_PHASE3 * np + p] += Total_sum;
+  }
+}
+
 }  // extern "C"

@@ -63,6 +63,10 @@ double orc_tt_costheta(double gf, double af, double gb, double ab, double cc,
 /* Henyey-Greenstein cos(theta) sample (kernels.metal:696-703) in double. */
 double orc_hg_costheta(double g, double u);
 
+/* MetalMC.m:628-742 speckle mutual interference (see nmc_speckle_mutual). */
+void orc_speckle_mutual(int nx, int ny, const float* maps, const nmc_speckle* rec, const int32_t* counts,
+                        int kmax, float lambda, float lc, float* out);
+
 #ifdef __cplusplus
 }
 #endif

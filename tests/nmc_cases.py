@@ -232,7 +232,7 @@ def cbs_case(n_settings: int = 8, photons: int = 12_500_000, cone_n: int = 256, 
                            raman_wavelength_cm=700e-7, mu_raman=mu_raman, n_medium=1.33, n_outside=1.0,
                            n_angles=1801, cone_n=cone_n, cone_half_angle=cone_half_angle, sep_n=sep_n,
                            sep_half_width=sep_half_width, map_n=64, map_dx=0.01, depth_bins=100, depth_dz=0.01,
-                           seed=seed, flags=0, pad=0)
+                           seed=seed, flags=0, speckle_max=0)
     settings = []
     for k in range(n_settings):
         pol = (k % 4) * math.pi / 4

@@ -130,3 +130,50 @@ def test_batched_setting_equals_alone(gpu):
     a = efield.run(cfg1, S633, [st1[2]], S_raman=S700)
     for k in ("photons", "Rd", "co", "cross", "scatters", "raman_n"):
         assert a[k][0] == pytest.approx(r[k][2], rel=1e-9, abs=1e-9), k
+
+
+def test_speckle_mutual_matches_oracle(gpu, oracle):
+    # the reference's post-processing (MetalMC.m:628-742) on synthetic maps
+    # and records: GPU kernel against the oracle's restatement
+    from nmc_gb300 import efield
+
+    rng = np.random.default_rng(17)
+    nx, ny, kmax = 24, 20, 40
+    maps = np.zeros((len(abi.EF_MAPS), nx, ny), np.float32)
+    det = rng.integers(0, 60, (nx, ny)).astype(np.float32)
+    maps[abi.EF_MAPS.index("Det")] = det
+    for k in ("XX", "XY", "YX", "YY", "Rd"):
+        maps[abi.EF_MAPS.index(k)] = rng.uniform(0, 1, (nx, ny)) * det
+    for k in ("Phase0", "Phase1", "Phase2", "Phase3"):
+        maps[abi.EF_MAPS.index(k)] = rng.uniform(-math.pi, math.pi, (nx, ny)) * det
+    rec = np.zeros((kmax, nx, ny), abi.SPECKLE_DTYPE)
+    for f in ("Phase", "Path", "Scatt", "Total"):
+        rec[f] = rng.uniform(-math.pi, math.pi, rec.shape)
+    for f in ("XX", "XY", "Ryx"):
+        rec[f] = rng.uniform(0, 0.2, rec.shape)
+    rec["XX"][0, 0, 0] = np.nan  # the reference's sanitising of non-finite values
+    counts = rng.integers(0, kmax + 5, (nx, ny)).astype(np.int32)
+    for lam, lc in ((633e-6, 0.05), (633e-6, 0.005)):  # lc <= 0.01 switches the envelope off
+        base = rng.uniform(0, 1, maps.shape).astype(np.float32)
+        got = efield.speckle_mutual(maps, rec, counts, lam, lc, out=base.copy())
+        want = oracle.speckle_mutual(maps, rec, counts, lam, lc, base.copy().reshape(len(abi.EF_MAPS), -1))
+        np.testing.assert_allclose(got.reshape(want.shape), want, rtol=2e-6, atol=2e-6)
+
+
+def test_efield_speckle_records(gpu):
+    from nmc_gb300 import efield
+
+    cfg, S633, S700, settings = cases.cbs_case(n_settings=1, photons=20_000, cone_n=8, sep_n=8)
+    cfg.speckle_max = 16
+    cfg.map_n, cfg.map_dx = 64, 0.05  # outer pixels see fewer than 16 photons
+    r = efield.run(cfg, S633, settings, S_raman=S700)
+    spk, cnt, maps = r["speckles"][0], r["speckle_counts"][0], r["maps"]
+    assert cnt.max() <= 16 and cnt.sum() > 0
+    det = maps["Det"][0]
+    full = (det < 16) & (det > 0)  # every arrival recorded
+    assert full.any()
+    k = np.arange(16)[:, None, None] < cnt[None]
+    for f, m in (("XX", "XX"), ("XY", "XY"), ("Ryx", "Rd")):
+        s = np.where(k, spk[f], 0).sum(0)
+        np.testing.assert_allclose(s[full], maps[m][0][full], rtol=1e-4)
+    np.testing.assert_array_equal(cnt[full], det[full].astype(np.int32))
