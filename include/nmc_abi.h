@@ -477,6 +477,42 @@ nmc_status nmc_speckle_mutual(int32_t device, int32_t nx, int32_t ny, const floa
                               const nmc_speckle* records, const int32_t* counts, int32_t max_records,
                               float lambda, float lc, float* out_maps);
 
+/* ------------------------------------------------------ layered mcsub */
+/* A stack of plane layers (MAXLAYERS = 100, definitions.h:24, declared by
+ * the reference but unused): the mcsub kernel's hop / drop / spin /
+ * roulette per layer, Fresnel reflection or Snell refraction at every
+ * boundary, escape into the ambient media above (Rd) and below (Tt).
+ * thickness is in cm; the last layer may be semi-infinite (INFINITY), then
+ * it needs mua + mus > 0.  Normal pencil beam at the origin. */
+typedef struct nmc_layer {
+  float mua, mus, g, n, thickness;
+} nmc_layer;
+
+typedef struct nmc_layered_config {
+  int32_t n_layers;            /* 1..100 */
+  float n_above, n_below;      /* ambient refractive indices */
+  int32_t nr;                  /* Rd(r), Tt(r), A(r,z): nr bins of dr + one overflow bin */
+  float dr;
+  int32_t nz;                  /* A(z): nz bins of dz + one overflow bin */
+  float dz;
+  uint32_t flags;              /* NMC_FLAG_PRECISE_MATH */
+  uint64_t seed;
+} nmc_layered_config;
+
+/* Per-run sums of nmc_layered_run (weights, not yet divided by photons). */
+enum {
+  NMC_LAY_PHOTONS = 0, NMC_LAY_SPECULAR, NMC_LAY_RD, NMC_LAY_RD2, NMC_LAY_TT, NMC_LAY_TT2, NMC_LAY_A,
+  NMC_LAY_INTERACTIONS, NMC_LAY_FIELDS
+};
+
+/* Photons [first, first + photons) through the stack on `device`; out holds
+ * NMC_LAY_FIELDS doubles; rd_r, tt_r (nr+1), a_z (nz+1), a_rz ((nr+1)*(nz+1),
+ * index ir*(nz+1) + iz) and a_layer (n_layers) are added to (+=) and may be
+ * NULL.  Host pointers. */
+nmc_status nmc_layered_run(int32_t device, const nmc_layered_config* cfg, const nmc_layer* layers,
+                           uint64_t first, uint64_t photons, double* out, double* rd_r, double* tt_r,
+                           double* a_z, double* a_rz, double* a_layer);
+
 /* -------------------------------------------------------------- autotune */
 /* One launch configuration the autotuner timed. */
 typedef struct nmc_tune_entry {

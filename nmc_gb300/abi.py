@@ -175,6 +175,22 @@ SPECKLE_DTYPE = np.dtype([("Phase", "<f4"), ("Path", "<f4"), ("Scatt", "<f4"), (
                           ("XY", "<f4"), ("Ryx", "<f4")])
 
 
+class Layer(C.Structure):
+    """nmc_layer."""
+
+    _fields_ = [("mua", C.c_float), ("mus", C.c_float), ("g", C.c_float), ("n", C.c_float), ("thickness", C.c_float)]
+
+
+class LayeredConfig(C.Structure):
+    """nmc_layered_config."""
+
+    _fields_ = [("n_layers", C.c_int32), ("n_above", C.c_float), ("n_below", C.c_float), ("nr", C.c_int32),
+                ("dr", C.c_float), ("nz", C.c_int32), ("dz", C.c_float), ("flags", C.c_uint32), ("seed", C.c_uint64)]
+
+
+LAY_FIELDS = ("photons", "specular", "Rd", "Rd2", "Tt", "Tt2", "A", "interactions")
+
+
 class TuneEntry(C.Structure):
     """nmc_tune_entry."""
 

@@ -20,7 +20,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libnmc_gb300.so")
 CLI_SRC = os.path.join(HERE, "cli", "nmc.cpp")
 CLI = os.path.join(OUT, "nmc")
-SOURCES = ["mcxyz.cu", "mcxyz_voxel.cu", "mcxyz_sweep.cu", "efield.cu", "mie.cu", "mcsub.cu", "sweep.cu", "runtime.cu", "params.cu", "probe.cu", "noalloc.cu"]
+SOURCES = ["mcxyz.cu", "mcxyz_voxel.cu", "mcxyz_sweep.cu", "efield.cu", "mie.cu", "layered.cu", "mcsub.cu", "sweep.cu", "runtime.cu", "params.cu", "probe.cu", "noalloc.cu"]
 HEADERS = ["nmc_device.cuh", "engine.h", "mcxyz_kernel.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -1,0 +1,302 @@
+// layered.cu - multi-layer extension of the mcsub kernel: a stack of plane
+// layers, each with its own mua, mus, HG g, refractive index and thickness
+// (the last may be semi-infinite), between an ambient medium above and one
+// below.  The reference declares MAXLAYERS = 100 (definitions.h:24) but its
+// mcsub kernel (kernels.metal:59-319) has one semi-infinite layer; this
+// kernel keeps that kernel's physics per layer:
+//   HOP    s = -ln(xi) / mu_t of the current layer; a step that reaches a
+//          layer boundary stops there and the rest of the dimensionless
+//          step carries into the next layer (scaled by its mu_t);
+//   CROSS  at a boundary the photon reflects with the unpolarised Fresnel
+//          probability R(n_i, n_t, |uz|) (helpers.metal:243-291) by a random
+//          draw, as the mcsub kernel does at its surface (kernels.metal:
+//          183-214); otherwise it refracts (Snell) into the next layer, or
+//          escapes into the ambient medium (Rd(r) above, Tt(r) below);
+//   DROP   absorb = W mua / mu_t at each interaction (kernels.metal:224-234),
+//          tallied in A(z), A(r, z) and per layer;
+//   SPIN   Henyey-Greenstein with the layer's g (the reference's mcsub
+//          kernel samples isotropically, kernels.metal:252; this kernel uses
+//          the g it is given);
+//   ROULETTE below 1e-4, chance 0.1 (kernels.metal:289-294).
+// A launch is a normal pencil beam at the origin; the specular reflection
+// at the top surface leaves W0 = 1 - R_sp.  Random numbers: Philox4x32-10,
+// key (seed lo, seed hi), counter (photon lo, photon hi, interaction,
+// 'LAYR'): x step, y cos theta, z psi, w roulette; boundary events draw their
+// Fresnel choice from counter (photon lo, photon hi, event | 2^31, 'LAYR').
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "engine.h"
+#include "nmc_abi.h"
+
+namespace nmc {
+namespace {
+
+constexpr uint32_t kLayTag = 0x4C415952u;
+constexpr int kMaxLayers = 100;  // MAXLAYERS, definitions.h:24
+
+struct LayDev {
+  float mua, mus, inv_mut, n, z0, z1;  // z1 = +inf for a semi-infinite last layer
+  PhaseConst ph;
+};
+
+struct LayParams {
+  const LayDev* lay;
+  int nl;
+  float n_above, n_below, w0;
+  int nr, nz;
+  float idr, idz;
+  unsigned long long* rd_r;  // nr + 1 (last = overflow), u64 fixed point
+  unsigned long long* tt_r;  // nr + 1
+  unsigned long long* a_z;   // nz + 1
+  unsigned long long* a_rz;  // (nr + 1) * (nz + 1), or null
+  unsigned long long* a_layer;  // nl
+  double* sums;  // NMC_LAY_FIELDS
+  unsigned long long first, n;
+  uint32_t k0, k1;
+  unsigned long long* work;
+  unsigned int* flags;
+  uint32_t step_cap;
+};
+
+template <bool FAST>
+__global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
+  using M = Math<FAST>;
+  __shared__ LayDev s_lay[kMaxLayers];
+  __shared__ double s_sum[NMC_LAY_FIELDS];
+  for (int i = threadIdx.x; i < P.nl; i += blockDim.x) s_lay[i] = P.lay[i];
+  if (threadIdx.x < NMC_LAY_FIELDS) s_sum[threadIdx.x] = 0.0;
+  __syncthreads();
+  while (true) {
+    const unsigned long long g = next_photon(P.work);
+    if (g >= P.n) break;
+    const unsigned long long pid = P.first + g;
+    const uint32_t c0 = (uint32_t)pid, c1 = (uint32_t)(pid >> 32);
+    float x = 0.f, y = 0.f, z = 0.f, ux = 0.f, uy = 0.f, uz = 1.f, w = P.w0, sleft = 0.f;
+    int L = 0;
+    uint32_t hop = 0, ev = 0;
+    bool alive = true;
+    float rd = 0.f, tt = 0.f;
+    uint4 r = philox4x32_10(make_uint4(c0, c1, 0u, kLayTag), P.k0, P.k1);
+    while (alive) {
+      const LayDev& Ly = s_lay[L];
+      if (sleft <= 0.f) sleft = M::neglog(u01(r.x));
+      // distance to the layer boundary ahead
+      const float db = uz > 0.f ? (Ly.z1 - z) / uz : (uz < 0.f ? (Ly.z0 - z) / uz : INFINITY);
+      const float s = Ly.inv_mut > 0.f ? sleft * Ly.inv_mut : INFINITY;
+      if (s >= db) {  // reaches the boundary: CROSS
+        x = fmaf(db, ux, x);
+        y = fmaf(db, uy, y);
+        z = uz > 0.f ? Ly.z1 : Ly.z0;
+        sleft = Ly.inv_mut > 0.f ? fmaxf(sleft - db / Ly.inv_mut, 0.f) : sleft;
+        const bool down = uz > 0.f;
+        const int Ln = down ? L + 1 : L - 1;
+        const float nt = Ln < 0 ? P.n_above : (Ln >= P.nl ? P.n_below : s_lay[Ln].n);
+        float uzt = 0.f;
+        const float R = rfresnel(Ly.n, nt, fabsf(uz), &uzt);
+        const uint4 a = philox4x32_10(make_uint4(c0, c1, ev | 0x80000000u, kLayTag), P.k0, P.k1);
+        ++ev;
+        if (u01(a.x) <= R) {
+          uz = -uz;  // reflected
+        } else if (Ln < 0 || Ln >= P.nl) {  // escapes
+          const float rr = sqrtf(x * x + y * y);
+          const int ir = min((int)(rr * P.idr), P.nr);
+          if (Ln < 0) {
+            atomicAdd(P.rd_r + ir, to_fix(w));
+            rd += w;
+          } else {
+            atomicAdd(P.tt_r + ir, to_fix(w));
+            tt += w;
+          }
+          alive = false;
+        } else {  // refracted into the next layer (Snell)
+          const float ratio = Ly.n / nt;
+          ux *= ratio;
+          uy *= ratio;
+          uz = down ? uzt : -uzt;
+          L = Ln;
+        }
+        if (ev > P.step_cap) {
+          atomicOr(P.flags, (unsigned int)NMC_DEVFLAG_STEPCAP);
+          alive = false;
+        }
+        continue;
+      }
+      // interaction inside the layer: HOP, DROP, SPIN, ROULETTE
+      x = fmaf(s, ux, x);
+      y = fmaf(s, uy, y);
+      z = fmaf(s, uz, z);
+      sleft = 0.f;
+      const float absorb = w * Ly.mua * Ly.inv_mut;
+      w -= absorb;
+      if (absorb > 0.f) {
+        const unsigned long long fa = to_fix(absorb);
+        const int iz = min(max((int)(z * P.idz), 0), P.nz);
+        atomicAdd(P.a_z + iz, fa);
+        atomicAdd(P.a_layer + L, fa);
+        if (P.a_rz) {
+          const int ir = min((int)(sqrtf(x * x + y * y) * P.idr), P.nr);
+          atomicAdd(P.a_rz + (size_t)ir * (P.nz + 1) + iz, fa);
+        }
+      }
+      spin<FAST>(hg_sample<FAST>(Ly.ph, u01(r.y)), u01(r.z), ux, uy, uz);
+      if (w < kTHRESHOLD) {
+        if (u01(r.w) <= kCHANCE)
+          w /= kCHANCE;
+        else
+          alive = false;
+      }
+      ++hop;
+      if (hop > P.step_cap) {
+        atomicOr(P.flags, (unsigned int)NMC_DEVFLAG_STEPCAP);
+        alive = false;
+      }
+      r = philox4x32_10(make_uint4(c0, c1, hop, kLayTag), P.k0, P.k1);
+    }
+    atomicAdd(&s_sum[NMC_LAY_PHOTONS], 1.0);
+    atomicAdd(&s_sum[NMC_LAY_RD], (double)rd);
+    atomicAdd(&s_sum[NMC_LAY_RD2], (double)rd * (double)rd);
+    atomicAdd(&s_sum[NMC_LAY_TT], (double)tt);
+    atomicAdd(&s_sum[NMC_LAY_TT2], (double)tt * (double)tt);
+    atomicAdd(&s_sum[NMC_LAY_INTERACTIONS], (double)hop);
+  }
+  __syncthreads();
+  if (threadIdx.x < NMC_LAY_FIELDS && s_sum[threadIdx.x] != 0.0) atomicAdd(P.sums + threadIdx.x, s_sum[threadIdx.x]);
+}
+
+double host_fresnel_normal(double n1, double n2) {
+  const double r = (n1 - n2) / (n1 + n2);
+  return r * r;
+}
+
+}  // namespace
+}  // namespace nmc
+
+extern "C" nmc_status nmc_layered_run(int32_t device, const nmc_layered_config* cfg, const nmc_layer* layers,
+                                      uint64_t first, uint64_t photons, double* out, double* rd_r, double* tt_r,
+                                      double* a_z, double* a_rz, double* a_layer) {
+  using namespace nmc;
+  if (!cfg || !layers || !out) return NMC_EINVAL;
+  const nmc_layered_config& c = *cfg;
+  if (c.n_layers < 1 || c.n_layers > kMaxLayers || c.nr < 1 || c.nr > 65536 || c.nz < 1 || c.nz > 65536 ||
+      !(c.dr > 0.f) || !(c.dz > 0.f) || !(c.n_above > 0.f) || !(c.n_below > 0.f) || !std::isfinite(c.n_above) ||
+      !std::isfinite(c.n_below))
+    return NMC_EINVAL;
+  std::vector<LayDev> lay(c.n_layers);
+  double z = 0.0;
+  for (int i = 0; i < c.n_layers; ++i) {
+    const nmc_layer& q = layers[i];
+    const bool last = i == c.n_layers - 1;
+    if (!std::isfinite(q.mua) || q.mua < 0.f || !std::isfinite(q.mus) || q.mus < 0.f || !std::isfinite(q.g) ||
+        !(q.g > -1.f) || !(q.g < 1.f) || !(q.n > 0.f) || !std::isfinite(q.n) || !(q.thickness > 0.f) ||
+        (!last && !std::isfinite(q.thickness)) || (!std::isfinite(q.thickness) && !(q.mua + q.mus > 0.f)))
+      return NMC_EINVAL;
+    LayDev& d = lay[i];
+    d.mua = q.mua;
+    d.mus = q.mus;
+    d.inv_mut = q.mua + q.mus > 0.f ? (float)(1.0 / ((double)q.mua + q.mus)) : 0.f;
+    d.n = q.n;
+    d.z0 = (float)z;
+    z += q.thickness;
+    d.z1 = std::isfinite(q.thickness) ? (float)z : INFINITY;
+    nmc_tissue_params tp{};
+    tp.gv[1] = q.g;
+    d.ph = phase_const(tp, 1);
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return NMC_EDEVICE;
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return NMC_EDEVICE;
+  std::vector<void*> allocs;
+  auto dalloc = [&](size_t bytes) -> void* {
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+    allocs.push_back(p);
+    cudaMemsetAsync(p, 0, bytes, st);
+    return p;
+  };
+  auto done = [&](nmc_status s) {
+    cudaStreamSynchronize(st);
+    for (void* p : allocs) cudaFree(p);
+    cudaStreamDestroy(st);
+    return s;
+  };
+  const size_t nr1 = (size_t)c.nr + 1, nz1 = (size_t)c.nz + 1;
+  LayDev* dlay = (LayDev*)dalloc(sizeof(LayDev) * c.n_layers);
+  auto* drd = (unsigned long long*)dalloc(8 * nr1);
+  auto* dtt = (unsigned long long*)dalloc(8 * nr1);
+  auto* daz = (unsigned long long*)dalloc(8 * nz1);
+  auto* darz = a_rz ? (unsigned long long*)dalloc(8 * nr1 * nz1) : nullptr;
+  auto* dal = (unsigned long long*)dalloc(8 * c.n_layers);
+  auto* dsum = (double*)dalloc(sizeof(double) * NMC_LAY_FIELDS);
+  auto* dwork = (unsigned long long*)dalloc(16);
+  if (!dlay || !drd || !dtt || !daz || (a_rz && !darz) || !dal || !dsum || !dwork) return done(NMC_ENOMEM);
+  if (cudaMemcpyAsync(dlay, lay.data(), sizeof(LayDev) * c.n_layers, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return done(NMC_EDEVICE);
+  LayParams P{};
+  P.lay = dlay;
+  P.nl = c.n_layers;
+  P.n_above = c.n_above;
+  P.n_below = c.n_below;
+  const double rsp = host_fresnel_normal(c.n_above, layers[0].n);
+  P.w0 = (float)(1.0 - rsp);
+  P.nr = c.nr;
+  P.nz = c.nz;
+  P.idr = (float)(1.0 / c.dr);
+  P.idz = (float)(1.0 / c.dz);
+  P.rd_r = drd;
+  P.tt_r = dtt;
+  P.a_z = daz;
+  P.a_rz = darz;
+  P.a_layer = dal;
+  P.sums = dsum;
+  P.first = first;
+  P.n = photons;
+  P.k0 = (uint32_t)c.seed;
+  P.k1 = (uint32_t)(c.seed >> 32);
+  P.work = dwork;
+  P.flags = (unsigned int*)(dwork + 1);
+  P.step_cap = 20000000u;
+  const bool fast = !(c.flags & NMC_FLAG_PRECISE_MATH);
+  const void* f = fast ? (const void*)layered_kernel<true> : (const void*)layered_kernel<false>;
+  int per_sm = 0, nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, 256, 0) != cudaSuccess || per_sm < 1)
+    return done(NMC_EDEVICE);
+  const unsigned long long grid =
+      std::max<unsigned long long>(1, std::min<unsigned long long>((unsigned long long)nsm * per_sm,
+                                                                   (photons + 255) / 256));
+  void* args[] = {(void*)&P};
+  if (photons > 0 && cudaLaunchKernel(f, dim3((unsigned)grid), dim3(256), args, 0, st) != cudaSuccess)
+    return done(NMC_EDEVICE);
+  std::vector<unsigned long long> hrd(nr1), htt(nr1), haz(nz1), hal(c.n_layers), harz(a_rz ? nr1 * nz1 : 0);
+  unsigned int flags = 0;
+  if (cudaMemcpyAsync(out, dsum, sizeof(double) * NMC_LAY_FIELDS, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(hrd.data(), drd, 8 * nr1, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(htt.data(), dtt, 8 * nr1, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(haz.data(), daz, 8 * nz1, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(hal.data(), dal, 8 * c.n_layers, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      (a_rz && cudaMemcpyAsync(harz.data(), darz, 8 * nr1 * nz1, cudaMemcpyDeviceToHost, st) != cudaSuccess) ||
+      cudaMemcpyAsync(&flags, P.flags, sizeof flags, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return done(NMC_EDEVICE);
+  out[NMC_LAY_SPECULAR] = rsp * (double)photons;
+  double a_tot = 0.0;
+  for (int i = 0; i < c.n_layers; ++i) {
+    const double v = (double)hal[i] * kUnfix;
+    a_tot += v;
+    if (a_layer) a_layer[i] += v;
+  }
+  out[NMC_LAY_A] = a_tot;
+  for (size_t i = 0; i < nr1; ++i) {
+    if (rd_r) rd_r[i] += (double)hrd[i] * kUnfix;
+    if (tt_r) tt_r[i] += (double)htt[i] * kUnfix;
+  }
+  if (a_z)
+    for (size_t i = 0; i < nz1; ++i) a_z[i] += (double)haz[i] * kUnfix;
+  if (a_rz)
+    for (size_t i = 0; i < nr1 * nz1; ++i) a_rz[i] += (double)harz[i] * kUnfix;
+  return done((flags & NMC_DEVFLAG_STEPCAP) ? NMC_ESTEPCAP : NMC_OK);
+}

@@ -1,0 +1,87 @@
+"""Layered media (layered.cu).  No reference semantics exist for more than
+one layer (MAXLAYERS is declared, definitions.h:24, but unused), so the
+checks are the ones the physics fixes: one semi-infinite layer equals the
+mcsub kernel; a layer split in two equals the whole; a clear absorbing slab
+follows Beer-Lambert; a clear non-absorbing slab follows the Fresnel
+multiple-reflection sums; weight is conserved."""
+import math
+
+import numpy as np
+import pytest
+
+from nmc_gb300 import abi
+import nmc_cases as cases
+
+pytestmark = pytest.mark.gpu
+
+
+def test_single_layer_equals_mcsub(gpu):
+    from nmc_gb300 import layered
+
+    n = 400_000
+    r = layered.run([(1.0, 100.0, 0.9, 1.37, math.inf)], n, n_above=1.0, seed=4)
+    rp, tp, ext = cases.mcsub_case(g=0.9, seed=8)
+    with gpu.Engine(abi.SIM_MCSUB, 0, ext) as e:
+        e.prepare_data(rp, tp)
+        e.run(0, n)
+        sm = e.summary()
+    rd_m = sm["E"] / n
+    se_m = math.sqrt(max(sm["rd_sumsq"] / n - rd_m ** 2, 0) / n)
+    z = (r["rd"] - rd_m) / math.hypot(r["rd_se"], se_m)
+    print(f"Rd layered {r['rd']:.5f} +- {r['rd_se']:.5f}, mcsub {rd_m:.5f} +- {se_m:.5f}, z={z:.2f}")
+    assert abs(z) <= 3.0
+    assert r["specular"] / n == pytest.approx(sm["S"] / n, rel=1e-5)
+
+
+def test_split_layer_equals_whole(gpu):
+    from nmc_gb300 import layered
+
+    n = 400_000
+    whole = layered.run([(0.5, 80.0, 0.8, 1.4, 0.1), (2.0, 50.0, 0.7, 1.4, math.inf)], n, seed=1)
+    split = layered.run([(0.5, 80.0, 0.8, 1.4, 0.04), (0.5, 80.0, 0.8, 1.4, 0.06), (2.0, 50.0, 0.7, 1.4, math.inf)],
+                        n, seed=2)
+    z = (whole["rd"] - split["rd"]) / math.hypot(whole["rd_se"], split["rd_se"])
+    print(f"Rd whole {whole['rd']:.5f} split {split['rd']:.5f} z={z:.2f}")
+    assert abs(z) <= 3.0
+    a_top = split["a_layer"][0] + split["a_layer"][1]
+    assert a_top == pytest.approx(whole["a_layer"][0], rel=0.03)
+
+
+def test_beer_lambert_slab(gpu):
+    from nmc_gb300 import layered
+
+    n, mua, d = 200_000, 2.0, 0.3
+    r = layered.run([(mua, 0.0, 0.0, 1.0, d)], n, n_above=1.0, n_below=1.0, seed=3)
+    p = math.exp(-mua * d)
+    se = math.sqrt(p * (1 - p) / n)
+    print(f"Tt {r['tt']:.5f} vs {p:.5f}")
+    assert abs(r["tt"] - p) <= 4 * se
+    assert r["rd"] == 0.0
+
+
+def test_fresnel_slab(gpu):
+    from nmc_gb300 import layered
+
+    n, ns = 200_000, 1.5
+    r = layered.run([(0.0, 0.0, 0.0, ns, 1.0)], n, seed=5)
+    R = ((ns - 1) / (ns + 1)) ** 2
+    tt, rd = (1 - R) / (1 + R), (1 - R) * R / (1 + R)  # escape after an even / odd number of internal reflections
+    print(f"Tt {r['tt']:.5f} vs {tt:.5f}, Rd {r['rd']:.5f} vs {rd:.5f}")
+    assert abs(r["tt"] - tt) <= 4 * math.sqrt(tt * (1 - tt) / n)
+    assert abs(r["rd"] - rd) <= 4 * math.sqrt(rd * (1 - rd) / n) + 1e-4
+
+
+def test_weight_conservation_and_tallies(gpu):
+    from nmc_gb300 import layered
+
+    n = 200_000
+    lay = [(0.3, 120.0, 0.9, 1.4, 0.02), (5.0, 200.0, 0.85, 1.37, 0.05), (0.5, 90.0, 0.8, 1.45, 0.3)]
+    r = layered.run(lay, n, n_above=1.0, n_below=1.33, a_rz=True, seed=6)
+    total = (r["specular"] + r["Rd"] + r["Tt"] + r["A"]) / n
+    print(f"S+Rd+Tt+A = {total:.5f}")
+    assert total == pytest.approx(1.0, abs=2e-3)  # roulette keeps weight in expectation
+    assert r["a_layer"].sum() == pytest.approx(r["A"], rel=1e-9)
+    assert r["a_z"].sum() == pytest.approx(r["A"], rel=1e-6)
+    assert r["a_rz"].sum() == pytest.approx(r["A"], rel=1e-6)
+    assert r["rd_r"].sum() == pytest.approx(r["Rd"], rel=1e-6)
+    assert r["tt_r"].sum() == pytest.approx(r["Tt"], rel=1e-6)
