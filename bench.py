@@ -314,6 +314,8 @@ def run_sweep_workload(args) -> dict:
     build.build()
     torch.cuda.set_device(0)
     lam, tables, budgets = cases.skin_vessel_spectral_tables()
+    if args.budget_scale != 1.0:
+        budgets = np.maximum((budgets * args.budget_scale).astype(np.int64), 1)
     sets = [nsweep.TissueSet(t, b) for t, b in zip(tables, budgets)]
     total = int(budgets.sum())
     rp, tp0, v, ext = cases.skin_vessel_case(N=200, d=0.005, seed=11)
@@ -333,6 +335,10 @@ def run_sweep_workload(args) -> dict:
         return r, time.perf_counter() - t0
 
     res, batched_s = timed(lambda: nsweep.sweep(e, sets))
+    if args.profile_only:  # the batched launch alone, for ncu captures
+        e.close()
+        print(json.dumps({"profile_only": True, "photons": int(res["photons"].sum()), "seconds": batched_s}))
+        return {}
     tgt, batched_tgt_s = timed(lambda: nsweep.sweep(e, sets, target_rel_se=0.01))
     pilot = 20000
 
@@ -595,6 +601,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--photons", type=int, default=PHOTONS_PER_STEP)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--budget-scale", type=float, default=1.0,
+                    help="sweep workload: scale every wavelength's photon budget (profiling on a smaller case)")
     ap.add_argument("--tune", type=int, default=0,
                     help="autotune the launch shape on this many photons before the warm-up (0: defaults)")
     ap.add_argument("--profile-only", action="store_true",
