@@ -287,9 +287,106 @@ def run_ours(args) -> dict:
                                "sample": f"{cs['photons']} photons of the same workload, FP32 restatement with the "
                                          f"reference's generator ({cs['substeps_per_photon']:.0f} sub-steps/photon), "
                                          f"{cs['seconds']:.1f} s"}
+    if rank == 0 and world == 1 and not args.no_extras:
+        out["batched_to_1pct_se"] = batched_to_target_extra()
+        out["adjoint"] = adjoint_extra()
     if dist:
         dist.destroy_process_group()
     return out if rank == 0 else {}
+
+
+def _plain_sweep(e, sets, rp, v, ext_for, target, reprepare, pilot=20000):
+    """One plain run per wavelength on the same photon streams as the batched
+    sweep (set s: seed 11 + (s << 32)); with a target, the batched sweep's
+    pilot + top-up rule.  Returns (Rd, relative SE, photons) per set."""
+    import numpy as np
+
+    rd = np.zeros(len(sets))
+    rse = np.zeros(len(sets))
+    photons = 0
+    for i, q in enumerate(sets):
+        e.set_ext(ext_for(11 + (i << 32)))
+        if reprepare:
+            e.prepare_data(rp, q.tp, v)
+        else:
+            e.set_tissue_params(q.tp)
+            e.reset()
+        if target is None:
+            e.run(0, q.photons)
+        else:
+            n1 = min(pilot, q.photons)
+            e.run(0, n1)
+            s1 = e.summary()
+            me = s1["rd_sum"] / n1
+            var = max(s1["rd_sumsq"] / n1 - me * me, 1e-30)
+            need = int(np.ceil(1.15 * var / (target * max(me, 1e-30)) ** 2))
+            extra = max(min(need, q.photons) - n1, 0)
+            if extra:
+                e.run(n1, extra)
+        sm = e.summary()
+        n = sm["photons"]
+        photons += n
+        rd[i] = sm["rd_sum"] / n
+        rse[i] = np.sqrt(max(sm["rd_sumsq"] / n - rd[i] ** 2, 0) / n) / rd[i]
+    return rd, rse, photons
+
+
+def _timed(fn):
+    import torch
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = fn()
+    torch.cuda.synchronize()
+    return r, time.perf_counter() - t0
+
+
+def batched_to_target_extra() -> dict:
+    """The 351-wavelength skin-vessel sweep brought to 1% relative SE in Rd:
+    batched (pilot + top-up launches) against one plain run per wavelength
+    with the same rule (table swapped in place)."""
+    import numpy as np
+
+    import nmc_cases as cases
+    from nmc_gb300 import abi, engine
+    from nmc_gb300 import sweep as nsweep
+
+    lam, tables, budgets = cases.skin_vessel_spectral_tables()
+    sets = [nsweep.TissueSet(t, b) for t, b in zip(tables, budgets)]
+    rp, _, v, _ = cases.skin_vessel_case(N=200, d=0.005)
+    ext_for = lambda seed: abi.ext_defaults(rng=abi.RNG_PHILOX, seed=seed)  # noqa: E731
+    with engine.Engine(abi.SIM_MCXYZ_TT, 0, ext_for(11)) as e:
+        e.prepare_data(rp, tables[0], v)
+        e.run_sweep_tissues(tables[:8], [20000] * 8)
+        tgt, b_s = _timed(lambda: nsweep.sweep(e, sets, target_rel_se=0.01))
+        (_, p_rse, p_n), p_s = _timed(lambda: _plain_sweep(e, sets, rp, v, ext_for, 0.01, False))
+    n = int(tgt["photons"].sum())
+    return {"batched_s": b_s, "plain_s": p_s, "speedup": p_s / b_s, "photons": n,
+            "photons_per_s": n / b_s, "max_rel_se": float((tgt["Rd_se"] / tgt["Rd"]).max()),
+            "plain_max_rel_se": float(p_rse.max()), "launches": tgt["launches"],
+            "workload": "skin-vessel 200^3, 351 wavelengths, two-term HG, to 1% Rd SE"}
+
+
+def adjoint_extra(n: int = 1_000_000) -> dict:
+    """Forward + pMC adjoint against a plain forward, 64^3 per-voxel medium."""
+    import numpy as np
+
+    import nmc_cases as cases
+    from nmc_gb300 import abi, engine
+
+    rp, tp, v, ext, mua, mus, g, bins, dr = cases.adjoint_case()
+    G = np.random.default_rng(3).uniform(0.5, 1.5, bins + 1).astype(np.float32)
+    with engine.Engine(abi.SIM_MCXYZ, 0, ext) as e:
+        e.prepare_data(rp, tp, v)
+        e.set_radial_tally(bins, dr)
+        e.set_voxel_props(mua, mus, g)
+        fwd = lambda: (e.reset(), e.run(0, n))  # noqa: E731
+        adj = lambda: (e.reset(), e.adjoint_forward(0, n, 8 * n), e.adjoint_backward(G))  # noqa: E731
+        fwd(), adj()
+        t_f = min(_timed(fwd)[1] for _ in range(3))
+        t_a = min(_timed(adj)[1] for _ in range(3))
+    return {"forward_s": t_f, "forward_adjoint_s": t_a, "cost_ratio": t_a / t_f, "photons": n,
+            "workload": "64^3 per-voxel medium, gradient of Rd(r) w.r.t. all voxel mua, mus, g"}
 
 
 def run_sweep_workload(args) -> dict:
@@ -343,34 +440,7 @@ def run_sweep_workload(args) -> dict:
     pilot = 20000
 
     def plain(target, reprepare):
-        rd = np.zeros(len(sets))
-        rse = np.zeros(len(sets))
-        photons = 0
-        for i, q in enumerate(sets):
-            e.set_ext(ext_for(11 + (i << 32)))
-            if reprepare:
-                e.prepare_data(rp, q.tp, v)
-            else:
-                e.set_tissue_params(q.tp)
-                e.reset()
-            if target is None:
-                e.run(0, q.photons)
-            else:  # same pilot + top-up rule as the batched sweep
-                n1 = min(pilot, q.photons)
-                e.run(0, n1)
-                s1 = e.summary()
-                me = s1["rd_sum"] / n1
-                var = max(s1["rd_sumsq"] / n1 - me * me, 1e-30)
-                need = int(np.ceil(1.15 * var / (target * max(me, 1e-30)) ** 2))
-                extra = max(min(need, q.photons) - n1, 0)
-                if extra:
-                    e.run(n1, extra)
-            sm = e.summary()
-            n = sm["photons"]
-            photons += n
-            rd[i] = sm["rd_sum"] / n
-            rse[i] = np.sqrt(max(sm["rd_sumsq"] / n - rd[i] ** 2, 0) / n) / rd[i]
-        return rd, rse, photons
+        return _plain_sweep(e, sets, rp, v, ext_for, target, reprepare, pilot)
 
     (plain_rd, _, _), plain_s = timed(lambda: plain(None, False))
     (_, plain_tgt_rse, plain_tgt_n), plain_tgt_s = timed(lambda: plain(0.01, False))
@@ -601,6 +671,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--photons", type=int, default=PHOTONS_PER_STEP)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched-to-1%%-SE and adjoint comparisons of the default line")
     ap.add_argument("--budget-scale", type=float, default=1.0,
                     help="sweep workload: scale every wavelength's photon budget (profiling on a smaller case)")
     ap.add_argument("--tune", type=int, default=0,
