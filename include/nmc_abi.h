@@ -442,6 +442,9 @@ enum {
 typedef struct nmc_speckle {
   float Phase, Path, Scatt, Total, XX, XY, Ryx;
 } nmc_speckle;
+#ifdef __cplusplus
+static_assert(sizeof(nmc_speckle) == 28, "nmc_speckle layout (struct SPECKLE)");
+#endif
 
 /* Runs every setting's photons in one persistent launch on `device`.
  * S_primary / S_raman: n_angles x 4 Mie tables at the two wavelengths.
@@ -498,6 +501,10 @@ typedef struct nmc_layered_config {
   uint32_t flags;              /* NMC_FLAG_PRECISE_MATH */
   uint64_t seed;
 } nmc_layered_config;
+#ifdef __cplusplus
+static_assert(sizeof(nmc_layer) == 20, "nmc_layer layout");
+static_assert(sizeof(nmc_layered_config) == 40, "nmc_layered_config layout");
+#endif
 
 /* Per-run sums of nmc_layered_run (weights, not yet divided by photons). */
 enum {
@@ -526,6 +533,9 @@ typedef struct nmc_tune_result {
   int32_t n_tried;
   nmc_tune_entry tried[48];
 } nmc_tune_result;
+#ifdef __cplusplus
+static_assert(sizeof(nmc_tune_result) == 804, "nmc_tune_result layout");
+#endif
 
 /* Times the handle's kernel on photons [0, photons) under each candidate
  * launch configuration (block size; resident blocks per SM, i.e. photons in

@@ -90,3 +90,14 @@ def test_adjoint_case_and_autograd_module_import():
     assert 50.0 - 1e-4 <= mus.min() and mus.max() <= 300.0 + 1e-3
     assert np.all(g == np.float32(0.85))
     assert callable(autograd.radial_reflectance)
+
+
+def test_python_mirrors_of_the_new_structs():
+    # sizes the header pins with static_assert
+    assert C.sizeof(abi.EfieldConfig) == 88
+    assert C.sizeof(abi.EfieldSetting) == 24
+    assert C.sizeof(abi.Layer) == 20
+    assert C.sizeof(abi.LayeredConfig) == 40
+    assert C.sizeof(abi.TuneResult) == 804
+    assert abi.SPECKLE_DTYPE.itemsize == 28
+    assert C.sizeof(abi.SweepSet) == 64
