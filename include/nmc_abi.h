@@ -192,7 +192,8 @@ typedef struct nmc_summary {
 enum {
   NMC_DEVFLAG_STEPCAP = 1u << 0,
   NMC_DEVFLAG_BADTISSUE = 1u << 1,
-  NMC_DEVFLAG_REPLAY = 1u << 2 /* an adjoint replay did not reproduce a photon's recorded detections */
+  NMC_DEVFLAG_REPLAY = 1u << 2, /* an adjoint replay did not reproduce a photon's recorded detections */
+  NMC_DEVFLAG_BOUNDS = 1u << 3  /* checked build only: an index fell outside its buffer (access skipped) */
 };
 
 /* FP64 tallies readable with nmc_get_tally_f64. */

@@ -30,9 +30,14 @@ def nvcc() -> str:
     return cand if os.path.exists(cand) else "nvcc"
 
 
-def flags() -> list[str]:
-    return [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-            f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}"]
+CHECKED_OUT = os.path.join(OUT, "checked")
+CHECKED_LIB = os.path.join(CHECKED_OUT, "libnmc_gb300.so")
+
+
+def flags(checked: bool = False) -> list[str]:
+    f = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+         f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}"]
+    return f + ["-DNMC_CHECK_BOUNDS"] if checked else f
 
 
 def _stale(lib: str) -> bool:
@@ -44,9 +49,9 @@ def _stale(lib: str) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def _compile(src: str) -> str:
-    obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc(), *flags(), "-c", os.path.join(CSRC, src), "-o", obj]
+def _compile(src: str, checked: bool = False) -> str:
+    obj = os.path.join(CHECKED_OUT if checked else OUT, os.path.splitext(src)[0] + ".o")
+    cmd = [nvcc(), *flags(checked), "-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -71,6 +76,24 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+def build_checked(force: bool = False) -> str:
+    """The checked library (every tally index tested, NMC_DEVFLAG_BOUNDS on a
+    miss) in _build/checked/; select it with NMC_CHECKED=1 before importing
+    nmc_gb300.engine."""
+    os.makedirs(CHECKED_OUT, exist_ok=True)
+    if not force and not _stale(CHECKED_LIB):
+        return CHECKED_LIB
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, True), SOURCES))
+    tmp = CHECKED_LIB + ".tmp"
+    r = subprocess.run([nvcc(), ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-o", tmp], capture_output=True,
+                       text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CHECKED_LIB)
+    return CHECKED_LIB
+
+
 def build_cli() -> str:
     """The `nmc` program (host C++ over the C ABI), next to the library."""
     cxx = "g++" if subprocess.run(["which", "g++"], capture_output=True).returncode == 0 else nvcc()
@@ -89,3 +112,5 @@ def build_cli() -> str:
 
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose=True)
+    if "--checked" in sys.argv:
+        print(f"built {build_checked(force='--force' in sys.argv)}")

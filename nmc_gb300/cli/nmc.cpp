@@ -21,7 +21,11 @@
 //   --persistent    one persistent launch instead of the dispatch loop
 //   --device D      CUDA device (default 0)
 //   --dry-run       parse the inputs, print them and write _props.m only
+// Besides the reference's files it writes <name>_report.json: photons, kernel
+// time, photons/s, Rd with its standard error, sub-steps and scatterings per
+// photon (the reference only prints a rate, main.m:199).
 // Exit status 0, or 1 with a message (the reference exits 1 on unknown kinds).
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -376,6 +380,22 @@ int main(int argc, char** argv) {
       std::fprintf(f, "\t %1.6e", (!std::isnan(val) && !std::isinf(val)) ? val : 0.0);
     });
     table("_DetPhot2D.dat", [&](FILE* f, size_t idx) { std::fprintf(f, "\t %d", idx < n2d ? Det[idx] : 0); });
+  }
+  {  // structured run report
+    const double rd = kind == NMC_SIM_MCSUB ? (sm.S + sm.E) / N : sm.rd_sum / N;
+    const double m = (kind == NMC_SIM_MCSUB ? sm.E : sm.rd_sum) / N;
+    const double se = std::sqrt(std::max(0.0, sm.rd_sumsq / N - m * m) / N);
+    const std::string fn = name + "_report.json";
+    if (FILE* f = std::fopen(fn.c_str(), "w")) {
+      std::fprintf(f,
+                   "{\"name\": \"%s\", \"kind\": %d, \"photons\": %llu, \"rng\": \"%s\", "
+                   "\"kernel_ms\": %.6f, \"photons_per_s\": %.6e, \"Rd\": %.9f, \"Rd_se\": %.9f, "
+                   "\"substeps_per_photon\": %.6f, \"scatters_per_photon\": %.6f, \"device_flags\": %u}\n",
+                   rp.myname, kind, (unsigned long long)photons, philox ? "philox4x32-10" : "reference", sm.kernel_ms,
+                   photons / std::max(sm.kernel_ms * 1e-3, 1e-12), rd, se, (double)sm.substeps / N,
+                   (double)sm.scatters / N, sm.device_flags);
+      std::fclose(f);
+    }
   }
   nmc_destroy(h);
   return 0;

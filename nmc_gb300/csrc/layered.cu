@@ -105,10 +105,10 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
           const float rr = sqrtf(x * x + y * y);
           const int ir = min((int)(rr * P.idr), P.nr);
           if (Ln < 0) {
-            atomicAdd(P.rd_r + ir, to_fix(w));
+            if (idx_ok(ir, (unsigned)P.nr + 1u, P.flags)) atomicAdd(P.rd_r + ir, to_fix(w));
             rd += w;
           } else {
-            atomicAdd(P.tt_r + ir, to_fix(w));
+            if (idx_ok(ir, (unsigned)P.nr + 1u, P.flags)) atomicAdd(P.tt_r + ir, to_fix(w));
             tt += w;
           }
           alive = false;
@@ -135,11 +135,12 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
       if (absorb > 0.f) {
         const unsigned long long fa = to_fix(absorb);
         const int iz = min(max((int)(z * P.idz), 0), P.nz);
-        atomicAdd(P.a_z + iz, fa);
-        atomicAdd(P.a_layer + L, fa);
+        if (idx_ok(iz, (unsigned)P.nz + 1u, P.flags)) atomicAdd(P.a_z + iz, fa);
+        if (idx_ok(L, (unsigned)P.nl, P.flags)) atomicAdd(P.a_layer + L, fa);
         if (P.a_rz) {
           const int ir = min((int)(sqrtf(x * x + y * y) * P.idr), P.nr);
-          atomicAdd(P.a_rz + (size_t)ir * (P.nz + 1) + iz, fa);
+          if (idx_ok((size_t)ir * (P.nz + 1) + iz, (size_t)(P.nr + 1) * (P.nz + 1), P.flags))
+            atomicAdd(P.a_rz + (size_t)ir * (P.nz + 1) + iz, fa);
         }
       }
       spin<FAST>(hg_sample<FAST>(Ly.ph, u01(r.y)), u01(r.z), ux, uy, uz);
@@ -298,5 +299,6 @@ extern "C" nmc_status nmc_layered_run(int32_t device, const nmc_layered_config* 
     for (size_t i = 0; i < nz1; ++i) a_z[i] += (double)haz[i] * kUnfix;
   if (a_rz)
     for (size_t i = 0; i < nr1 * nz1; ++i) a_rz[i] += (double)harz[i] * kUnfix;
+  if (flags & NMC_DEVFLAG_BOUNDS) return done(NMC_EDEVICE);
   return done((flags & NMC_DEVFLAG_STEPCAP) ? NMC_ESTEPCAP : NMC_OK);
 }

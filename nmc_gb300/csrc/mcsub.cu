@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
         if (SMEM)
           smem_add(Jlo, Jhi, ir, W);
         else
-          atomicAdd(P.J + ir, to_fix(W));
+          if (idx_ok(ir, (unsigned)BINS + 1u, &P.sums->flags)) atomicAdd(P.J + ir, to_fix(W));
         E += W;
         if (TRACE) {
           ndet = 1;
@@ -195,7 +195,8 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
       if (SMEM)
         smem_add(Flo, Fhi, ir * BINS + iz, absorb);
       else
-        atomicAdd(P.F + (ir * BINS + iz), to_fix(absorb));
+        if (idx_ok(ir * BINS + iz, (unsigned long long)(BINS + 1) * (BINS + 1), &P.sums->flags))
+          atomicAdd(P.F + (ir * BINS + iz), to_fix(absorb));
     }
     // ---- SPIN (:243-279), ROULETTE (:289-294), next HOP's draw
     const bool need_roul = W < kTHRESHOLD;

@@ -96,13 +96,14 @@ __device__ __forceinline__ int lookup_index(int k, float f, int half, int odd, f
 struct Deposit {
   unsigned int idx;
   float acc;
-  __device__ __forceinline__ void flush(unsigned long long* F3D) {
-    if (acc > 0.f) atomicAdd(F3D + idx, to_fix(acc));
+  __device__ __forceinline__ void flush(unsigned long long* F3D, unsigned int nvox, unsigned int* flags) {
+    if (acc > 0.f && idx_ok(idx, nvox, flags)) atomicAdd(F3D + idx, to_fix(acc));
     acc = 0.f;
   }
-  __device__ __forceinline__ void add(unsigned long long* F3D, unsigned int i, float v) {
+  __device__ __forceinline__ void add(unsigned long long* F3D, unsigned int i, float v, unsigned int nvox,
+                                      unsigned int* flags) {
     if (i != idx) {
-      flush(F3D);
+      flush(F3D, nvox, flags);
       idx = i;
     }
     acc += v;
@@ -186,7 +187,7 @@ struct AdjAcc {
   unsigned int idx;
   float L, M, Q;
   __device__ __forceinline__ void flush(const XyzParams& P) {
-    if (idx != 0xFFFFFFFFu) {
+    if (idx != 0xFFFFFFFFu && idx_ok(idx, (unsigned long long)P.Nx * P.Ny * P.Nz, &P.sums->flags)) {
       if (L != 0.f) atomicAdd(P.gL + idx, (double)L);
       if (M != 0.f) atomicAdd(P.gM + idx, (double)M);
       if (Q != 0.f) atomicAdd(P.gQ + idx, (double)Q);
@@ -246,6 +247,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
   const bool replay = back || score;          // replays write no tallies
   const float* __restrict__ GF = ADJ ? P.adj_GF : nullptr;
   const int NyNx = P.Ny * P.Nx;
+  const unsigned int nvox = (unsigned int)(NyNx * P.Nz);
 
   RNG rng;
   int kx = 0, ky = 0, kz = 0, tiss = 0, depth = 0;
@@ -272,7 +274,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
         // the rounding of the two summation orders
         if (!(fabsf(D) <= 1e-4f * Dabs)) atomicOr(&P.sums->flags, (unsigned int)NMC_DEVFLAG_REPLAY);
       }
-      if (score && (st & kHave)) P.adj_Dw[pidx] = D;
+      if (score && (st & kHave) && idx_ok(pidx, P.n, &P.sums->flags)) P.adj_Dw[pidx] = D;
       if (SW && (st & kHave)) {  // per-set sums
         XyzSweepSums* q = P.sw_sums + set;
         atomicAdd(&q->photons, 1ull);
@@ -285,8 +287,9 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
         }
       }
       if ((st & kHave) && !replay && !SW) {  // retire the finished photon
-        dep.flush(P.F3D);
-        if (Rd_loc > 0.f) atomicAdd(P.rd_slots + slot, to_fix(Rd_loc));  // :753
+        dep.flush(P.F3D, nvox, &P.sums->flags);
+        if (Rd_loc > 0.f && idx_ok(slot, P.nslots, &P.sums->flags))
+          atomicAdd(P.rd_slots + slot, to_fix(Rd_loc));  // :753
         atomicAdd(&s_tot[0], 1ull);
         atomicAdd(&s_tot[1], (unsigned long long)nsub);
         atomicAdd(&s_tot[2], (unsigned long long)nsc);
@@ -305,7 +308,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
           r.x = (float)kx * P.dx + fx;
           r.y = (float)ky * P.dy + fy;
           r.z = (float)kz * P.dz + fz;
-          P.trace.recs[pidx] = r;
+          if (idx_ok(pidx, P.n, &P.sums->flags)) P.trace.recs[pidx] = r;
         }
       }
       pidx = next_photon(&P.sums->work);
@@ -349,7 +352,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
       const int iy = min(max(lookup_index(ky, fy, P.Ny / 2, 0, 0.f), 0), P.Ny - 1);
       const int iz = min(max(lookup_index(kz, fz, 0, 0, 0.f), 0), P.Nz - 1);
       i = (unsigned int)(iz * NyNx + ix * P.Ny + iy);
-      if (!VOX) tiss = __ldg(P.V + i);
+      if (!VOX) tiss = idx_ok(i, nvox, &P.sums->flags) ? __ldg(P.V + i) : 0;
       sleft = M::neglog(rng.first_step(k0, k1));  // HOP (:501-502)
       depth = 0;
       Rd_loc = Atot = 0.f;
@@ -368,7 +371,8 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
     // the step to the nearest face (:534-682) share one straight path; only
     // the face landing, the voxel lookup and the tissue load are predicated
     // on the crossing, so the lanes of a warp stay together.
-    const float4 c = VOX ? __ldg(P.vox + i) : (SW ? __ldg(P.sw_core + sbase + tiss) : s_core[tiss]);  // mua, mus, 1/mus, g
+    const float4 c = VOX ? __ldg(P.vox + (idx_ok(i, nvox, &P.sums->flags) ? i : 0u))
+                         : (SW ? __ldg(P.sw_core + sbase + tiss) : s_core[tiss]);  // mua, mus, 1/mus, g
     float s = sleft * c.z;
     ++nsub;
     ++depth;
@@ -415,7 +419,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
           Dabs += fabsf(e_dep);
         }
       } else if (!SW && (st & kBflag)) {
-        dep.add(P.F3D, i, absorb);
+        dep.add(P.F3D, i, absorb, nvox, &P.sums->flags);
       }
     }
     sleft = sv ? 0.f : sleft - s * c.y;
@@ -471,9 +475,12 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
                 Rd_loc += dw;
                 if (!SW) {
                   const unsigned int i2d = (unsigned int)(jx * P.Ny + jy);
-                  atomicAdd(P.Rd2D + i2d, to_fix(dw));
-                  atomicAdd(P.Det2D + i2d, 1u);
-                  if (P.rd_r) atomicAdd(P.rd_r + rbin, to_fix(dw));
+                  if (idx_ok(i2d, (unsigned long long)P.Nx * P.Ny, &P.sums->flags)) {
+                    atomicAdd(P.Rd2D + i2d, to_fix(dw));
+                    atomicAdd(P.Det2D + i2d, 1u);
+                  }
+                  if (P.rd_r && idx_ok(rbin, (unsigned)P.rd_bins + 1u, &P.sums->flags))
+                    atomicAdd(P.rd_r + rbin, to_fix(dw));
                 }
                 if (ADJ) {  // record pass: keep (photon, bin, weight) for the backward pass
                   const unsigned long long k = atomicAdd(P.ev_count, 1ull);
@@ -540,7 +547,8 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
           if (TRACE) ++ndet;
           if (!SW) {
             const int jx = min(max(ix, 0), P.Nx - 1), jy = min(max(iy, 0), P.Ny - 1);
-            atomicAdd(P.Rd2D + (unsigned int)(jx * P.Ny + jy), to_fix(W));
+            if (idx_ok((unsigned)(jx * P.Ny + jy), (unsigned long long)P.Nx * P.Ny, &P.sums->flags))
+              atomicAdd(P.Rd2D + (unsigned int)(jx * P.Ny + jy), to_fix(W));
           }
         }
         if (kz < 0) {
@@ -569,7 +577,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
         }
       }
       i = (unsigned int)(iz * NyNx + ix * P.Ny + iy);  // :675-679
-      if (!VOX) tiss = __ldg(P.V + i);
+      if (!VOX) tiss = idx_ok(i, nvox, &P.sums->flags) ? __ldg(P.V + i) : 0;
     }
     if (nsub >= P.step_cap) {  // device-side cap: not a reference behaviour
       kill(NMC_FATE_STEPCAP);
@@ -608,7 +616,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
     if (hard_kill && (W < kMIN_VALUE || (int)nsc > kMAX_SCATT))
       kill(W < kMIN_VALUE ? NMC_FATE_MINWEIGHT : NMC_FATE_MAXSCATT);
     if (TRACE && nev < P.trace.k_events) {
-      P.trace.events[pidx * P.trace.k_events + nev] =
+      if (idx_ok(pidx, P.n, &P.sums->flags)) P.trace.events[pidx * P.trace.k_events + nev] =
           make_float4((float)kx * P.dx + fx, (float)ky * P.dy + fy, (float)kz * P.dz + fz, W);
       ++nev;
     }

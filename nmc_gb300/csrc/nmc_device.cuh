@@ -368,6 +368,22 @@ __device__ __forceinline__ void spin(float costheta, float upsi, float& ux, floa
   }
 }
 
+// ----------------------------------------------------------- index checks
+// The checked build (-DNMC_CHECK_BOUNDS, nmc_gb300/_build/checked/) tests
+// every tally index against its buffer; an index out of range raises
+// NMC_DEVFLAG_BOUNDS and the access is skipped.  compute-sanitizer is not
+// available for these kernels, so this is the bounds checker; in the normal
+// build the test compiles away.
+#ifdef NMC_CHECK_BOUNDS
+__device__ __forceinline__ bool idx_ok(unsigned long long i, unsigned long long n, unsigned int* flags) {
+  if (i < n) return true;
+  atomicOr(flags, (unsigned int)NMC_DEVFLAG_BOUNDS);
+  return false;
+}
+#else
+__device__ __forceinline__ bool idx_ok(unsigned long long, unsigned long long, unsigned int*) { return true; }
+#endif
+
 // ----------------------------------------------------------- work queue
 // Hands out photon indices in warp-aggregated chunks: one atomic per group
 // of threads that need a photon at the same time.

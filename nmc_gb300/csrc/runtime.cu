@@ -359,6 +359,8 @@ nmc_status sync_all(nmc_handle* h) {
   NMC_CUDA(h, cudaMemcpy(&flags, &h->d_sums->flags, sizeof flags, cudaMemcpyDeviceToHost));
   const unsigned int fresh = flags & ~h->seen_flags;
   h->seen_flags = flags;
+  if (fresh & NMC_DEVFLAG_BOUNDS)
+    return fail(h, NMC_EDEVICE, "a tally index fell outside its buffer (checked build)");
   if (fresh & NMC_DEVFLAG_REPLAY)
     return fail(h, NMC_EDEVICE, "the adjoint replay did not reproduce the recorded detections");
   if (fresh & NMC_DEVFLAG_STEPCAP)

@@ -20,7 +20,9 @@ import numpy as np
 
 from . import abi
 
-LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "libnmc_gb300.so")
+_BUILD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build")
+# NMC_CHECKED=1 selects the checked build (every tally index tested)
+LIB_PATH = os.path.join(_BUILD, "checked" if os.environ.get("NMC_CHECKED") == "1" else "", "libnmc_gb300.so")
 
 _lib = None
 _P = C.c_void_p

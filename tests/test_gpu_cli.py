@@ -44,6 +44,11 @@ def test_cli_mcxyz_files(gpu, tmp_path):
     idx = np.arange(rp.Ny)[None, :] + np.arange(rp.Nx)[:, None] * rp.Nx
     np.testing.assert_allclose(ryx, res["Rd2D"][idx], rtol=1e-6, atol=1e-12)
     np.testing.assert_array_equal(det, res["DetPhot2D"][idx])
+    import json
+
+    rep = json.load(open(name + "_report.json"))
+    assert rep["photons"] == 100_000 and rep["rng"] == "reference"
+    assert rep["Rd"] == pytest.approx(float(rd), rel=1e-5) and 0 < rep["Rd_se"] < rep["Rd"]
 
 
 def test_cli_mcsub_files(gpu, tmp_path):
