@@ -521,6 +521,16 @@ nmc_status nmc_layered_run(int32_t device, const nmc_layered_config* cfg, const 
                            uint64_t first, uint64_t photons, double* out, double* rd_r, double* tt_r,
                            double* a_z, double* a_rz, double* a_layer);
 
+/* The same run with per-layer gradients of L = sum_b grad_rd_r[b] rd_r[b] +
+ * sum_b grad_tt_r[b] tt_r[b] (un-normalised tallies; either gradient may be
+ * NULL, not both): grad_mua, grad_mus, grad_g (n_layers each, +=) from the
+ * path length, interaction count and d ln p_HG/dg each photon collects per
+ * layer (perturbation Monte Carlo; at most 16 layers). */
+nmc_status nmc_layered_adjoint(int32_t device, const nmc_layered_config* cfg, const nmc_layer* layers,
+                               uint64_t first, uint64_t photons, const float* grad_rd_r, const float* grad_tt_r,
+                               double* out, double* rd_r, double* tt_r, double* grad_mua, double* grad_mus,
+                               double* grad_g);
+
 /* -------------------------------------------------------------- autotune */
 /* One launch configuration the autotuner timed. */
 typedef struct nmc_tune_entry {

@@ -23,6 +23,16 @@
 // key (seed lo, seed hi), counter (photon lo, photon hi, interaction,
 // 'LAYR'): x step, y cos theta, z psi, w roulette; boundary events draw their
 // Fresnel choice from counter (photon lo, photon hi, event | 2^31, 'LAYR').
+//
+// Adjoint (ADJ): a photon scores once, when it escapes (G_rd[r bin] or
+// G_tt[r bin] times its weight), so the per-layer derivatives of the loss
+// accumulate directly from per-photon sums kept per layer: the geometric path
+// L_l, the interactions n_l and Q_l = sum d ln p_HG(cos; g_l)/dg.  With
+// implicit capture (weight x mus/mu_t per interaction, paths sampled with
+// mu_t) the likelihood ratio of the path and the weight's own derivative give
+//   d score/d mua_l = -score L_l,
+//   d score/d mus_l = score (n_l / mus_l - L_l),
+//   d score/d g_l   = score Q_l.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -37,9 +47,15 @@ namespace {
 
 constexpr uint32_t kLayTag = 0x4C415952u;
 constexpr int kMaxLayers = 100;  // MAXLAYERS, definitions.h:24
+constexpr int kMaxAdjLayers = 16;  // per-photon sums of the adjoint live in local memory
+
+__device__ __forceinline__ float dln_hg_dg(float g, float mu) {  // p = (1-g^2)/(2 (1+g^2-2g mu)^1.5)
+  return -2.f * g / (1.f - g * g) - 3.f * (g - mu) / (1.f + g * g - 2.f * g * mu);
+}
 
 struct LayDev {
   float mua, mus, inv_mut, n, z0, z1;  // z1 = +inf for a semi-infinite last layer
+  float g;
   PhaseConst ph;
 };
 
@@ -60,15 +76,22 @@ struct LayParams {
   unsigned long long* work;
   unsigned int* flags;
   uint32_t step_cap;
+  // adjoint
+  const float* g_rd;  // nr + 1 upstream gradient of rd_r (may be null)
+  const float* g_tt;  // nr + 1 upstream gradient of tt_r (may be null)
+  double* grad;       // 3 * nl: d/dmua, d/dmus, d/dg
 };
 
-template <bool FAST>
+template <bool FAST, bool ADJ>
 __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
   using M = Math<FAST>;
   __shared__ LayDev s_lay[kMaxLayers];
   __shared__ double s_sum[NMC_LAY_FIELDS];
+  __shared__ double s_grad[ADJ ? 3 * kMaxAdjLayers : 1];
   for (int i = threadIdx.x; i < P.nl; i += blockDim.x) s_lay[i] = P.lay[i];
   if (threadIdx.x < NMC_LAY_FIELDS) s_sum[threadIdx.x] = 0.0;
+  if (ADJ)
+    for (int i = threadIdx.x; i < 3 * kMaxAdjLayers; i += blockDim.x) s_grad[i] = 0.0;
   __syncthreads();
   while (true) {
     const unsigned long long g = next_photon(P.work);
@@ -80,6 +103,10 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
     uint32_t hop = 0, ev = 0;
     bool alive = true;
     float rd = 0.f, tt = 0.f;
+    float aL[ADJ ? kMaxAdjLayers : 1], aN[ADJ ? kMaxAdjLayers : 1], aQ[ADJ ? kMaxAdjLayers : 1];
+    float score = 0.f;
+    if (ADJ)
+      for (int l = 0; l < P.nl; ++l) aL[l] = aN[l] = aQ[l] = 0.f;
     uint4 r = philox4x32_10(make_uint4(c0, c1, 0u, kLayTag), P.k0, P.k1);
     while (alive) {
       const LayDev& Ly = s_lay[L];
@@ -91,6 +118,7 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
         x = fmaf(db, ux, x);
         y = fmaf(db, uy, y);
         z = uz > 0.f ? Ly.z1 : Ly.z0;
+        if (ADJ) aL[L] += db;
         sleft = Ly.inv_mut > 0.f ? fmaxf(sleft - db / Ly.inv_mut, 0.f) : sleft;
         const bool down = uz > 0.f;
         const int Ln = down ? L + 1 : L - 1;
@@ -107,9 +135,11 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
           if (Ln < 0) {
             if (idx_ok(ir, (unsigned)P.nr + 1u, P.flags)) atomicAdd(P.rd_r + ir, to_fix(w));
             rd += w;
+            if (ADJ && P.g_rd) score = w * __ldg(P.g_rd + ir);
           } else {
             if (idx_ok(ir, (unsigned)P.nr + 1u, P.flags)) atomicAdd(P.tt_r + ir, to_fix(w));
             tt += w;
+            if (ADJ && P.g_tt) score = w * __ldg(P.g_tt + ir);
           }
           alive = false;
         } else {  // refracted into the next layer (Snell)
@@ -130,6 +160,10 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
       y = fmaf(s, uy, y);
       z = fmaf(s, uz, z);
       sleft = 0.f;
+      if (ADJ) {
+        aL[L] += s;
+        aN[L] += 1.f;
+      }
       const float absorb = w * Ly.mua * Ly.inv_mut;
       w -= absorb;
       if (absorb > 0.f) {
@@ -143,7 +177,9 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
             atomicAdd(P.a_rz + (size_t)ir * (P.nz + 1) + iz, fa);
         }
       }
-      spin<FAST>(hg_sample<FAST>(Ly.ph, u01(r.y)), u01(r.z), ux, uy, uz);
+      const float cth = hg_sample<FAST>(Ly.ph, u01(r.y));
+      if (ADJ && Ly.ph.hg_mode == 0) aQ[L] += dln_hg_dg(Ly.g, cth);
+      spin<FAST>(cth, u01(r.z), ux, uy, uz);
       if (w < kTHRESHOLD) {
         if (u01(r.w) <= kCHANCE)
           w /= kCHANCE;
@@ -163,8 +199,21 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
     atomicAdd(&s_sum[NMC_LAY_TT], (double)tt);
     atomicAdd(&s_sum[NMC_LAY_TT2], (double)tt * (double)tt);
     atomicAdd(&s_sum[NMC_LAY_INTERACTIONS], (double)hop);
+    if (ADJ && score != 0.f)
+      for (int l = 0; l < P.nl; ++l) {
+        atomicAdd(&s_grad[l], (double)(-score * aL[l]));
+        atomicAdd(&s_grad[kMaxAdjLayers + l],
+                  (double)(score * (s_lay[l].mus > 0.f ? aN[l] / s_lay[l].mus - aL[l] : -aL[l])));
+        atomicAdd(&s_grad[2 * kMaxAdjLayers + l], (double)(score * aQ[l]));
+      }
   }
   __syncthreads();
+  if (ADJ)
+    for (int i = threadIdx.x; i < 3 * P.nl; i += blockDim.x) {
+      const int k = i / P.nl, l = i % P.nl;
+      const double v = s_grad[k * kMaxAdjLayers + l];
+      if (v != 0.0) atomicAdd(P.grad + i, v);
+    }
   if (threadIdx.x < NMC_LAY_FIELDS && s_sum[threadIdx.x] != 0.0) atomicAdd(P.sums + threadIdx.x, s_sum[threadIdx.x]);
 }
 
@@ -176,11 +225,16 @@ double host_fresnel_normal(double n1, double n2) {
 }  // namespace
 }  // namespace nmc
 
-extern "C" nmc_status nmc_layered_run(int32_t device, const nmc_layered_config* cfg, const nmc_layer* layers,
-                                      uint64_t first, uint64_t photons, double* out, double* rd_r, double* tt_r,
-                                      double* a_z, double* a_rz, double* a_layer) {
+namespace {
+
+nmc_status layered_impl(int32_t device, const nmc_layered_config* cfg, const nmc_layer* layers, uint64_t first,
+                        uint64_t photons, double* out, double* rd_r, double* tt_r, double* a_z, double* a_rz,
+                        double* a_layer, const float* g_rd, const float* g_tt, double* grad_mua, double* grad_mus,
+                        double* grad_g) {
   using namespace nmc;
+  const bool adj = g_rd || g_tt;
   if (!cfg || !layers || !out) return NMC_EINVAL;
+  if (adj && cfg->n_layers > kMaxAdjLayers) return NMC_EINVAL;
   const nmc_layered_config& c = *cfg;
   if (c.n_layers < 1 || c.n_layers > kMaxLayers || c.nr < 1 || c.nr > 65536 || c.nz < 1 || c.nz > 65536 ||
       !(c.dr > 0.f) || !(c.dz > 0.f) || !(c.n_above > 0.f) || !(c.n_below > 0.f) || !std::isfinite(c.n_above) ||
@@ -200,6 +254,7 @@ extern "C" nmc_status nmc_layered_run(int32_t device, const nmc_layered_config* 
     d.mus = q.mus;
     d.inv_mut = q.mua + q.mus > 0.f ? (float)(1.0 / ((double)q.mua + q.mus)) : 0.f;
     d.n = q.n;
+    d.g = q.g;
     d.z0 = (float)z;
     z += q.thickness;
     d.z1 = std::isfinite(q.thickness) ? (float)z : INFINITY;
@@ -233,8 +288,15 @@ extern "C" nmc_status nmc_layered_run(int32_t device, const nmc_layered_config* 
   auto* dal = (unsigned long long*)dalloc(8 * c.n_layers);
   auto* dsum = (double*)dalloc(sizeof(double) * NMC_LAY_FIELDS);
   auto* dwork = (unsigned long long*)dalloc(16);
-  if (!dlay || !drd || !dtt || !daz || (a_rz && !darz) || !dal || !dsum || !dwork) return done(NMC_ENOMEM);
-  if (cudaMemcpyAsync(dlay, lay.data(), sizeof(LayDev) * c.n_layers, cudaMemcpyHostToDevice, st) != cudaSuccess)
+  auto* dgrd = g_rd ? (float*)dalloc(4 * nr1) : nullptr;
+  auto* dgtt = g_tt ? (float*)dalloc(4 * nr1) : nullptr;
+  auto* dgrad = adj ? (double*)dalloc(sizeof(double) * 3 * c.n_layers) : nullptr;
+  if (!dlay || !drd || !dtt || !daz || (a_rz && !darz) || !dal || !dsum || !dwork || (g_rd && !dgrd) ||
+      (g_tt && !dgtt) || (adj && !dgrad))
+    return done(NMC_ENOMEM);
+  if (cudaMemcpyAsync(dlay, lay.data(), sizeof(LayDev) * c.n_layers, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      (g_rd && cudaMemcpyAsync(dgrd, g_rd, 4 * nr1, cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+      (g_tt && cudaMemcpyAsync(dgtt, g_tt, 4 * nr1, cudaMemcpyHostToDevice, st) != cudaSuccess))
     return done(NMC_EDEVICE);
   LayParams P{};
   P.lay = dlay;
@@ -260,8 +322,12 @@ extern "C" nmc_status nmc_layered_run(int32_t device, const nmc_layered_config* 
   P.work = dwork;
   P.flags = (unsigned int*)(dwork + 1);
   P.step_cap = 20000000u;
+  P.g_rd = dgrd;
+  P.g_tt = dgtt;
+  P.grad = dgrad;
   const bool fast = !(c.flags & NMC_FLAG_PRECISE_MATH);
-  const void* f = fast ? (const void*)layered_kernel<true> : (const void*)layered_kernel<false>;
+  const void* f = adj ? (fast ? (const void*)layered_kernel<true, true> : (const void*)layered_kernel<false, true>)
+                      : (fast ? (const void*)layered_kernel<true, false> : (const void*)layered_kernel<false, false>);
   int per_sm = 0, nsm = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, 256, 0) != cudaSuccess || per_sm < 1)
@@ -273,6 +339,7 @@ extern "C" nmc_status nmc_layered_run(int32_t device, const nmc_layered_config* 
   if (photons > 0 && cudaLaunchKernel(f, dim3((unsigned)grid), dim3(256), args, 0, st) != cudaSuccess)
     return done(NMC_EDEVICE);
   std::vector<unsigned long long> hrd(nr1), htt(nr1), haz(nz1), hal(c.n_layers), harz(a_rz ? nr1 * nz1 : 0);
+  std::vector<double> hgrad(adj ? 3 * c.n_layers : 0);
   unsigned int flags = 0;
   if (cudaMemcpyAsync(out, dsum, sizeof(double) * NMC_LAY_FIELDS, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaMemcpyAsync(hrd.data(), drd, 8 * nr1, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
@@ -280,6 +347,8 @@ extern "C" nmc_status nmc_layered_run(int32_t device, const nmc_layered_config* 
       cudaMemcpyAsync(haz.data(), daz, 8 * nz1, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaMemcpyAsync(hal.data(), dal, 8 * c.n_layers, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       (a_rz && cudaMemcpyAsync(harz.data(), darz, 8 * nr1 * nz1, cudaMemcpyDeviceToHost, st) != cudaSuccess) ||
+      (adj && cudaMemcpyAsync(hgrad.data(), dgrad, sizeof(double) * 3 * c.n_layers, cudaMemcpyDeviceToHost, st) !=
+                  cudaSuccess) ||
       cudaMemcpyAsync(&flags, P.flags, sizeof flags, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return done(NMC_EDEVICE);
@@ -299,6 +368,29 @@ extern "C" nmc_status nmc_layered_run(int32_t device, const nmc_layered_config* 
     for (size_t i = 0; i < nz1; ++i) a_z[i] += (double)haz[i] * kUnfix;
   if (a_rz)
     for (size_t i = 0; i < nr1 * nz1; ++i) a_rz[i] += (double)harz[i] * kUnfix;
+  for (int l = 0; adj && l < c.n_layers; ++l) {
+    if (grad_mua) grad_mua[l] += hgrad[l];
+    if (grad_mus) grad_mus[l] += hgrad[c.n_layers + l];
+    if (grad_g) grad_g[l] += hgrad[2 * c.n_layers + l];
+  }
   if (flags & NMC_DEVFLAG_BOUNDS) return done(NMC_EDEVICE);
   return done((flags & NMC_DEVFLAG_STEPCAP) ? NMC_ESTEPCAP : NMC_OK);
+}
+
+}  // namespace
+
+extern "C" nmc_status nmc_layered_run(int32_t device, const nmc_layered_config* cfg, const nmc_layer* layers,
+                                      uint64_t first, uint64_t photons, double* out, double* rd_r, double* tt_r,
+                                      double* a_z, double* a_rz, double* a_layer) {
+  return layered_impl(device, cfg, layers, first, photons, out, rd_r, tt_r, a_z, a_rz, a_layer, nullptr, nullptr,
+                      nullptr, nullptr, nullptr);
+}
+
+extern "C" nmc_status nmc_layered_adjoint(int32_t device, const nmc_layered_config* cfg, const nmc_layer* layers,
+                                          uint64_t first, uint64_t photons, const float* grad_rd_r,
+                                          const float* grad_tt_r, double* out, double* rd_r, double* tt_r,
+                                          double* grad_mua, double* grad_mus, double* grad_g) {
+  if (!grad_rd_r && !grad_tt_r) return NMC_EINVAL;
+  return layered_impl(device, cfg, layers, first, photons, out, rd_r, tt_r, nullptr, nullptr, nullptr, grad_rd_r,
+                      grad_tt_r, grad_mua, grad_mus, grad_g);
 }

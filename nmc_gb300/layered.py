@@ -21,6 +21,9 @@ def _bind():
         L.nmc_layered_run.argtypes = [C.c_int32, C.POINTER(abi.LayeredConfig), C.POINTER(abi.Layer), C.c_uint64,
                                       C.c_uint64, _P, _P, _P, _P, _P, _P]
         L.nmc_layered_run.restype = C.c_int
+        L.nmc_layered_adjoint.argtypes = [C.c_int32, C.POINTER(abi.LayeredConfig), C.POINTER(abi.Layer),
+                                          C.c_uint64, C.c_uint64, _P, _P, _P, _P, _P, _P, _P, _P]
+        L.nmc_layered_adjoint.restype = C.c_int
         L._lay_bound = True
     return L
 
@@ -54,4 +57,32 @@ def run(layers, photons: int, n_above: float = 1.0, n_below: float = 1.0, nr: in
     res.update(rd_r=rd, tt_r=tt, a_z=az, a_layer=al)
     if a_rz:
         res["a_rz"] = arz
+    return res
+
+
+def adjoint(layers, photons: int, grad_rd_r=None, grad_tt_r=None, n_above: float = 1.0, n_below: float = 1.0,
+            nr: int = 100, dr: float = 0.01, seed: int = 0, first: int = 0, device: int = 0) -> dict:
+    """Per-layer gradients of L = grad_rd_r . rd_r + grad_tt_r . tt_r (the
+    un-normalised radial tallies of photons [first, first + photons)) with
+    respect to each layer's mua, mus and g (perturbation Monte Carlo), with
+    the run's tallies.  At most 16 layers."""
+    L = _bind()
+    nl = len(layers)
+    arr = (abi.Layer * nl)(*[abi.Layer(*map(float, q)) for q in layers])
+    cfg = abi.LayeredConfig(n_layers=nl, n_above=n_above, n_below=n_below, nr=nr, dr=dr, nz=1, dz=1.0, flags=0,
+                            seed=seed)
+    grd = None if grad_rd_r is None else np.ascontiguousarray(grad_rd_r, np.float32)
+    gtt = None if grad_tt_r is None else np.ascontiguousarray(grad_tt_r, np.float32)
+    for g in (grd, gtt):
+        if g is not None and g.size != nr + 1:
+            raise ValueError(f"upstream gradients need nr + 1 = {nr + 1} values")
+    out = np.zeros(len(abi.LAY_FIELDS), np.float64)
+    rd, tt = np.zeros(nr + 1), np.zeros(nr + 1)
+    ga, gs, gg = np.zeros(nl), np.zeros(nl), np.zeros(nl)
+    st = L.nmc_layered_adjoint(int(device), C.byref(cfg), arr, int(first), int(photons), _ptr(grd), _ptr(gtt),
+                               _ptr(out), _ptr(rd), _ptr(tt), _ptr(ga), _ptr(gs), _ptr(gg))
+    if st != 0:
+        raise NMCError(st, "nmc_layered_adjoint")
+    res = {k: out[i] for i, k in enumerate(abi.LAY_FIELDS)}
+    res.update(rd_r=rd, tt_r=tt, grad_mua=ga, grad_mus=gs, grad_g=gg)
     return res

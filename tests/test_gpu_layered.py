@@ -85,3 +85,41 @@ def test_weight_conservation_and_tallies(gpu):
     assert r["a_rz"].sum() == pytest.approx(r["A"], rel=1e-6)
     assert r["rd_r"].sum() == pytest.approx(r["Rd"], rel=1e-6)
     assert r["tt_r"].sum() == pytest.approx(r["Tt"], rel=1e-6)
+
+
+def test_layer_adjoint_matches_crn_finite_differences(gpu):
+    # per-layer pMC gradients of a loss on Rd(r) and Tt(r) against central
+    # differences with common random numbers, 16 batches of 40k photons
+    from nmc_gb300 import layered
+
+    lay = [[0.5, 120.0, 0.9, 1.4, 0.02], [3.0, 150.0, 0.85, 1.4, 0.05], [1.0, 80.0, 0.8, 1.4, 0.2]]
+    nr, B, nb = 60, 16, 40_000
+    rng = np.random.default_rng(9)
+    G_rd = rng.uniform(0.5, 1.5, nr + 1).astype(np.float32)
+    G_tt = rng.uniform(0.0, 1.0, nr + 1).astype(np.float32)
+    loss = lambda r: float(G_rd.astype(np.float64) @ r["rd_r"] + G_tt.astype(np.float64) @ r["tt_r"])  # noqa: E731
+    pm = np.zeros((B, 3, 3))
+    fd = np.zeros((B, 3, 3))
+    for b in range(B):
+        a = layered.adjoint(lay, nb, G_rd, G_tt, nr=nr, dr=0.005, first=b * nb, seed=2)
+        pm[b] = np.stack([a["grad_mua"], a["grad_mus"], a["grad_g"]])
+    for p, idx, rel in ((0, 0, 0.02), (1, 1, 0.02), (2, 2, None)):
+        for l in range(3):
+            base = lay[l][idx]
+            h = 0.01 if rel is None else rel * base
+            sides = []
+            for sgn in (1, -1):
+                l2 = [list(q) for q in lay]
+                l2[l][idx] = base + sgn * h
+                sides.append(np.array([loss(layered.run(l2, nb, nr=nr, dr=0.005, first=b * nb, seed=2))
+                                       for b in range(B)]))
+            fd[:, p, l] = (sides[0] - sides[1]) / (2 * h)
+    for p, name in enumerate(("mua", "mus", "g")):
+        d = pm[:, p] - fd[:, p]
+        t = d.mean(0) / (d.std(0, ddof=1) / np.sqrt(B))
+        print(f"{name}: pmc {pm[:, p].mean(0)} fd {fd[:, p].mean(0)} t {t}")
+        if name == "mua":
+            P, F = pm[:, p].mean(0), fd[:, p].mean(0)
+            assert np.all(np.abs(P - F) <= np.maximum(4.5 * d.std(0, ddof=1) / np.sqrt(B), 1e-3 * np.abs(F)))
+        else:
+            assert np.all(np.abs(t) <= 4.5)
