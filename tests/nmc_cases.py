@@ -248,3 +248,39 @@ def hg_amplitude_table(g: float, n_angles: int = 1801) -> np.ndarray:
     p = (1 - g * g) / (1 + g * g - 2 * g * np.cos(th)) ** 1.5
     a = np.sqrt(p).astype(np.float32)
     return np.stack([a, np.zeros_like(a), a, np.zeros_like(a)], axis=1)
+
+
+def notebook_skinvessel_map(N: int = 200, d: float = 0.0005, zsurf: float = 0.01) -> np.ndarray:
+    """The sample notebooks' skin-vessel label volume (example2/3 cell 4):
+    dermis (4), air (1) above zsurf, epidermis (5) for 0.006 cm below it,
+    blood (3) in a cylinder along y of radius 0.01 cm at x = 0, z = N/2 d;
+    in the engine's voxel order (the notebooks write T(y, x, z) in Fortran
+    order, which is the same order)."""
+    x = (np.arange(1, N + 1) - N / 2.0) * d
+    z = np.arange(1, N + 1) * d
+    T = np.full((N, N, N), 4, np.uint8)  # [iy, ix, iz]
+    a = int(round(zsurf / d))
+    if a >= 1:
+        T[:, :, :a] = 1
+    e1 = max(int(round(zsurf / d)) + 1, 1)
+    e2 = min(int(round((zsurf + 0.006) / d)), N)
+    if e2 >= e1:
+        T[:, :, e1 - 1:e2] = 5
+    inside = (x[:, None] ** 2 + (z[None, :] - N / 2.0 * d) ** 2) <= 0.01 ** 2  # [ix, iz]
+    T[:, inside] = 3
+    return np.ascontiguousarray(T.transpose(2, 1, 0)).reshape(-1)
+
+
+def write_notebook_mci(path: str, tissues, N: int = 200, d: float = 0.0005):
+    """_H.mci exactly as example2/3 cell 5 writes it (skin vessel, "%.4f")."""
+    import math as _m
+
+    vals = [f"{10.0:.2f}", f"{N}", f"{N}", f"{N}", f"{d:.4f}", f"{d:.4f}", f"{d:.4f}", "0", "0", "2",
+            f"{0.0:.4f}", f"{0.0:.4f}", f"{0.0101:.4f}", f"{0.0:.4f}", f"{0.0:.4f}", f"{_m.inf:.4f}",
+            f"{0.7:.4f}", f"{0.4:.4f}", f"{_m.sqrt(1 - 0.49 - 0.16):.4f}", f"{0.03:.4f}", f"{0.03:.4f}",
+            f"{0.01:.4f}", f"{15.0:.4f}", f"{0.0:.4f}", f"{1.4:.4f}", f"{1.001:.4f}", f"{90.0:.4f}",
+            f"{532e-6:.4f}", f"{0.001:.4f}", "0", "1", "0", "1", f"{len(tissues)}"]
+    for mua, mus, g in tissues:
+        vals += [f"{mua:.4f}", f"{mus:.4f}", f"{g:.4f}"]
+    with open(path, "w") as f:
+        f.write("\n".join(vals) + "\n")
