@@ -38,7 +38,10 @@ constexpr float kFix = 4294967296.0f;     // 2^32
 constexpr double kUnfix = 1.0 / 4294967296.0;
 
 __device__ __forceinline__ unsigned long long to_fix(float v) {
-  return v > 0.f ? __float2ull_rn(v * kFix) : 0ull;
+  // below 2^32 the 32-bit conversion gives the same integer and is cheaper
+  const float t = v * kFix;
+  if (!(v > 0.f)) return 0ull;
+  return t < kFix ? (unsigned long long)__float2uint_rn(t) : __float2ull_rn(t);
 }
 
 // ----------------------------------------------------------------- Philox

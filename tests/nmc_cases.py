@@ -284,3 +284,23 @@ def write_notebook_mci(path: str, tissues, N: int = 200, d: float = 0.0005):
         vals += [f"{mua:.4f}", f"{mus:.4f}", f"{g:.4f}"]
     with open(path, "w") as f:
         f.write("\n".join(vals) + "\n")
+
+
+def example1_mus(n_runs: int = 10) -> list[float]:
+    """The scattering coefficients example1 cell 4 sweeps: n_runs log-spaced
+    values from 0.1 to 1e7 (its get_log_scale)."""
+    f = math.exp(math.log(1e7 / 0.1) / max(n_runs - 1, 1))
+    return [0.1 * f ** i for i in range(n_runs)]
+
+
+def write_example1_mci(path: str, mus: float, N: int = 200, d: float = 0.02):
+    """_H.mci exactly as example1 cell 3 writes it for one run of its sweep
+    (cell 2: homogeneous tissue 1, mua 10, g 0.9, point collimated source at
+    the origin (mcflag 4), boundaryflag 0, zsurf 0, n1 1.001, n2 1.4)."""
+    vals = [f"{1:.2f}", f"{N}", f"{N}", f"{N}", f"{d:.4f}", f"{d:.4f}", f"{d:.4f}", "4", "0", "0",
+            f"{0.0:.4f}", f"{0.0:.4f}", f"{0.0:.4f}", f"{0.0:.4f}", f"{0.0:.4f}", f"{1e12:.4f}",
+            f"{0.7:.4f}", f"{0.4:.4f}", f"{math.sqrt(1 - 0.49 - 0.16):.4f}", f"{1.0:.4f}", f"{1.0:.4f}",
+            f"{0.0:.4f}", f"{5.0:.4f}", f"{0.0:.4f}", f"{1.001:.4f}", f"{1.4:.4f}", f"{90.0:.4f}",
+            f"{640e-6:.4f}", f"{0.001:.4f}", "0", "1", "0", "1", "1", f"{10.0:.4f}", f"{mus:.4f}", f"{0.9:.4f}"]
+    with open(path, "w") as f:
+        f.write("\n".join(vals) + "\n")

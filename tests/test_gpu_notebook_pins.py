@@ -2,6 +2,9 @@
 sample notebooks (tests/golden/notebook_pins.json, extracted by
 tests/golden/make_notebook_fixture.py):
 
+  * example1: a homogeneous 200^3 cube (0.02 per voxel), point collimated
+    source, mua 10, mus swept over 0.1 ... 1e7, 1e5 photons per run, through
+    `nmc` on the reference's streams (within a tenth of a standard error).
   * example2: skin vessel, 200^3 voxels of 0.0005 cm, 532 nm, 1e6 photons,
     Total Rd = 0.26982540 on the reference's Metal build.  Run here through
     the `nmc` program with the reference's own random streams and dispatch
@@ -45,6 +48,26 @@ def test_example2_rd_through_the_nmc_program(gpu, tmp_path):
     print(f"example2: Rd {rep['Rd']:.8f} +- {rep['Rd_se']:.8f} vs notebook {pin['Rd']:.8f} (z={z:.2f}), "
           f"{rep['substeps_per_photon']:.0f} sub-steps/photon")
     assert abs(z) <= 3.0
+
+
+def test_example1_mus_sweep_through_the_nmc_program(gpu, tmp_path):
+    # 10 runs, mus 0.1 ... 1e7 (log-spaced), 1e5 photons each on the
+    # reference's streams.  With mua = 10 the photons stay within ~1 of the
+    # origin, where the reference's FP32 walk does not stall, so the engine
+    # follows the same photons: the recorded Rd comes back to a tenth of a
+    # standard error (5-6 significant digits) over five decades of Rd
+    name = str(tmp_path / "test")
+    mci.write_tissue(name, np.ones(200 ** 3, np.uint8))
+    for mus, pin in zip(cases.example1_mus(), PINS["example1"]["Rd"]):
+        cases.write_example1_mci(name + "_H.mci", mus)
+        p = mci.run_nmc(name, timeout=900)
+        assert p.returncode == 0, p.stdout[-2000:] + p.stderr[-2000:]
+        rep = json.load(open(name + "_report.json"))
+        assert rep["photons"] == 100000
+        print(f"mus {mus:.6g}: Rd {rep['Rd']:.6g} +- {rep['Rd_se']:.2g} vs notebook {pin:.6g}, "
+              f"{rep['substeps_per_photon']:.0f} sub-steps/photon")
+        assert abs(rep["Rd"] - pin) <= 0.1 * rep["Rd_se"] + 1e-8
+        assert abs(mci.read_rd(name) - pin) <= 2 * rep["Rd_se"] + 1e-4  # the _Rd.dat file, 4 decimals
 
 
 SHORT = [r for r in PINS["example3"] if r["nm"] <= 590]  # absorbed before they wander far
