@@ -304,3 +304,26 @@ def write_example1_mci(path: str, mus: float, N: int = 200, d: float = 0.02):
             f"{640e-6:.4f}", f"{0.001:.4f}", "0", "1", "0", "1", "1", f"{10.0:.4f}", f"{mus:.4f}", f"{0.9:.4f}"]
     with open(path, "w") as f:
         f.write("\n".join(vals) + "\n")
+
+
+def example0_params():
+    """RunParams and TissueParams as `nmc` reads them from example0's _H.mci
+    (cell 2: homogeneous 200^3 at 0.02, uniform beam of radius 1.2 at the
+    origin, boundaryflag 2, zsurf 0, mua 1, mus 100, g 0.9, n1 1.4, n2 1.001)."""
+    rp = abi.run_params(myname="test", Nx=200, Ny=200, Nz=200, dx=0.02, dy=0.02, dz=0.02, mcflag=0, launchflag=0,
+                        boundaryflag=2, xs=0.0, ys=0.0, zs=0.0, xfocus=0.0, yfocus=0.0, zfocus=1e12, ux0=0.7,
+                        uy0=0.4, uz0=0.5916, radius=1.2, waist=1.2, zsurf=0.0, det_radius=5.0, xd=0.0, n1=1.4,
+                        n2=1.001, na=90.0, lambda_=0.0006, lc=0.001, semiflag=1, det_state=0,
+                        mckernelflag=abi.SIM_MCXYZ, Nt=1)
+    return rp, abi.tissue_params(mua=[1.0], mus=[100.0], g=[0.9])
+
+
+def write_example0_mci(path: str):
+    """_H.mci exactly as example0 cell 3 writes it."""
+    vals = [f"{1.0:.2f}", "200", "200", "200", f"{0.02:.4f}", f"{0.02:.4f}", f"{0.02:.4f}", "0", "0", "2",
+            f"{0.0:.4f}", f"{0.0:.4f}", f"{0.0:.4f}", f"{0.0:.4f}", f"{0.0:.4f}", f"{1e12:.4f}",
+            f"{0.7:.4f}", f"{0.4:.4f}", f"{math.sqrt(1 - 0.49 - 0.16):.4f}", f"{1.2:.4f}", f"{1.2:.4f}",
+            f"{0.0:.4f}", f"{5.0:.4f}", f"{0.0:.4f}", f"{1.4:.4f}", f"{1.001:.4f}", f"{90.0:.4f}",
+            f"{640e-6:.4f}", f"{0.001:.4f}", "0", "1", "0", "1", "1", f"{1.0:.4f}", f"{100.0:.4f}", f"{0.9:.4f}"]
+    with open(path, "w") as f:
+        f.write("\n".join(vals) + "\n")

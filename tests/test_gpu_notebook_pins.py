@@ -2,6 +2,10 @@
 sample notebooks (tests/golden/notebook_pins.json, extracted by
 tests/golden/make_notebook_fixture.py):
 
+  * example0: a homogeneous 200^3 cube (0.02 per voxel), uniform beam of
+    radius 1.2, 1e5 photons on the reference's streams: the oracle's FP32
+    restatement reproduces the recorded Rd, and the engine follows the FP64
+    oracle, 0.85 % lower (the reference's FP32 face stall).
   * example1: a homogeneous 200^3 cube (0.02 per voxel), point collimated
     source, mua 10, mus swept over 0.1 ... 1e7, 1e5 photons per run, through
     `nmc` on the reference's streams (within a tenth of a standard error).
@@ -48,6 +52,36 @@ def test_example2_rd_through_the_nmc_program(gpu, tmp_path):
     print(f"example2: Rd {rep['Rd']:.8f} +- {rep['Rd_se']:.8f} vs notebook {pin['Rd']:.8f} (z={z:.2f}), "
           f"{rep['substeps_per_photon']:.0f} sub-steps/photon")
     assert abs(z) <= 3.0
+
+
+def test_example0_rd_and_the_reference_fp32_walk(gpu, oracle, tmp_path):
+    # uniform beam of radius 1.2 on a 200^3 x 0.02 cube: photons reach |x| ~ 1
+    # and beyond, where the reference's global FP32 coordinates stall at
+    # voxel faces (5.7e3 sub-steps per photon against 1.05e3).  On the
+    # reference's streams the FP32 restatement of the reference reproduces
+    # the recorded Rd; the engine follows the FP64 oracle photon for photon
+    # and the recorded value sits ~0.85 % above both
+    rp, tp = cases.example0_params()
+    v = np.ones(200 ** 3, np.uint8)
+    name = str(tmp_path / "test")
+    cases.write_example0_mci(name + "_H.mci")
+    mci.write_tissue(name, v)
+    pin = PINS["example0"]
+    n = pin["photons"]
+    p = mci.run_nmc(name, "--photons", str(n), timeout=900)
+    assert p.returncode == 0, p.stdout[-2000:] + p.stderr[-2000:]
+    rep = json.load(open(name + "_report.json"))
+    o = {bits: oracle.run(abi.SIM_MCXYZ, rp, tp, v, ext=abi.ext_defaults(rng=abi.RNG_TAUS_REF), n=n,
+                          real_bits=bits, tallies=False) for bits in (64, 32)}
+    rd = {bits: o[bits]["rd_sum"] / n for bits in o}
+    se = rep["Rd_se"]
+    print(f"example0: engine {rep['Rd']:.6f} ({rep['substeps_per_photon']:.0f} sub-steps/photon), FP64 oracle "
+          f"{rd[64]:.6f} ({o[64]['substeps'] / n:.0f}), FP32 oracle {rd[32]:.6f} ({o[32]['substeps'] / n:.0f}), "
+          f"notebook {pin['Rd']:.6f}, se {se:.6f}")
+    assert abs(rep["Rd"] - rd[64]) <= 0.25 * se
+    assert abs(rd[32] - pin["Rd"]) <= 0.25 * se
+    assert o[32]["substeps"] > 4 * o[64]["substeps"]
+    assert pin["Rd"] - rep["Rd"] >= 0.005 * pin["Rd"]
 
 
 def test_example1_mus_sweep_through_the_nmc_program(gpu, tmp_path):
