@@ -663,6 +663,52 @@ def run_cbs_workload(args) -> dict:
     }
 
 
+def run_layered_workload(args) -> dict:
+    """Layered media: a three-layer skin stack (epidermis 0.01 cm, dermis
+    0.2 cm, semi-infinite subcutis; mua 3 / 0.3 / 0.1, mus 200 / 150 / 100
+    /cm, g 0.8 / 0.85 / 0.9, n 1.4 / 1.4 / 1.44), normal pencil beam, Rd(r),
+    Tt(r), A(z) and per-layer absorption, 1e8 photons per call; the CPU
+    restatement of the same model times a bounded sample on the host cores."""
+    import torch
+
+    import nmc_cases as cases
+    from nmc_gb300 import build, layered
+
+    build.build()
+    torch.cuda.set_device(0)
+    n = args.photons if args.photons != PHOTONS_PER_STEP else 100_000_000
+    kw = dict(nr=100, dr=0.01, nz=100, dz=0.01, seed=11)
+    for _ in range(max(args.warmup, 1)):
+        layered.run(cases.LAYERED_SKIN3, 1_000_000, **kw)
+    best, r = None, None
+    for _ in range(max(args.steps, 1)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = layered.run(cases.LAYERED_SKIN3, n, **kw)
+        t = time.perf_counter() - t0
+        best = t if best is None else min(best, t)
+    out = {
+        "metric": "photons/s, layered mcsub (3-layer skin stack)", "unit": "photons/s", "value": n / best,
+        "seconds": best, "photons": n, "rd": r["rd"], "rd_se": r["rd_se"],
+        "interactions_per_photon": r["interactions"] / n, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "3 layers: 0.01 cm (mua 3, mus 200, g 0.8, n 1.4), 0.2 cm (0.3, 150, 0.85, 1.4), "
+                               "semi-infinite (0.1, 100, 0.9, 1.44); pencil beam; Rd(r), Tt(r) 100 x 0.01 cm, "
+                               "A(z) 100 x 0.01 cm",
+                   "timing": f"best of {max(args.steps, 1)} host-timed calls (allocation, launch, tally copies)"},
+    }
+    if not args.no_cpu:
+        from oracle import bindings as orc
+
+        threads = os.cpu_count() or 1
+        sample = 200_000
+        t0 = time.perf_counter()
+        orc.layered(cases.LAYERED_SKIN3, sample, real_bits=32, nthreads=threads, **kw)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": sample / dt, "unit": "photons/s", "cores": threads, "kind": "port",
+                               "sample": f"{sample} photons of the same stack, FP32 CPU restatement, {dt:.1f} s"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -679,7 +725,7 @@ def main():
                     help="autotune the launch shape on this many photons before the warm-up (0: defaults)")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warm-up and timed transport launches (for ncu)")
-    ap.add_argument("--workload", default="skinvessel", choices=["skinvessel", "sweep", "sweep_mcsub", "adjoint", "cbs"])
+    ap.add_argument("--workload", default="skinvessel", choices=["skinvessel", "sweep", "sweep_mcsub", "adjoint", "cbs", "layered"])
     args = ap.parse_args()
     if args.workload == "sweep":
         out = run_sweep_workload(args)
@@ -689,6 +735,8 @@ def main():
         out = run_adjoint_workload(args)
     elif args.workload == "cbs":
         out = run_cbs_workload(args)
+    elif args.workload == "layered":
+        out = run_layered_workload(args)
     else:
         out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if out:

@@ -70,6 +70,7 @@ struct LayParams {
   unsigned long long* a_z;   // nz + 1
   unsigned long long* a_rz;  // (nr + 1) * (nz + 1), or null
   unsigned long long* a_layer;  // nl
+  int smem_az;   // A(z) privatised in shared memory (nz + 1 bins after the layer sums)
   double* sums;  // NMC_LAY_FIELDS
   unsigned long long first, n;
   uint32_t k0, k1;
@@ -88,6 +89,14 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
   __shared__ LayDev s_lay[kMaxLayers];
   __shared__ double s_sum[NMC_LAY_FIELDS];
   __shared__ double s_grad[ADJ ? 3 * kMaxAdjLayers : 1];
+  // absorbed weight per layer, then (if it fits) A(z): block-private u64
+  // fixed-point sums, added to the global tallies once at the end; every
+  // interaction deposits, and a handful of global addresses would serialise
+  extern __shared__ unsigned long long s_tally[];
+  unsigned long long* const s_al = s_tally;
+  unsigned long long* const s_az = s_tally + P.nl;
+  const int n_priv = P.nl + (P.smem_az ? P.nz + 1 : 0);
+  for (int i = threadIdx.x; i < n_priv; i += blockDim.x) s_tally[i] = 0ull;
   for (int i = threadIdx.x; i < P.nl; i += blockDim.x) s_lay[i] = P.lay[i];
   if (threadIdx.x < NMC_LAY_FIELDS) s_sum[threadIdx.x] = 0.0;
   if (ADJ)
@@ -103,6 +112,8 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
     uint32_t hop = 0, ev = 0;
     bool alive = true;
     float rd = 0.f, tt = 0.f;
+    int dep_l = 0;        // the layer whose absorbed weight dep_w holds
+    float dep_w = 0.f;    // merged while the photon stays in one layer
     float aL[ADJ ? kMaxAdjLayers : 1], aN[ADJ ? kMaxAdjLayers : 1], aQ[ADJ ? kMaxAdjLayers : 1];
     float score = 0.f;
     if (ADJ)
@@ -169,8 +180,13 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
       if (absorb > 0.f) {
         const unsigned long long fa = to_fix(absorb);
         const int iz = min(max((int)(z * P.idz), 0), P.nz);
-        if (idx_ok(iz, (unsigned)P.nz + 1u, P.flags)) atomicAdd(P.a_z + iz, fa);
-        if (idx_ok(L, (unsigned)P.nl, P.flags)) atomicAdd(P.a_layer + L, fa);
+        if (idx_ok(iz, (unsigned)P.nz + 1u, P.flags)) atomicAdd((P.smem_az ? s_az : P.a_z) + iz, fa);
+        if (L != dep_l) {
+          if (dep_w > 0.f && idx_ok(dep_l, (unsigned)P.nl, P.flags)) atomicAdd(s_al + dep_l, to_fix(dep_w));
+          dep_l = L;
+          dep_w = 0.f;
+        }
+        dep_w += absorb;
         if (P.a_rz) {
           const int ir = min((int)(sqrtf(x * x + y * y) * P.idr), P.nr);
           if (idx_ok((size_t)ir * (P.nz + 1) + iz, (size_t)(P.nr + 1) * (P.nz + 1), P.flags))
@@ -193,6 +209,7 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
       }
       r = philox4x32_10(make_uint4(c0, c1, hop, kLayTag), P.k0, P.k1);
     }
+    if (dep_w > 0.f && idx_ok(dep_l, (unsigned)P.nl, P.flags)) atomicAdd(s_al + dep_l, to_fix(dep_w));
     atomicAdd(&s_sum[NMC_LAY_PHOTONS], 1.0);
     atomicAdd(&s_sum[NMC_LAY_RD], (double)rd);
     atomicAdd(&s_sum[NMC_LAY_RD2], (double)rd * (double)rd);
@@ -208,6 +225,10 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
       }
   }
   __syncthreads();
+  for (int i = threadIdx.x; i < n_priv; i += blockDim.x) {
+    const unsigned long long v = s_tally[i];
+    if (v) atomicAdd(i < P.nl ? P.a_layer + i : P.a_z + (i - P.nl), v);
+  }
   if (ADJ)
     for (int i = threadIdx.x; i < 3 * P.nl; i += blockDim.x) {
       const int k = i / P.nl, l = i % P.nl;
@@ -328,15 +349,18 @@ nmc_status layered_impl(int32_t device, const nmc_layered_config* cfg, const nmc
   const bool fast = !(c.flags & NMC_FLAG_PRECISE_MATH);
   const void* f = adj ? (fast ? (const void*)layered_kernel<true, true> : (const void*)layered_kernel<false, true>)
                       : (fast ? (const void*)layered_kernel<true, false> : (const void*)layered_kernel<false, false>);
+  // A(z) joins the per-layer sums in shared memory while both fit in 16 KB
+  P.smem_az = (size_t)(c.n_layers + nz1) * 8 <= 16384 ? 1 : 0;
+  const size_t smem = (size_t)(c.n_layers + (P.smem_az ? nz1 : 0)) * 8;
   int per_sm = 0, nsm = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, 256, 0) != cudaSuccess || per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, 256, smem) != cudaSuccess || per_sm < 1)
     return done(NMC_EDEVICE);
   const unsigned long long grid =
       std::max<unsigned long long>(1, std::min<unsigned long long>((unsigned long long)nsm * per_sm,
                                                                    (photons + 255) / 256));
   void* args[] = {(void*)&P};
-  if (photons > 0 && cudaLaunchKernel(f, dim3((unsigned)grid), dim3(256), args, 0, st) != cudaSuccess)
+  if (photons > 0 && cudaLaunchKernel(f, dim3((unsigned)grid), dim3(256), args, smem, st) != cudaSuccess)
     return done(NMC_EDEVICE);
   std::vector<unsigned long long> hrd(nr1), htt(nr1), haz(nz1), hal(c.n_layers), harz(a_rz ? nr1 * nz1 : 0);
   std::vector<double> hgrad(adj ? 3 * c.n_layers : 0);

@@ -344,10 +344,10 @@ R tt_costheta(G& rng, const TTq<R>& q, R gf, R af, R gb, R ab, R cc) {
 }
 
 // psi sample and the new direction (kernels.metal:255-279, :706-730).
-template <class R, class G>
-void spin(G& rng, R costheta, R& ux, R& uy, R& uz) {
+template <class R>
+void spin_u(R costheta, R u_psi, R& ux, R& uy, R& uz) {
   const R sintheta = std::sqrt(R(1) - costheta * costheta);
-  const R psi = R(2.0 * kPI) * rng.template u<R>(D_PSI);
+  const R psi = R(2.0 * kPI) * u_psi;
   const R cospsi = std::cos(psi);
   const R sinpsi = psi < R(kPI) ? std::sqrt(R(1) - cospsi * cospsi)
                                 : -std::sqrt(R(1) - cospsi * cospsi);
@@ -365,6 +365,11 @@ void spin(G& rng, R costheta, R& ux, R& uy, R& uz) {
   ux = uxx;
   uy = uyy;
   uz = uzz;
+}
+
+template <class R, class G>
+void spin(G& rng, R costheta, R& ux, R& uy, R& uz) {
+  spin_u<R>(costheta, rng.template u<R>(D_PSI), ux, uy, uz);
 }
 
 // Replays a fixed list of uniforms (used by the sampler entry points).
@@ -922,6 +927,139 @@ bool valid_inputs(const Cfg& c) {
   return true;
 }
 
+// ------------------------------------------------------------ layered media
+// The multi-layer extension of the mcsub kernel behind nmc_layered_run.  The
+// reference declares MAXLAYERS = 100 (definitions.h:24) and never uses it, so
+// this restates the engine's own model, which keeps the mcsub kernel's
+// physics (kernels.metal:59-319) in every layer:
+//   HOP    s = -ln(xi) / mu_t of the current layer; a step that reaches a
+//          layer boundary stops there and the rest of the dimensionless step
+//          carries into the next layer;
+//   CROSS  Fresnel reflection R(n_i, n_t, |uz|) (helpers.metal:243-291) by a
+//          random draw, as the mcsub kernel does at its surface
+//          (kernels.metal:183-214); otherwise refraction (Snell) into the
+//          next layer, or escape into the ambient medium (Rd(r) above,
+//          Tt(r) below);
+//   DROP   absorb = W mua / mu_t (kernels.metal:224-234);
+//   SPIN   Henyey-Greenstein with the layer's g (kernels.metal:244-279);
+//   ROULETTE below 1e-4, chance 0.1 (kernels.metal:289-294).
+// Random numbers, as the engine draws them: Philox4x32-10, key (seed lo,
+// seed hi), counter (photon lo, photon hi, interaction, 'LAYR'): x step,
+// y cos theta, z psi, w roulette; boundary events draw their Fresnel choice
+// from counter (photon lo, photon hi, event | 2^31, 'LAYR').
+constexpr uint32_t kLayTag = 0x4C415952u;
+constexpr uint32_t kLayStepCap = 20000000u;
+
+struct LayTally {
+  std::vector<double> rd, tt, az, al;
+  double s[NMC_LAY_FIELDS] = {};
+  bool capped = false;
+};
+
+struct LayGeom {
+  nmc_layered_config c;
+  std::vector<nmc_layer> lay;
+  std::vector<double> z0, z1;  // z1 = +inf for a semi-infinite last layer
+  double w0;
+};
+
+template <class R>
+void layered_photon(const LayGeom& G, uint64_t pid, LayTally& T) {
+  const uint32_t c0 = (uint32_t)pid, c1 = (uint32_t)(pid >> 32);
+  const uint32_t k0 = (uint32_t)G.c.seed, k1 = (uint32_t)(G.c.seed >> 32);
+  auto block = [&](uint32_t c2, uint32_t* out) {
+    uint32_t q[4] = {c0, c1, c2, kLayTag};
+    philox10(q, k0, k1);
+    std::memcpy(out, q, sizeof q);
+  };
+  auto u = [](uint32_t x) { return R(x >> 9) * R(1.0 / 8388608.0) + R(1.0 / 16777216.0); };
+  const int nl = G.c.n_layers, nr = G.c.nr, nz = G.c.nz;
+  const R idr = R(1) / R(G.c.dr), idz = R(1) / R(G.c.dz);
+  R x = 0, y = 0, z = 0, ux = 0, uy = 0, uz = 1, w = R(G.w0), sleft = 0, rd = 0, tt = 0;
+  int L = 0;
+  uint32_t hop = 0, ev = 0;
+  bool alive = true;
+  uint32_t r[4];
+  block(0u, r);
+  while (alive) {
+    const nmc_layer& Ly = G.lay[L];
+    const R mut = R(Ly.mua) + R(Ly.mus);
+    if (sleft <= R(0)) sleft = -std::log(u(r[0]));
+    const R db = uz > R(0) ? (R(G.z1[L]) - z) / uz : (uz < R(0) ? (R(G.z0[L]) - z) / uz : R(INFINITY));
+    const R s = mut > R(0) ? sleft / mut : R(INFINITY);
+    if (s >= db) {  // CROSS
+      x += db * ux;
+      y += db * uy;
+      z = uz > R(0) ? R(G.z1[L]) : R(G.z0[L]);
+      if (mut > R(0)) sleft = std::max(sleft - db * mut, R(0));
+      const bool down = uz > R(0);
+      const int Ln = down ? L + 1 : L - 1;
+      const R nt = Ln < 0 ? R(G.c.n_above) : (Ln >= nl ? R(G.c.n_below) : R(G.lay[Ln].n));
+      R uzt = 0;
+      const R Rf = rfresnel<R>(R(Ly.n), nt, std::fabs(uz), &uzt);
+      uint32_t a[4];
+      block(ev | 0x80000000u, a);
+      ++ev;
+      if (u(a[0]) <= Rf) {
+        uz = -uz;
+      } else if (Ln < 0 || Ln >= nl) {  // escapes
+        const int ir = std::min((int)(std::sqrt(x * x + y * y) * idr), nr);
+        if (Ln < 0) {
+          if (!T.rd.empty()) T.rd[ir] += (double)w;
+          rd += w;
+        } else {
+          if (!T.tt.empty()) T.tt[ir] += (double)w;
+          tt += w;
+        }
+        alive = false;
+      } else {  // refracted (Snell)
+        const R ratio = R(Ly.n) / nt;
+        ux *= ratio;
+        uy *= ratio;
+        uz = down ? uzt : -uzt;
+        L = Ln;
+      }
+      if (ev > kLayStepCap) {
+        T.capped = true;
+        alive = false;
+      }
+      continue;
+    }
+    // interaction inside the layer: HOP, DROP, SPIN, ROULETTE
+    x += s * ux;
+    y += s * uy;
+    z += s * uz;
+    sleft = 0;
+    const R absorb = w * R(Ly.mua) / mut;
+    w -= absorb;
+    if (absorb > R(0)) {
+      const int iz = std::min(std::max((int)(z * idz), 0), nz);
+      if (!T.az.empty()) T.az[iz] += (double)absorb;
+      T.al[L] += (double)absorb;
+    }
+    const R cth = hg_costheta<R>(R(Ly.g), u(r[1]));
+    spin_u<R>(cth, u(r[2]), ux, uy, uz);
+    if (w < R(kTHRESHOLD)) {
+      if (u(r[3]) <= R(kCHANCE))
+        w /= R(kCHANCE);
+      else
+        alive = false;
+    }
+    ++hop;
+    if (hop > kLayStepCap) {
+      T.capped = true;
+      alive = false;
+    }
+    block(hop, r);
+  }
+  T.s[NMC_LAY_PHOTONS] += 1.0;
+  T.s[NMC_LAY_RD] += (double)rd;
+  T.s[NMC_LAY_RD2] += (double)rd * (double)rd;
+  T.s[NMC_LAY_TT] += (double)tt;
+  T.s[NMC_LAY_TT2] += (double)tt * (double)tt;
+  T.s[NMC_LAY_INTERACTIONS] += (double)hop;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1019,6 +1157,70 @@ double orc_tt_costheta(double gf, double af, double gb, double ab, double cc, do
 }
 
 double orc_hg_costheta(double g, double u) { return hg_costheta<double>(g, u); }
+
+int orc_layered_run(int real_bits, const nmc_layered_config* cfg, const nmc_layer* layers, uint64_t first,
+                    uint64_t n, int nthreads, double* out, double* rd_r, double* tt_r, double* a_z,
+                    double* a_layer) {
+  if (!cfg || !layers || !out || (real_bits != 32 && real_bits != 64)) return NMC_EINVAL;
+  LayGeom G;
+  G.c = *cfg;
+  const nmc_layered_config& c = G.c;
+  if (c.n_layers < 1 || c.n_layers > 100 || c.nr < 1 || c.nz < 1 || !(c.dr > 0.f) || !(c.dz > 0.f) ||
+      !(c.n_above > 0.f) || !(c.n_below > 0.f))
+    return NMC_EINVAL;
+  double zc = 0.0;
+  for (int i = 0; i < c.n_layers; ++i) {
+    const nmc_layer& q = layers[i];
+    const bool last = i == c.n_layers - 1;
+    if (!(q.mua >= 0.f) || !(q.mus >= 0.f) || !(q.g > -1.f) || !(q.g < 1.f) || !(q.n > 0.f) ||
+        !(q.thickness > 0.f) || (!last && !std::isfinite(q.thickness)) ||
+        (!std::isfinite(q.thickness) && !(q.mua + q.mus > 0.f)))
+      return NMC_EINVAL;
+    G.lay.push_back(q);
+    G.z0.push_back(zc);
+    zc += q.thickness;
+    G.z1.push_back(std::isfinite(q.thickness) ? zc : INFINITY);
+  }
+  const double rs = ((double)c.n_above - layers[0].n) / ((double)c.n_above + layers[0].n);
+  const double rsp = rs * rs;
+  G.w0 = 1.0 - rsp;
+  if (nthreads < 1) nthreads = 1;
+  if ((uint64_t)nthreads > n) nthreads = n ? (int)n : 1;
+  std::vector<LayTally> T(nthreads);
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; ++t) {
+    const uint64_t lo = n * t / nthreads, hi = n * (t + 1) / nthreads;
+    th.emplace_back([&, t, lo, hi] {
+      LayTally& tl = T[t];
+      if (rd_r) tl.rd.assign((size_t)c.nr + 1, 0.0);
+      if (tt_r) tl.tt.assign((size_t)c.nr + 1, 0.0);
+      if (a_z) tl.az.assign((size_t)c.nz + 1, 0.0);
+      tl.al.assign((size_t)c.n_layers, 0.0);
+      for (uint64_t i = lo; i < hi; ++i) {
+        if (real_bits == 64)
+          layered_photon<double>(G, first + i, tl);
+        else
+          layered_photon<float>(G, first + i, tl);
+      }
+    });
+  }
+  for (auto& x : th) x.join();
+  bool capped = false;
+  for (int t = 0; t < nthreads; ++t) {
+    const LayTally& tl = T[t];
+    for (int k = 0; k < NMC_LAY_FIELDS; ++k) out[k] += tl.s[k];
+    for (size_t k = 0; k < tl.rd.size(); ++k) rd_r[k] += tl.rd[k];
+    for (size_t k = 0; k < tl.tt.size(); ++k) tt_r[k] += tl.tt[k];
+    for (size_t k = 0; k < tl.az.size(); ++k) a_z[k] += tl.az[k];
+    for (int k = 0; k < c.n_layers; ++k) {
+      out[NMC_LAY_A] += tl.al[k];
+      if (a_layer) a_layer[k] += tl.al[k];
+    }
+    capped = capped || tl.capped;
+  }
+  out[NMC_LAY_SPECULAR] += rsp * (double)n;
+  return capped ? NMC_ESTEPCAP : 0;
+}
 
 // The speckle mutual-interference post-processing of -[MetalMC
 // getComputeResults:] (MetalMC.m:628-742), restated with the reference's

@@ -63,6 +63,13 @@ double orc_tt_costheta(double gf, double af, double gb, double ab, double cc,
 /* Henyey-Greenstein cos(theta) sample (kernels.metal:696-703) in double. */
 double orc_hg_costheta(double g, double u);
 
+/* The engine's multi-layer model (nmc_layered_run) restated on the CPU, same
+ * Philox layout; out (NMC_LAY_FIELDS) and the tallies are added to (+=) and
+ * may be NULL except out.  Returns 0, NMC_EINVAL or NMC_ESTEPCAP. */
+int orc_layered_run(int real_bits, const nmc_layered_config* cfg, const nmc_layer* layers, uint64_t first,
+                    uint64_t n, int nthreads, double* out, double* rd_r, double* tt_r, double* a_z,
+                    double* a_layer);
+
 /* MetalMC.m:628-742 speckle mutual interference (see nmc_speckle_mutual). */
 void orc_speckle_mutual(int nx, int ny, const float* maps, const nmc_speckle* rec, const int32_t* counts,
                         int kmax, float lambda, float lc, float* out);

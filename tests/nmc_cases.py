@@ -327,3 +327,8 @@ def write_example0_mci(path: str):
             f"{640e-6:.4f}", f"{0.001:.4f}", "0", "1", "0", "1", "1", f"{1.0:.4f}", f"{100.0:.4f}", f"{0.9:.4f}"]
     with open(path, "w") as f:
         f.write("\n".join(vals) + "\n")
+
+
+# Three-layer skin stack for the layered model: (mua, mus, g, n, thickness),
+# cm^-1 and cm: epidermis 0.01, dermis 0.2, semi-infinite subcutis.
+LAYERED_SKIN3 = [(3.0, 200.0, 0.8, 1.4, 0.01), (0.3, 150.0, 0.85, 1.4, 0.2), (0.1, 100.0, 0.9, 1.44, math.inf)]

@@ -1,0 +1,43 @@
+"""The oracle's restatement of the layered model (orc_layered_run) against
+closed forms, on the CPU: a clear absorbing slab transmits exp(-mua d) of
+the weight (Beer-Lambert), a clear non-absorbing slab between two index
+steps transmits (1 - r)/(1 + r) (incoherent multiple reflections), and
+weight is conserved up to Russian roulette."""
+import math
+
+import numpy as np
+
+
+def test_beer_lambert_slab(oracle):
+    n = 40_000
+    r = oracle.layered([(2.0, 0.0, 0.0, 1.0, 0.3)], n, n_above=1.0, n_below=1.0, seed=3)
+    t = math.exp(-2.0 * 0.3)
+    se = math.sqrt(t * (1 - t) / n)
+    assert r["specular"] == 0.0 and r["rd"] == 0.0
+    assert abs(r["tt"] - t) <= 4 * se
+    assert abs(r["A"] / n - (1 - t)) <= 4 * se
+
+
+def test_fresnel_slab(oracle):
+    # normal incidence; the photon never turns, so every pass is a Fresnel
+    # draw: T = (1 - r)^2 / (1 - r^2) of the launched unit weight
+    n = 40_000
+    r = oracle.layered([(0.0, 0.0, 0.0, 1.5, 0.1)], n, n_above=1.0, n_below=1.0, seed=4)
+    rf = (0.5 / 2.5) ** 2
+    w0 = 1 - rf
+    t = (1 - rf) / (1 + rf)  # of the incident weight, specular included
+    assert abs(r["specular"] / n - rf) <= 1e-12
+    p = t / w0  # probability that a launched photon leaves through the bottom
+    se = math.sqrt(p * (1 - p) / n) * w0
+    assert abs(r["tt"] - t) <= 4 * se
+    assert abs(r["rd"] + r["tt"] - w0) <= 1e-6
+
+
+def test_weight_conserved(oracle):
+    n = 20_000
+    lay = [(3.0, 200.0, 0.8, 1.4, 0.01), (0.3, 150.0, 0.85, 1.4, 0.2), (0.1, 100.0, 0.9, 1.44, math.inf)]
+    r = oracle.layered(lay, n, nr=20, dr=0.05, nz=20, dz=0.02, seed=9)
+    total = (r["specular"] + r["Rd"] + r["Tt"] + r["A"]) / n
+    assert abs(total - 1.0) <= 0.01  # roulette is unbiased, not exact
+    assert np.isclose(r["rd_r"].sum(), r["Rd"]) and np.isclose(r["a_z"].sum(), r["A"])
+    assert np.isclose(r["a_layer"].sum(), r["A"]) and r["tt"] == 0.0

@@ -1,9 +1,11 @@
 """Layered media (layered.cu).  No reference semantics exist for more than
-one layer (MAXLAYERS is declared, definitions.h:24, but unused), so the
-checks are the ones the physics fixes: one semi-infinite layer equals the
-mcsub kernel; a layer split in two equals the whole; a clear absorbing slab
-follows Beer-Lambert; a clear non-absorbing slab follows the Fresnel
-multiple-reflection sums; weight is conserved."""
+one layer (MAXLAYERS is declared, definitions.h:24, but unused).  The
+engine follows the oracle's CPU restatement of the same model on the same
+Philox streams, photon for photon, and the checks the physics fixes hold:
+one semi-infinite layer equals the mcsub kernel; a layer split in two equals
+the whole; a clear absorbing slab follows Beer-Lambert; a clear
+non-absorbing slab follows the Fresnel multiple-reflection sums; weight is
+conserved."""
 import math
 
 import numpy as np
@@ -13,6 +15,32 @@ from nmc_gb300 import abi
 import nmc_cases as cases
 
 pytestmark = pytest.mark.gpu
+
+SKIN3 = cases.LAYERED_SKIN3
+SLABS = [(0.5, 80.0, 0.9, 1.33, 0.05), (2.0, 30.0, 0.0, 1.5, 0.02), (0.2, 120.0, 0.7, 1.37, 0.1)]
+
+
+@pytest.mark.parametrize("layers,n_below", [(SKIN3, 1.0), (SLABS, 1.2)], ids=["skin3", "finite_slabs"])
+def test_layered_follows_the_oracle(gpu, oracle, layers, n_below):
+    # same Philox streams: the FP32 engine and the FP64 restatement follow the
+    # same photons, so their sums agree far inside the statistical error
+    from nmc_gb300 import layered
+
+    n = 200_000
+    kw = dict(n_above=1.0, n_below=n_below, nr=40, dr=0.02, nz=40, dz=0.01, seed=5, first=1000)
+    g = layered.run(layers, n, **kw)
+    o = oracle.layered(layers, n, **kw)
+    print(f"Rd {g['rd']:.6f} / {o['rd']:.6f}, Tt {g['tt']:.6f} / {o['tt']:.6f}, A {g['A'] / n:.6f} / "
+          f"{o['A'] / n:.6f}, interactions {g['interactions']:.0f} / {o['interactions']:.0f}")
+    assert g["photons"] == o["photons"] == n
+    assert abs(g["specular"] - o["specular"]) <= 1e-9 * n
+    for k in ("rd", "tt"):
+        assert abs(g[k] - o[k]) <= 0.05 * g[k + "_se"] + 1e-9
+    assert abs(g["A"] - o["A"]) <= 1e-3 * o["A"]
+    assert abs(g["interactions"] - o["interactions"]) <= 1e-3 * o["interactions"]
+    np.testing.assert_allclose(g["a_layer"], o["a_layer"], rtol=2e-3, atol=1e-6 * n)
+    for t in ("rd_r", "tt_r", "a_z"):
+        assert np.abs(g[t] - o[t]).sum() <= 5e-3 * max(o[t].sum(), 1e-9) + 1e-6 * n, t
 
 
 def test_single_layer_equals_mcsub(gpu):
