@@ -21,7 +21,9 @@ def main(ref_root):
     load = lambda n: json.load(open(os.path.join(d, n)))  # noqa: E731
     pins = {}
     t0 = "".join(outputs(load("example0.ipynb")))
-    pins["example0"] = {"Rd": float(re.findall(r"Total Rd = ([0-9.]+)", t0)[0]), "photons": 100000}
+    fit = re.findall(r"a = ([0-9.e+-]+), b = ([0-9.]+) 1/mm", t0)[0]
+    pins["example0"] = {"Rd": float(re.findall(r"Total Rd = ([0-9.]+)", t0)[0]), "photons": 100000,
+                        "a": float(fit[0]), "b": float(fit[1])}
     t1 = "".join(outputs(load("example1.ipynb")))
     pins["example1"] = {"Rd": [float(v) for v in re.findall(r"Total Rd = ([0-9.]+)", t1)]}
     t2 = "".join(outputs(load("example2.ipynb")))

@@ -72,7 +72,7 @@ def test_example0_rd_and_the_reference_fp32_walk(gpu, oracle, tmp_path):
     assert p.returncode == 0, p.stdout[-2000:] + p.stderr[-2000:]
     rep = json.load(open(name + "_report.json"))
     o = {bits: oracle.run(abi.SIM_MCXYZ, rp, tp, v, ext=abi.ext_defaults(rng=abi.RNG_TAUS_REF), n=n,
-                          real_bits=bits, tallies=False) for bits in (64, 32)}
+                          real_bits=bits, tallies=True) for bits in (64, 32)}
     rd = {bits: o[bits]["rd_sum"] / n for bits in o}
     se = rep["Rd_se"]
     print(f"example0: engine {rep['Rd']:.6f} ({rep['substeps_per_photon']:.0f} sub-steps/photon), FP64 oracle "
@@ -82,6 +82,26 @@ def test_example0_rd_and_the_reference_fp32_walk(gpu, oracle, tmp_path):
     assert abs(rd[32] - pin["Rd"]) <= 0.25 * se
     assert o[32]["substeps"] > 4 * o[64]["substeps"]
     assert pin["Rd"] - rep["Rd"] >= 0.005 * pin["Rd"]
+    # the notebook's fit of the on-axis fluence, phi(z) = a exp(-b z) over
+    # z <= 1.3 (example0 cell 8), from _F.bin as cell 6 reads it
+    fits = {"engine": _example0_axis_fit(mci.read_fluence(name, rp))}
+    for bits in (64, 32):
+        fits[bits] = _example0_axis_fit((o[bits]["F3D"] / (0.02 ** 3 * n * 1.0)).astype(np.float32))
+    print("example0 axis fit (a, b):", fits, "notebook", (pin["a"], pin["b"]))
+    assert abs(fits["engine"][1] - fits[64][1]) <= 0.01 * fits[64][1]
+    assert abs(fits["engine"][0] - fits[64][0]) <= 0.03 * fits[64][0]
+    assert fits[32][1] - fits[64][1] >= 0.02 * fits[64][1]  # the stall steepens the decay
+    assert pin["b"] - fits["engine"][1] >= 0.02 * pin["b"]
+
+
+def _example0_axis_fit(F):
+    Fz = (np.asarray(F, np.float32).reshape(200, 200, 200) / 1e5 * 0.02 * 0.02 * 0.02)[:, 100, 100]
+    z = np.arange(1, 201) * 0.02
+    i2 = int(np.searchsorted(z, 1.3, side="right"))
+    zf, ff = z[:i2 + 1], Fz[:i2 + 1]
+    ok = ff > 0
+    c = np.polyfit(zf[ok], np.log(ff[ok]), 1)
+    return float(math.exp(c[1])), float(-c[0])
 
 
 def test_example1_mus_sweep_through_the_nmc_program(gpu, tmp_path):
