@@ -77,8 +77,9 @@ struct XyzParams {
   // batched sweep over tissue tables (one table per set, e.g. per wavelength)
   const float4* sw_core;               // n_sets * NMC_NTISS (mua, mus, 1/mus, g)
   const PhaseConst* sw_phase;          // n_sets * NMC_NTISS
-  const unsigned long long* sw_prefix; // n_sets + 1 budget prefix sums
-  const unsigned long long* sw_first;  // id of each set's first photon
+  const unsigned long long* sw_prefix; // n_sets + 1 budget prefix sums, in queue order
+  const unsigned long long* sw_first;  // id of each queue slot's first photon
+  const unsigned int* sw_order;        // the set each queue slot runs
   XyzSweepSums* sw_sums;               // n_sets
   int sw_nsets;
 };
@@ -110,15 +111,16 @@ enum SubPhase { kPhaseHG = 0, kPhaseIsoRef = 1, kPhaseTT = 2 };
 
 // One parameter set of a batched sweep, as the kernel reads it.
 struct __align__(16) SweepSetDev {
-  float mut, albedo, n1, n2, rsp, pad;
+  float mut, albedo, n1, n2, rsp;
+  unsigned int id;           // the set's index (its key offset and its tallies)
   unsigned long long first;  // id of the set's first photon
   PhaseConst ph;
 };
 
 struct SweepParams {
   int nsets;
-  const SweepSetDev* sets;
-  const unsigned long long* prefix;  // nsets + 1 prefix sums of the budgets
+  const SweepSetDev* sets;           // in queue order
+  const unsigned long long* prefix;  // nsets + 1 prefix sums of the budgets, in queue order
   unsigned long long total;
   int bins;
   float idr;

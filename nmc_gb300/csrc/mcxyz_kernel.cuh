@@ -323,15 +323,15 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
       }
       if (score) D = 0.f;
       unsigned long long pid = P.first + pidx;
-      if (SW) {  // the set whose budget holds this photon: last s with prefix[s] <= pidx
+      if (SW) {  // the queue slot whose budget holds this photon: last k with prefix[k] <= pidx
         unsigned int lo = 0, hi = (unsigned int)P.sw_nsets;
         while (hi - lo > 1) {
           const unsigned int mid = (lo + hi) >> 1;
           if (__ldg(P.sw_prefix + mid) <= pidx) lo = mid; else hi = mid;
         }
-        set = lo;
+        set = __ldg(P.sw_order + lo);
         sbase = set * NMC_NTISS;
-        pid = __ldg(P.sw_first + set) + (pidx - __ldg(P.sw_prefix + set));
+        pid = __ldg(P.sw_first + lo) + (pidx - __ldg(P.sw_prefix + lo));
         k1 = P.rng.k1 + set;
       }
       slot = (unsigned int)(pid % P.nslots);

@@ -50,6 +50,7 @@ struct nmc_handle {
   nmc_tissue_params tp{};
   bool prepared = false;
   uint32_t tiss_used = 0;  // bit t: tissue t occurs in the map
+  uint64_t tiss_count[NMC_NTISS] = {};  // voxels of each tissue id in the map
   std::string err;
   int32_t run = 1;
   cudaStream_t stream = nullptr;
@@ -209,7 +210,7 @@ nmc_status validate(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue_pa
   if (rp->boundaryflag < 0 || rp->boundaryflag > 2) return fail(h, NMC_EINVAL, "boundaryflag must be 0, 1 or 2");
   if (rp->det_state != 0 && rp->det_state != 1) return fail(h, NMC_EINVAL, "det_state must be 0 or 1");
   if (!(rp->n1 > 0.f) || !(rp->n2 > 0.f)) return fail(h, NMC_EINVAL, "n1, n2 must be > 0");
-  bool used[NMC_NTISS] = {false};
+  uint64_t count[NMC_NTISS] = {};
   const size_t n = (size_t)rp->Nx * rp->Ny * rp->Nz;
   for (size_t k = 0; k < n; ++k) {
     if (v[k] >= NMC_NTISS) {
@@ -217,13 +218,16 @@ nmc_status validate(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue_pa
       std::snprintf(msg, sizeof msg, "tissue id %u at voxel %zu exceeds %d", (unsigned)v[k], k, NMC_NTISS - 1);
       return fail(h, NMC_EINVAL, msg);
     }
-    used[v[k]] = true;
+    ++count[v[k]];
   }
   uint32_t mask = 0;
   for (int t = 0; t < NMC_NTISS; ++t)
-    if (used[t]) mask |= 1u << t;
+    if (count[t]) mask |= 1u << t;
   nmc_status st = check_tissues(h, tp, mask, -1);
-  if (st == NMC_OK) h->tiss_used = mask;
+  if (st == NMC_OK) {
+    h->tiss_used = mask;
+    std::copy(count, count + NMC_NTISS, h->tiss_count);
+  }
   return st;
 }
 
@@ -846,7 +850,17 @@ nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_set
   const int bins = h->ext.sub_bins, nJ = bins + 1;
   std::vector<nmc::SweepSetDev> hs(n_sets);
   std::vector<unsigned long long> prefix(n_sets + 1, 0ull);
-  for (int s = 0; s < n_sets; ++s) {
+  // queue order: decreasing estimated cost per photon, mu_t / mu_a (the
+  // interactions before the weight decays); results do not depend on it
+  std::vector<uint32_t> order(n_sets);
+  for (int s = 0; s < n_sets; ++s) order[s] = (uint32_t)s;
+  auto est = [&](uint32_t s) {  // invalid sets are rejected below; keep the ordering strict
+    const double a = sets[s].mua, b = sets[s].mus, e = (a + b) / std::max(a, 1e-6);
+    return std::isfinite(e) ? e : 0.0;
+  };
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return est(a) > est(b); });
+  for (int k = 0; k < n_sets; ++k) {
+    const int s = (int)order[k];
     const nmc_sweep_set& q = sets[s];
     const float vals[] = {q.mua, q.mus, q.g, q.gf, q.af, q.gb, q.ab, q.cc, q.n1, q.n2};
     for (float v : vals)
@@ -862,8 +876,9 @@ nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_set
     tp.gb[1] = q.gb;
     tp.ab[1] = q.ab;
     tp.CC[1] = q.cc;
-    nmc::SweepSetDev& d = hs[s];
+    nmc::SweepSetDev& d = hs[k];
     d = nmc::SweepSetDev{};
+    d.id = (unsigned int)s;
     d.mut = q.mua + q.mus;
     d.albedo = q.mus / d.mut;
     d.n1 = q.n1;
@@ -873,7 +888,7 @@ nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_set
     d.rsp = t * t;
     d.first = q.first_photon;
     d.ph = nmc::phase_const(tp, 1);
-    prefix[s + 1] = prefix[s] + q.photons;
+    prefix[k + 1] = prefix[k] + q.photons;
   }
   nmc::SweepParams p{};
   p.nsets = n_sets;
@@ -982,6 +997,15 @@ nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables,
   std::vector<float4> core(nt);
   std::vector<nmc::PhaseConst> phase(nt);
   std::vector<unsigned long long> prefix(n_sets + 1, 0ull), first(n_sets, 0ull);
+  // The work queue hands out the sets in decreasing order of an estimated
+  // cost per photon, so that the long-lived photons of the costliest sets
+  // start first and the launch does not end waiting on them.  Estimate:
+  // sub-steps along a photon's path grow with (mus + 1/d) / mua in the
+  // tissues it crosses, weighted by each tissue's share of the map.  The
+  // order changes no result: a photon's stream is a function of its set and
+  // its index within the set, and the tallies are integer sums.
+  std::vector<double> cost(n_sets, 0.0);
+  const double inv_d = 1.0 / std::min(h->rp.dx, std::min(h->rp.dy, h->rp.dz));
   for (int s = 0; s < n_sets; ++s) {
     if ((st = check_tissues(h, &tables[s], h->tiss_used, s)) != NMC_OK) return st;
     nmc::XyzParams tmp{};
@@ -989,16 +1013,26 @@ nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables,
     for (int t = 0; t < NMC_NTISS; ++t) {
       core[(size_t)s * NMC_NTISS + t] = tmp.core[t];
       phase[(size_t)s * NMC_NTISS + t] = tmp.phase[t];
+      if (h->tiss_count[t])
+        cost[s] += (double)h->tiss_count[t] * ((double)tables[s].musv[t] + inv_d) /
+                   std::max((double)tables[s].muav[t], 1e-6);
     }
-    if (first_photon) first[s] = first_photon[s];
-    prefix[s + 1] = prefix[s] + photons[s];
+  }
+  std::vector<uint32_t> order(n_sets);
+  for (int s = 0; s < n_sets; ++s) order[s] = (uint32_t)s;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
+  for (int k = 0; k < n_sets; ++k) {  // queue slot k runs set order[k]
+    if (first_photon) first[k] = first_photon[order[k]];
+    prefix[k + 1] = prefix[k] + photons[order[k]];
   }
   nmc::XyzParams p = h->xp;
   const size_t b_core = sizeof(float4) * nt, b_ph = sizeof(nmc::PhaseConst) * nt, b_pre = 8 * (n_sets + 1),
-               b_first = 8 * (size_t)n_sets, b_sums = sizeof(nmc::XyzSweepSums) * n_sets;
+               b_first = 8 * (size_t)n_sets, b_sums = sizeof(nmc::XyzSweepSums) * n_sets,
+               b_order = 4 * (size_t)n_sets;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   char* base = nullptr;
-  NMC_CUDA(h, cudaMalloc((void**)&base, al(b_core) + al(b_ph) + al(b_pre) + al(b_first) + al(b_sums)));
+  NMC_CUDA(h, cudaMalloc((void**)&base,
+                         al(b_core) + al(b_ph) + al(b_pre) + al(b_first) + al(b_sums) + al(b_order)));
   char* cur = base;
   auto take = [&](size_t b) {
     char* r = cur;
@@ -1010,6 +1044,7 @@ nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables,
   p.sw_prefix = (const unsigned long long*)take(b_pre);
   p.sw_first = (const unsigned long long*)take(b_first);
   p.sw_sums = (nmc::XyzSweepSums*)take(b_sums);
+  p.sw_order = (const unsigned int*)take(b_order);
   p.sw_nsets = n_sets;
   p.first = 0;
   p.n = prefix[n_sets];
@@ -1022,6 +1057,8 @@ nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables,
       cudaMemcpyAsync((void*)p.sw_phase, phase.data(), b_ph, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
       cudaMemcpyAsync((void*)p.sw_prefix, prefix.data(), b_pre, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
       cudaMemcpyAsync((void*)p.sw_first, first.data(), b_first, cudaMemcpyHostToDevice, h->stream) !=
+          cudaSuccess ||
+      cudaMemcpyAsync((void*)p.sw_order, order.data(), b_order, cudaMemcpyHostToDevice, h->stream) !=
           cudaSuccess ||
       cudaMemsetAsync(p.sw_sums, 0, b_sums, h->stream) != cudaSuccess ||
       cudaMemsetAsync(&h->d_sums->work, 0, sizeof(unsigned long long), h->stream) != cudaSuccess)

@@ -7,7 +7,9 @@
 // slice of one global photon index space: threads take photon indices from
 // a warp-aggregated counter (work stealing across sets), find the photon's
 // set by binary search over the budgets' prefix sums, and read that set's
-// optical constants through the read-only cache.  Uneven budgets therefore
+// optical constants through the read-only cache.  The host lays the sets
+// out in decreasing order of estimated cost per photon, so the photons that
+// live longest start first.  Uneven budgets therefore
 // cost nothing extra: the GPU stays full until the last photon of the last
 // set, and there is one tail for the whole sweep instead of one per set.
 // Per-set totals are u64 fixed point in shared memory, folded into global
@@ -53,16 +55,16 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepParams P) {
       const unsigned long long g = next_photon(P.work);
       if (g >= P.total) break;
       have = true;
-      // set of global photon g: prefix[set] <= g < prefix[set + 1]
+      // queue slot of global photon g: prefix[k] <= g < prefix[k + 1]
       int lo = 0, hi = P.nsets;
       while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
         if (__ldg(P.prefix + mid) <= g) lo = mid; else hi = mid;
       }
-      set = lo;
-      S = P.sets + set;
+      S = P.sets + lo;
+      set = (int)__ldg(&S->id);
       k1 = P.k1 + (uint32_t)set;
-      rng.init(__ldg(&S->first) + (g - __ldg(P.prefix + set)));
+      rng.init(__ldg(&S->first) + (g - __ldg(P.prefix + lo)));
       // ---- LAUNCH (kernels.metal:106-168) with this set's indices
       const float n1 = __ldg(&S->n1), n2 = __ldg(&S->n2);
       x = y = z = 0.f;
