@@ -14,11 +14,17 @@
 //           <name>_DetPhot2D.dat (tab text, rows of Ny values taken at
 //           j + i*Nx as main.m:519-561 does).
 // The reference's own generator and stream schedule are the default
-// (NMC_RNG_TAUS_REF), so the photons are the reference's; options:
+// (NMC_RNG_TAUS_REF), so the photons are the reference's.  They run in one
+// persistent launch: photon (run r, index i) of the reference's dispatch loop
+// (main.m:144-187) is photon (r - 1) * batch + i here and draws the same
+// stream, and the tallies are integer sums, so the files equal the loop's bit
+// for bit while the GPU waits for one tail instead of one per dispatch.
+// Options:
 //   --photons N     photons (default PHOTON_TOTAL = 100000, multiple of the batch)
 //   --batch B       photons per dispatch (default PHOTON_BATCH = 10000)
 //   --philox S      the engine's Philox streams with seed S instead
-//   --persistent    one persistent launch instead of the dispatch loop
+//   --dispatch      run the reference's loop of photons / batch blocking dispatches
+//   --persistent    one persistent launch (the default)
 //   --device D      CUDA device (default 0)
 //   --dry-run       parse the inputs, print them and write _props.m only
 // Besides the reference's files it writes <name>_report.json: photons, kernel
@@ -210,14 +216,14 @@ void save_mcout(const float* J, const float* F, double S, double A, double E, do
 
 int main(int argc, char** argv) {
   if (argc < 2) {
-    std::printf("USAGE: nmc name [--photons N] [--batch B] [--philox SEED] [--persistent] [--device D] "
+    std::printf("USAGE: nmc name [--photons N] [--batch B] [--philox SEED] [--dispatch] [--device D] "
                 "[--dry-run]\nwhich will load the files name_H.mci and name_T.bin\n"
                 "and run the Monte Carlo program.\n");
     return 0;
   }
   const std::string name = argv[1];
   uint64_t photons = NMC_PHOTON_TOTAL_DEFAULT, batch = NMC_PHOTON_BATCH_DEFAULT, seed = 0;
-  bool philox = false, persistent = false, dry = false;
+  bool philox = false, persistent = true, dry = false;
   int device = 0;
   for (int i = 2; i < argc; ++i) {
     const std::string a = argv[i];
@@ -232,6 +238,7 @@ int main(int argc, char** argv) {
     else if (a == "--batch") batch = std::strtoull(val("--batch"), nullptr, 10);
     else if (a == "--philox") { philox = true; seed = std::strtoull(val("--philox"), nullptr, 10); }
     else if (a == "--persistent") persistent = true;
+    else if (a == "--dispatch") persistent = false;
     else if (a == "--device") device = std::atoi(val("--device"));
     else if (a == "--dry-run") dry = true;
     else {

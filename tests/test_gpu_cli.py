@@ -70,3 +70,19 @@ def test_cli_mcsub_files(gpu, tmp_path):
     assert out["E"] == pytest.approx(float(sae[2]), rel=1e-6)
     assert f"{mci.read_rd(name):.4f}" == f"{np.float32(sae[2] + sae[0]):.4f}"
     assert out["F"].shape == (B, B)
+
+
+def test_persistent_launch_equals_the_dispatch_loop(gpu, tmp_path):
+    # the default single launch and the reference's ten blocking dispatches
+    # draw the same streams per photon; every file is identical
+    rp, tp, v, ext = cases.skin_vessel_case(N=40, d=0.005)
+    outs = {}
+    for mode in ("default", "--dispatch"):
+        name = str(tmp_path / mode.strip("-"))
+        mci.write_mci(name, rp, tp)
+        mci.write_tissue(name, v)
+        r = mci.run_nmc(name, *([] if mode == "default" else [mode]))
+        assert r.returncode == 0, r.stdout + r.stderr
+        outs[mode] = {ext_: open(name + ext_, "rb").read() for ext_ in ("_F.bin", "_Rd.dat", "_Ryx.dat",
+                                                                       "_DetPhot2D.dat")}
+    assert outs["default"] == outs["--dispatch"]
