@@ -125,6 +125,28 @@ def test_mcxyz_fp32_oracle_replays_reference(oracle):
     assert o["rd_sum"] == pytest.approx(r["rd_slots"].sum(), rel=0.02)
 
 
+def test_two_term_fp32_oracle_replays_reference(oracle):
+    """MCXYZKernelTT (kernels.metal:757-1118): the FP32 restatement with the
+    reference's generator, seeded from run 1 as the reference's TT kernel
+    is, against the reference kernel itself on a 60^3 skin-vessel map with
+    two-term tissues (g_f 0.9, g_b 0.3, a 0.5, C 0.9)."""
+    if not oracle.ref_available():
+        pytest.skip("reference sources not present")
+    rp, tp, v, _ = cases.skin_vessel_case(N=60, d=0.005)
+    rp.mckernelflag = abi.SIM_MCXYZ_TT
+    rp.boundaryflag = 1  # the reference's two-term Rd2D index is unclamped (kernels.metal:984)
+    for t in range(1, 5):
+        tp.gf[t], tp.af[t], tp.gb[t], tp.ab[t], tp.CC[t] = 0.9, 0.5, 0.3, 0.5, 0.9
+    ext = abi.ext_defaults(rng=abi.RNG_TAUS_REF, flags=abi.FLAG_TT_REPLAY_RUN1)
+    r = oracle.ref_mcxyz_tt(rp, tp, v, 1, 1, 4000, replay_run1=True, per_photon=True)
+    o = oracle.run(abi.SIM_MCXYZ_TT, rp, tp, v, ext=ext, n=4000, trace=True, real_bits=32)
+    d = np.abs(r["per_photon"] - o["recs"]["detected"])
+    print(f"two-term per-photon agreement {np.mean(d < 1e-5):.3f}, Rd ref {r['rd_slots'].sum() / 4000:.5f} "
+          f"oracle {o['rd_sum'] / 4000:.5f}")
+    assert np.mean(d < 1e-5) >= 0.8
+    assert o["rd_sum"] == pytest.approx(r["rd_slots"].sum(), rel=0.02)
+
+
 def test_notebook_rd_reproduced_by_reference_build(oracle):
     """example0.ipynb cell 5 records Rd = 0.26601276 for 1e5 photons of its
     homogeneous cube (Metal, AMD Radeon Pro 5500 XT).  The reference kernel
