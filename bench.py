@@ -39,7 +39,7 @@ WORKLOAD = "mcxyz skin-vessel 200^3 @0.005 cm, 1e8 photons per GPU per step"
 # from the source of the transport loop: FP32/INT lane operations issued on
 # the FMA/ALU pipes for the sub-step proper (position update, same-voxel
 # test, face distances, absorption, voxel index and tissue lookup) and the
-# per-hop SPIN/roulette share.  Fixed once; see the design doc.
+# per-hop SPIN/roulette share.  Fixed once, not re-counted per build.
 OPS_PER_SUBSTEP = 64.0
 MUFU_PER_SUBSTEP = 3.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 1e8-photon
