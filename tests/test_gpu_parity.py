@@ -124,6 +124,31 @@ def test_mcxyz_two_term_per_photon(gpu, oracle):
     assert frac >= 0.75
 
 
+@pytest.mark.parametrize("case", ["C1 mcsub mua 1 mus 100 g 0.9", "C2 skin-vessel 200^3 x 0.005 cm"])
+def test_step_counts_match_the_fp64_oracle(gpu, oracle, case):
+    # the unit of the roofline is the photon step (mcsub) or voxel sub-step
+    # (mcxyz), counted in the kernel: on the same photons the mean count
+    # equals the FP64 oracle's to within 1 %.  Per photon, mcsub counts are
+    # equal; a voxel walk in FP32 cell offsets can land a few steps exactly on
+    # a face where FP64 lands beside it, so its counts agree within 1 %.
+    if case.startswith("C1"):
+        sim, (rp, tp, ext), v, n = abi.SIM_MCSUB, cases.mcsub_case(), None, 20_000
+    else:
+        rp, tp, v, ext = cases.skin_vessel_case(N=200, d=0.005)
+        sim, n = abi.SIM_MCXYZ, 3_000
+    e = _engine(gpu, sim, rp, tp, v, ext)
+    recs, _ = e.run_traced(0, n)
+    o = oracle.run(sim, rp, tp, v, ext=ext, n=n, trace=True)
+    g_sub, o_sub = recs["n_sub"].astype(np.float64), o["recs"]["n_sub"].astype(np.float64)
+    same = np.mean(g_sub == o_sub)
+    close = np.mean(np.abs(g_sub - o_sub) <= np.maximum(2.0, 0.01 * o_sub))
+    print(f"{case}: steps/photon gpu {g_sub.mean():.2f} oracle {o_sub.mean():.2f}; per photon equal {same:.4f}, "
+          f"within 1 % {close:.4f}")
+    assert abs(g_sub.mean() - o_sub.mean()) <= 0.01 * o_sub.mean()
+    assert (same if sim == abi.SIM_MCSUB else close) >= 0.95
+    assert e.summary()["substeps"] == int(g_sub.sum())
+
+
 def test_tallies_bit_reproducible(gpu):
     rp, tp, v, ext = cases.skin_vessel_case(N=48)
     out = []
