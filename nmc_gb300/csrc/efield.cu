@@ -121,20 +121,31 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // a conj(b)
 __device__ __forceinline__ float cnorm(float2 a) { return a.x * a.x + a.y * a.y; }
 __device__ __forceinline__ float wrap_pi(float a) { return a - kTwoPi * rintf(a * (1.f / kTwoPi)); }
 
-// phi in [0, 2 pi) with CDF (phi + beta/2 (sin(2 phi - tp0) + sin tp0)) / (2 pi) = u.
-__device__ __forceinline__ float sample_phi(float u, float beta, float tp0) {
+// phi in [0, 2 pi) with CDF (phi + beta/2 (sin(2 phi - tp0) + sin tp0)) / (2 pi) = u,
+// by Newton steps kept inside a shrinking bracket; s0, c0 = sin tp0, cos tp0.
+// One sincos of 2 phi per step; in fast math its argument is first wrapped to
+// [-pi, pi], where the hardware approximation's absolute error (~1e-6) stays
+// below the 2e-6 tolerance.
+template <bool FAST>
+__device__ __forceinline__ void sincos_w(float a, float* s, float* c) {
+  if (FAST) __sincosf(wrap_pi(a), s, c); else sincosf(a, s, c);
+}
+template <bool FAST>
+__device__ __forceinline__ float sample_phi(float u, float beta, float s0, float c0) {
   const float target = kTwoPi * u;
   if (fabsf(beta) < 1e-6f) return target;
-  const float s0 = sinf(tp0);
   float lo = 0.f, hi = kTwoPi, phi = target;
   for (int it = 0; it < 40; ++it) {
-    const float G = phi + 0.5f * beta * (sinf(2.f * phi - tp0) + s0) - target;
+    float s2, c2;
+    sincos_w<FAST>(2.f * phi, &s2, &c2);
+    const float sa = s2 * c0 - c2 * s0, ca = c2 * c0 + s2 * s0;  // sin, cos (2 phi - tp0)
+    const float G = phi + 0.5f * beta * (sa + s0) - target;
     if (fabsf(G) < 2e-6f) break;
     if (G > 0.f)
       hi = phi;
     else
       lo = phi;
-    const float dG = 1.f + beta * cosf(2.f * phi - tp0);
+    const float dG = 1.f + beta * ca;
     float nx = dG > 1e-6f ? phi - G / dG : 0.5f * (lo + hi);
     if (!(nx > lo && nx < hi)) nx = 0.5f * (lo + hi);
     phi = nx;
@@ -266,7 +277,8 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
         const float s1 = cnorm(S1), s2 = cnorm(S2), hd = 0.5f * (Pp - Qp);
         const float rho = sqrtf(hd * hd + Cp * Cp), den = (s1 + s2) * 0.5f * (Pp + Qp);
         const float beta = den > 0.f ? fminf(fmaxf((s2 - s1) * rho / den, -1.f), 1.f) : 0.f;
-        const float phi = sample_phi(u01(r.z), beta, atan2f(Cp, hd));
+        const float irho = rho > 0.f ? 1.f / rho : 0.f;  // (cos, sin) of 2 phi0 = (hd, Cp) / rho
+        const float phi = sample_phi<FAST>(u01(r.z), beta, Cp * irho, hd * irho);
         float sph, cph;
         if (FAST) __sincosf(phi, &sph, &cph); else sincosf(phi, &sph, &cph);
         // frame: e1 = cos e_par + sin e_perp, e2 = -sin e_par + cos e_perp
