@@ -146,7 +146,7 @@ __device__ __forceinline__ float sample_phi(float u, float beta, float s0, float
     else
       lo = phi;
     const float dG = 1.f + beta * ca;
-    float nx = dG > 1e-6f ? phi - G / dG : 0.5f * (lo + hi);
+    float nx = dG > 1e-6f ? phi - Math<FAST>::div(G, dG) : 0.5f * (lo + hi);
     if (!(nx > lo && nx < hi)) nx = 0.5f * (lo + hi);
     phi = nx;
   }
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
           if (cdf[mid] <= uth) a0 = mid; else a1 = mid;
         }
         const float q0 = cdf[a0], q1 = cdf[a1];
-        const float fr = q1 > q0 ? fminf(fmaxf((uth - q0) / (q1 - q0), 0.f), 1.f) : 0.5f;
+        const float fr = q1 > q0 ? fminf(fmaxf(M::div(uth - q0, q1 - q0), 0.f), 1.f) : 0.5f;
         const float th = ((float)a0 + fr) * P.dtheta;
         float sth, cth;
         if (FAST) __sincosf(th, &sth, &cth); else sincosf(th, &sth, &cth);
@@ -276,8 +276,8 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
         const float Cp = T00.x * T10.x + T00.y * T10.y + T01.x * T11.x + T01.y * T11.y;
         const float s1 = cnorm(S1), s2 = cnorm(S2), hd = 0.5f * (Pp - Qp);
         const float rho = sqrtf(hd * hd + Cp * Cp), den = (s1 + s2) * 0.5f * (Pp + Qp);
-        const float beta = den > 0.f ? fminf(fmaxf((s2 - s1) * rho / den, -1.f), 1.f) : 0.f;
-        const float irho = rho > 0.f ? 1.f / rho : 0.f;  // (cos, sin) of 2 phi0 = (hd, Cp) / rho
+        const float beta = den > 0.f ? fminf(fmaxf(M::div((s2 - s1) * rho, den), -1.f), 1.f) : 0.f;
+        const float irho = rho > 0.f ? M::rcp(rho) : 0.f;  // (cos, sin) of 2 phi0 = (hd, Cp) / rho
         const float phi = sample_phi<FAST>(u01(r.z), beta, Cp * irho, hd * irho);
         float sph, cph;
         if (FAST) __sincosf(phi, &sph, &cph); else sincosf(phi, &sph, &cph);
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
         T10 = cmul(S1, b10);
         T11 = cmul(S1, b11);
         const float fn = cnorm(T00) + cnorm(T01) + cnorm(T10) + cnorm(T11);
-        const float sc = fn > 0.f ? sqrtf(2.f / fn) : 0.f;
+        const float sc = fn > 0.f ? (FAST ? 1.41421356f * rsqrtf(fn) : sqrtf(2.f / fn)) : 0.f;
         T00 = make_float2(T00.x * sc, T00.y * sc);
         T01 = make_float2(T01.x * sc, T01.y * sc);
         T10 = make_float2(T10.x * sc, T10.y * sc);
