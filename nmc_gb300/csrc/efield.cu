@@ -153,6 +153,21 @@ __device__ __forceinline__ float sample_phi(float u, float beta, float s0, float
   return phi;
 }
 
+// The photon's path length, a sum of thousands of positive steps whose phase
+// k * path needs ~1e-9 relative precision: an unevaluated float pair (TwoSum,
+// then a Fast2Sum renormalisation), ~48 significant bits on the FP32 pipes.
+struct PathSum {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float b) {
+    const float t = hi + b, bp = t - hi;
+    const float e = (hi - (t - bp)) + (b - bp);
+    const float l = lo + e, h = t + l;
+    lo = l - (h - t);
+    hi = h;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
 // A unit vector perpendicular to u (the s direction z x u, or y for u along z).
 __device__ __forceinline__ void perp_of(float ux, float uy, float uz, float& px, float& py, float& pz) {
   const float n2 = ux * ux + uy * uy;
@@ -197,7 +212,7 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
     float x = 0.f, y = 0.f, z = 0.f, ux = S.ux, uy = S.uy, uz = S.uz, px = S.px, py = S.py, pz = S.pz;
     float2 T00 = S.t[0], T01 = S.t[1], T10 = S.t[2], T11 = S.t[3];
     float w = S.w0, fx = 0.f, fy = 0.f, lx = 0.f, ly = 0.f;
-    double path = 0.0;
+    PathSum path;
     int med = 0;
     unsigned int nsc = 0;
     uint32_t hop = 0;
@@ -211,7 +226,7 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
         x = fmaf(d, ux, x);
         y = fmaf(d, uy, y);
         z = 0.f;
-        path += d;
+        path.add(d);
         float uzt;
         const float rsp = rfresnel(P.n_medium, P.n_outside, -uz, &uzt);
         const uint4 a = philox4x32_10(make_uint4(c0, c1, hop | 0x40000000u, kEfTag), P.k0, k1);
@@ -229,12 +244,12 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
         x = fmaf(rest, ux, x);
         y = fmaf(rest, uy, y);
         z = rest * uz;
-        path += rest;
+        path.add(rest);
       } else {
         x = fmaf(s, ux, x);
         y = fmaf(s, uy, y);
         z = fmaf(s, uz, z);
-        path += s;
+        path.add(s);
       }
       w *= Md.surv;
       if (med == 0 && u01(r.w) < Md.p_raman) {  // Raman conversion
@@ -413,7 +428,7 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
       const int ix = (int)floorf(x * P.map_inv + 0.5f * P.map_n), iy = (int)floorf(y * P.map_inv + 0.5f * P.map_n);
       if (ix >= 0 && ix < P.map_n && iy >= 0 && iy < P.map_n) {
         float* m = P.maps + (size_t)set * NMC_EF_MAPS * MN + (size_t)ix * P.map_n + iy;
-        const float ph_path = (float)fmod(path * (double)P.med[0].kmed, 6.283185307179586);
+        const float ph_path = (float)fmod(path.value() * (double)P.med[0].kmed, 6.283185307179586);
         const float a_co = atan2f(Eco.y, Eco.x), a_cr = atan2f(Ecr.y, Ecr.x);
         atomicAdd(m + NMC_EF_MAP_XX * (size_t)MN, Ixx);
         atomicAdd(m + NMC_EF_MAP_XY * (size_t)MN, Ixy);
