@@ -153,6 +153,8 @@ __device__ __forceinline__ float sample_phi(float u, float beta, float s0, float
   return phi;
 }
 
+constexpr int kEfGuide = 1024;  // guide entries per scattering table
+
 // The photon's path length, a sum of thousands of positive steps whose phase
 // k * path needs ~1e-9 relative precision: an unevaluated float pair (TwoSum,
 // then a Fast2Sum renormalisation), ~48 significant bits on the FP32 pipes.
@@ -190,6 +192,21 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
   __shared__ double s_sum[kEfMaxSets * NMC_EF_FIELDS];
   for (int i = threadIdx.x; i < 2 * P.n_angles; i += blockDim.x) s_cdf[i] = P.cdf[i];
   for (int i = threadIdx.x; i < P.nsets * NMC_EF_FIELDS; i += blockDim.x) s_sum[i] = 0.0;
+  // guide to the inverse-CDF search: s_guide[m][k] = the bracket start of
+  // u = k / kEfGuide, so a draw's bracket search spans a few entries instead
+  // of all n_angles (the same bracket, found in fewer dependent steps)
+  __shared__ unsigned int s_guide[2 * (kEfGuide + 1)];
+  __syncthreads();
+  for (int i = threadIdx.x; i < 2 * (kEfGuide + 1); i += blockDim.x) {
+    const float* cdf = s_cdf + (i / (kEfGuide + 1)) * P.n_angles;
+    const float u = (float)(i % (kEfGuide + 1)) * (1.f / kEfGuide);
+    int a0 = 0, a1 = P.n_angles - 1;
+    while (a1 - a0 > 1) {
+      const int mid = (a0 + a1) >> 1;
+      if (cdf[mid] <= u) a0 = mid; else a1 = mid;
+    }
+    s_guide[i] = (unsigned int)a0;
+  }
   __syncthreads();
   const int MN = P.map_n * P.map_n, SN = P.sep_n * P.sep_n;
 
@@ -273,7 +290,9 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
       } else {  // scattering
         const float* cdf = s_cdf + Md.cdf_off;
         const float uth = u01(r.y);
-        int a0 = 0, a1 = P.n_angles - 1;
+        const unsigned int* gd = s_guide + med * (kEfGuide + 1);
+        const int gk = min((int)(uth * kEfGuide), kEfGuide - 1);
+        int a0 = (int)gd[gk], a1 = min((int)gd[gk + 1] + 1, P.n_angles - 1);
         while (a1 - a0 > 1) {
           const int mid = (a0 + a1) >> 1;
           if (cdf[mid] <= uth) a0 = mid; else a1 = mid;
