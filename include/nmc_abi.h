@@ -593,7 +593,9 @@ enum {
  * the sets).  Photons of set s use Philox key (seed lo, seed hi + s), so set
  * s reproduces a plain run with seed + (s << 32).  `out` holds n_sets *
  * NMC_SWEEP_FIELDS doubles; `J` (optional) n_sets * (BINS+1) doubles of the
- * escaping flux J[ir] per set (un-normalised). */
+ * escaping flux J[ir] per set (un-normalised).  The launch hands the sets
+ * out in decreasing estimated cost per photon (mu_t / mu_a), which shortens
+ * its tail and changes no result. */
 nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_sets, double* out,
                          double* J);
 
@@ -608,7 +610,10 @@ nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_set
  * (NMC-samples/example3.ipynb cell 5).  `out` holds n_sets *
  * NMC_SWEEP_FIELDS doubles: HOPS counts voxel sub-steps, S is 0, E the
  * detected weight, RD = E / photons (the run's Total Rd, main.m:294-305).
- * No map tallies (F3D, Rd2D) are kept. */
+ * No map tallies (F3D, Rd2D) are kept.  The launch hands the sets out in
+ * decreasing estimated cost per photon (sum over the map's tissues of
+ * voxels * (mus + 1/d) / mua), which shortens its tail and changes no
+ * result. */
 nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables, const uint64_t* photons,
                                  const uint64_t* first_photon, int32_t n_sets, double* out);
 
