@@ -332,3 +332,41 @@ def write_example0_mci(path: str):
 # Three-layer skin stack for the layered model: (mua, mus, g, n, thickness),
 # cm^-1 and cm: epidermis 0.01, dermis 0.2, semi-infinite subcutis.
 LAYERED_SKIN3 = [(3.0, 200.0, 0.8, 1.4, 0.01), (0.3, 150.0, 0.85, 1.4, 0.2), (0.1, 100.0, 0.9, 1.44, math.inf)]
+
+
+# Media and modes of the per-photon parity tests over the launch, boundary and
+# detection branches (kernels.metal:366-463, :556-637, :646-672).
+def modes_medium(Nx=40, Ny=40, Nz=40, dx=0.01, dy=0.01, dz=0.01, **run):
+    """Air above zsurf = 2 dz, tissue (mua 1, mus 80, g 0.85) below, a
+    spherical inclusion (mua 5, mus 120, g 0.9) of radius 0.06 cm at depth 0.1."""
+    zsurf = 2 * dz
+    base = dict(myname="modes", Nx=Nx, Ny=Ny, Nz=Nz, dx=dx, dy=dy, dz=dz, mcflag=0, launchflag=0,
+                boundaryflag=2, xs=0.0, ys=0.0, zs=zsurf + 1e-4, xfocus=0.0, yfocus=0.0, zfocus=float("inf"),
+                ux0=0.0, uy0=0.0, uz0=1.0, radius=0.03, waist=0.03, zsurf=zsurf, det_radius=15.0, xd=0.0,
+                n1=1.37, n2=1.0, na=90.0, det_state=0, mckernelflag=abi.SIM_MCXYZ, Nt=3)
+    base.update(run)
+    rp = abi.run_params(**base)
+    tp = abi.tissue_params(mua=[0.0001, 1.0, 5.0], mus=[1.0, 80.0, 120.0], g=[1.0, 0.85, 0.9])
+    T = np.full((Nz, Nx, Ny), 2, np.uint8)
+    T[:2] = 1
+    x = (np.arange(Nx) + 0.5 - Nx / 2) * dx
+    y = (np.arange(Ny) + 0.5 - Ny / 2) * dy
+    z = (np.arange(Nz) + 0.5) * dz
+    inc = (x[None, :, None] ** 2 + y[None, None, :] ** 2 + (z[:, None, None] - 0.1) ** 2) <= 0.06 ** 2
+    T[inc] = 3
+    return rp, tp, T.reshape(-1)
+
+
+PARITY_MODES = {
+    "gaussian-beam": dict(mcflag=1, radius=0.02, waist=0.02, zfocus=0.1),
+    "isotropic-point": dict(mcflag=2, xs=0.0, ys=0.0, zs=0.1),
+    "rectangle": dict(mcflag=3, radius=0.05),
+    "point-collimated": dict(mcflag=4),
+    "manual-direction": dict(launchflag=1, xs=0.01, ys=-0.02, zs=0.0201, ux0=0.3, uy0=0.2,
+                             uz0=math.sqrt(1 - 0.13)),
+    "boundary-0": dict(boundaryflag=0),
+    "boundary-1": dict(boundaryflag=1),
+    "transmittance": dict(det_state=1, Nz=16, zsurf=0.16, boundaryflag=1),
+    "ring-detector": dict(xd=0.05, det_radius=0.02, na=30.0),
+    "odd-noncubic-grid": dict(Nx=41, Ny=37, Nz=29, dx=0.011, dy=0.009, dz=0.0125),
+}

@@ -147,6 +147,28 @@ def test_two_term_fp32_oracle_replays_reference(oracle):
     assert o["rd_sum"] == pytest.approx(r["rd_slots"].sum(), rel=0.02)
 
 
+@pytest.mark.parametrize("mode", list(cases.PARITY_MODES))
+def test_fp32_oracle_replays_reference_in_every_mode(oracle, mode):
+    """The oracle's FP32 restatement against the reference's MCXYZKernel
+    compiled here, on the reference's own streams, over its launch modes
+    (kernels.metal:366-463), boundary modes (:646-672) and detection modes
+    (:556-637), and an odd, non-cubic grid: photon for photon on the detected
+    weight, and the total Rd."""
+    if not oracle.ref_available():
+        pytest.skip("reference sources not present")
+    rp, tp, v = cases.modes_medium(**cases.PARITY_MODES[mode])
+    n = 4000
+    ext = abi.ext_defaults(rng=abi.RNG_TAUS_REF, photons_per_dispatch=n)
+    r = oracle.ref_mcxyz(rp, tp, v, 1, 1, n, per_photon=True)
+    o = oracle.run(abi.SIM_MCXYZ, rp, tp, v, ext=ext, n=n, trace=True, real_bits=32)
+    d = np.abs(r["per_photon"] - o["recs"]["detected"])
+    agree = np.mean(d <= 1e-5 + 1e-4 * np.abs(r["per_photon"]))
+    rd_ref, rd_orc = r["rd_slots"].sum() / n, o["rd_sum"] / n
+    print(f"{mode}: per-photon agreement {agree:.4f}, Rd reference {rd_ref:.5f} oracle {rd_orc:.5f}")
+    assert agree >= 0.8
+    assert abs(rd_orc - rd_ref) <= 0.02 * rd_ref + 1e-4
+
+
 def test_notebook_rd_reproduced_by_reference_build(oracle):
     """example0.ipynb cell 5 records Rd = 0.26601276 for 1e5 photons of its
     homogeneous cube (Metal, AMD Radeon Pro 5500 XT).  The reference kernel
