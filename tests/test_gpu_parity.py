@@ -149,6 +149,44 @@ def test_step_counts_match_the_fp64_oracle(gpu, oracle, case):
     assert e.summary()["substeps"] == int(g_sub.sum())
 
 
+@pytest.mark.parametrize("kind", ["mcsub", "mcxyz"])
+def test_every_tally_within_3_sigma_of_the_fp64_oracle(gpu, oracle, kind):
+    # every bin of every tally of the engine against the FP64 oracle over the
+    # same photons; each bin's standard error comes from the spread of the
+    # oracle's 10 batches.  The relative error of each tally's total against
+    # the oracle is printed.
+    B = 10
+    if kind == "mcsub":
+        rp, tp, ext = cases.mcsub_case()
+        sim, v, per = abi.SIM_MCSUB, None, 20_000
+        which = {"J": abi.TALLY_J, "F": abi.TALLY_F}
+    else:
+        rp, tp, v, ext = cases.skin_vessel_case(N=48)
+        sim, per = abi.SIM_MCXYZ, 4_000
+        which = {"F3D": abi.TALLY_F3D, "Rd2D": abi.TALLY_RD2D, "DetPhot2D": abi.TALLY_DETPHOT2D,
+                 "rd_slots": abi.TALLY_RD_SLOTS}
+    batches = [oracle.run(sim, rp, tp, v, ext=ext, first=b * per, n=per) for b in range(B)]
+    e = _engine(gpu, sim, rp, tp, v, ext)
+    e.run(0, B * per)
+    for name, t in which.items():
+        orc = np.stack([r[name] for r in batches])
+        tot = orc.sum(0)
+        se = np.sqrt(B) * orc.std(0, ddof=1)
+        g = e.tally(t)
+        assert g.shape == tot.shape, name
+        live = se > 0
+        z = (g[live] - tot[live]) / se[live]
+        far = np.mean(np.abs(z) > 3) if live.any() else 0.0
+        rel = abs(g.sum() - tot.sum()) / max(tot.sum(), 1e-30)
+        print(f"{kind} {name}: {live.sum()} bins with spread, max |z| {np.abs(z).max():.2f}, "
+              f"beyond 3 sigma {far:.4f}; total {g.sum():.6g} vs oracle {tot.sum():.6g} (rel error {rel:.2e})")
+        assert np.abs(z).max() <= 3.0, name
+        assert rel <= 1e-3, name
+        # bins without spread in the oracle hold the same value in every batch
+        # (mostly empty): the engine agrees there up to a single photon's weight
+        assert np.all(np.abs(g[~live] - tot[~live]) <= 1.0 + 1e-6 * np.abs(tot[~live])), name
+
+
 def test_tallies_bit_reproducible(gpu):
     rp, tp, v, ext = cases.skin_vessel_case(N=48)
     out = []
