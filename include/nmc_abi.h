@@ -323,6 +323,15 @@ size_t nmc_tally_size(nmc_handle* h, int32_t which);
 /* Clears all tallies and counters; keeps the prepared inputs. */
 nmc_status nmc_reset(nmc_handle* h);
 
+/* Tallies accumulate as 64-bit fixed point on the device (32 fractional
+ * bits: integer sums, the same whatever the thread order).  Before a bin
+ * could wrap, the library folds every tally into an FP64 carry, in stream
+ * order: by default after each 2^31 photons, and a longer run is launched in
+ * pieces of that size.  Results read back include the carries.  This sets
+ * the interval in photons, in [1, 2^31] (no counterpart in the reference,
+ * whose float atomics lose precision instead). */
+nmc_status nmc_set_fold_interval(nmc_handle* h, uint64_t photons);
+
 /* The cudaStream_t the handle launches on (for timing and overlap). */
 void* nmc_stream(nmc_handle* h);
 

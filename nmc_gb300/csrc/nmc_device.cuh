@@ -415,10 +415,11 @@ __device__ __forceinline__ void warp_add_f64(double* dst, double v) {
 // Totals every launch adds into (device memory, one per handle).
 struct DevSums {
   unsigned long long photons, substeps, scatters;
-  unsigned long long S, A, E, rd;  // fixed point 2^-32
+  unsigned long long S, A, E, rd;  // fixed point 2^-32, since the last fold
   double rd_sumsq;
   unsigned int flags, pad;
   unsigned long long work;         // photon counter of the running launch
+  double carry[4];                 // S, A, E, rd moved out of the fixed-point words by folds
 };
 
 struct RngParams {

@@ -64,6 +64,13 @@ struct nmc_handle {
   unsigned long long* d_J = nullptr;
   unsigned long long* d_F = nullptr;
   size_t nvox = 0, n2d = 0, nslots = 0, nJ = 0, nF = 0;
+  // Fixed-point tallies are folded into FP64 carries before they could wrap:
+  // a photon adds at most about one weight unit (2^32 fixed-point units) to a
+  // bin, so 2^31 photons between folds keep every u64 word below 2^63 and
+  // every u32 count below 2^31.  Carries are allocated at the first fold.
+  double *c_F3D = nullptr, *c_Rd2D = nullptr, *c_Det = nullptr, *c_slots = nullptr, *c_J = nullptr,
+         *c_F = nullptr, *c_rdr = nullptr;
+  uint64_t since_fold = 0, fold_every = 1ull << 31;
   float* d_stage = nullptr;  // conversion buffer for results (floats)
   float* h_stage = nullptr;  // pinned host copy
   size_t stage_elems = 0;
@@ -124,6 +131,14 @@ void free_buffers(nmc_handle* h) {
   dfree(h->d_rdr);
   dfree(h->d_ev);
   dfree(h->d_evcount);
+  dfree(h->c_F3D);
+  dfree(h->c_Rd2D);
+  dfree(h->c_Det);
+  dfree(h->c_slots);
+  dfree(h->c_J);
+  dfree(h->c_F);
+  dfree(h->c_rdr);
+  h->since_fold = 0;
   for (ReduceGraph& g : h->graphs) cudaGraphExecDestroy(g.exec);
   h->graphs.clear();
   if (h->h_stage) cudaFreeHost(h->h_stage);
@@ -277,10 +292,27 @@ struct AdjArgs {
   double* gQ;
 };
 
+nmc_status fold(nmc_handle* h);
+
 nmc_status launch(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_record* d_recs,
                   float4* d_events, uint32_t k_events, const AdjArgs* adj = nullptr) {
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   if (n == 0) return NMC_OK;
+  if (!d_recs && !adj && n > h->fold_every) {  // launches of at most fold_every photons, folded between
+    for (uint64_t done = 0; done < n;) {
+      const uint64_t m = std::min<uint64_t>(h->fold_every, n - done);
+      const nmc_status st = launch(h, first + done, m, nullptr, nullptr, 0, nullptr);
+      if (st != NMC_OK) return st;
+      done += m;
+    }
+    return NMC_OK;
+  }
+  if (h->since_fold + n > h->fold_every) {
+    NMC_CUDA(h, cudaSetDevice(h->device));
+    const nmc_status st = fold(h);
+    if (st != NMC_OK) return st;
+  }
+  h->since_fold += n;
   if (adj && !h->voxel_mode) return fail(h, NMC_ESTATE, "the adjoint needs per-voxel properties");
   if (h->voxel_mode && h->sim == NMC_SIM_MCXYZ_TT)
     return fail(h, NMC_EUNSUPPORTED, "per-voxel media use the one-term HG kernel (NMC_SIM_MCXYZ)");
@@ -372,19 +404,50 @@ nmc_status sync_all(nmc_handle* h) {
   return NMC_OK;
 }
 
-__global__ void unfix_f32(const unsigned long long* __restrict__ s, float* __restrict__ d, size_t n,
-                          double scale) {
+__global__ void unfix_f32(const unsigned long long* __restrict__ s, const double* __restrict__ c,
+                          float* __restrict__ d, size_t n, double scale) {
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-    d[k] = (float)((double)s[k] * scale);
+    d[k] = (float)((double)s[k] * scale + (c ? c[k] : 0.0));
 }
 __global__ void unfix_f64(const unsigned long long* __restrict__ s, double* __restrict__ d, size_t n,
                           double scale) {
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
     d[k] = (double)s[k] * scale;
 }
-__global__ void u32_to_f32(const unsigned int* __restrict__ s, float* __restrict__ d, size_t n) {
-  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-    d[k] = __uint_as_float(s[k]);
+__global__ void u32_to_f32(const unsigned int* __restrict__ s, const double* __restrict__ c,
+                           float* __restrict__ d, size_t n) {
+  // counts travel as int32 bits (the reference's DetPhot2D is int); saturate
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const double t = (double)s[k] + (c ? c[k] : 0.0);
+    d[k] = __uint_as_float((unsigned int)fmin(t, 2147483647.0));
+  }
+}
+// Moves fixed-point tallies into their FP64 carries (exact while a carry
+// stays below 2^53 fixed-point units) and clears them.
+__global__ void fold_u64(unsigned long long* __restrict__ s, double* __restrict__ c, size_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const unsigned long long v = s[k];
+    if (v) {
+      c[k] += (double)v * nmc::kUnfix;
+      s[k] = 0ull;
+    }
+  }
+}
+__global__ void fold_u32(unsigned int* __restrict__ s, double* __restrict__ c, size_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const unsigned int v = s[k];
+    if (v) {
+      c[k] += (double)v;
+      s[k] = 0u;
+    }
+  }
+}
+__global__ void fold_sums(DevSums* d) {
+  d->carry[0] += (double)d->S * nmc::kUnfix;
+  d->carry[1] += (double)d->A * nmc::kUnfix;
+  d->carry[2] += (double)d->E * nmc::kUnfix;
+  d->carry[3] += (double)d->rd * nmc::kUnfix;
+  d->S = d->A = d->E = d->rd = 0ull;
 }
 
 // The reduction graph for `mask` (regions of StageRegion), captured on first
@@ -397,6 +460,7 @@ nmc_status reduce_graph(nmc_handle* h, unsigned mask, cudaGraphExec_t* out) {
       return NMC_OK;
     }
   const void* src[kStN] = {h->d_J, h->d_F, h->d_F3D, h->d_slots, h->d_Rd2D, h->d_Det, h->d_sums};
+  const double* carry[kStN] = {h->c_J, h->c_F, h->c_F3D, h->c_slots, h->c_Rd2D, h->c_Det, nullptr};
   NMC_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaSuccess;
   for (int k = 0; k < kStN && e == cudaSuccess; ++k) {
@@ -409,9 +473,10 @@ nmc_status reduce_graph(nmc_handle* h, unsigned mask, cudaGraphExec_t* out) {
       const int block = 256;
       const int grid = (int)std::min<size_t>((n + block - 1) / block, (size_t)h->nsm * 8);
       if (k == kStDet)
-        u32_to_f32<<<grid, block, 0, h->stream>>>((const unsigned int*)src[k], dst, n);
+        u32_to_f32<<<grid, block, 0, h->stream>>>((const unsigned int*)src[k], carry[k], dst, n);
       else
-        unfix_f32<<<grid, block, 0, h->stream>>>((const unsigned long long*)src[k], dst, n, nmc::kUnfix);
+        unfix_f32<<<grid, block, 0, h->stream>>>((const unsigned long long*)src[k], carry[k], dst, n,
+                                                  nmc::kUnfix);
       e = cudaGetLastError();
     }
     if (e == cudaSuccess)
@@ -429,6 +494,46 @@ nmc_status reduce_graph(nmc_handle* h, unsigned mask, cudaGraphExec_t* out) {
   if (e != cudaSuccess) return cuda_fail(h, e, "instantiating the result reduction");
   h->graphs.push_back(ReduceGraph{mask, exec});
   *out = exec;
+  return NMC_OK;
+}
+
+// Folds every fixed-point tally and the fixed-point totals into their FP64
+// carries, in stream order (no host wait).  A carry allocated here changes
+// what the reduction graphs read, so they are captured again.
+nmc_status fold(nmc_handle* h) {
+  struct T {
+    void* s;
+    double** c;
+    size_t n;
+    bool u32;
+  } t[] = {{h->d_F3D, &h->c_F3D, h->nvox, false}, {h->d_Rd2D, &h->c_Rd2D, h->n2d, false},
+           {h->d_Det, &h->c_Det, h->n2d, true},   {h->d_slots, &h->c_slots, h->nslots, false},
+           {h->d_J, &h->c_J, h->nJ, false},       {h->d_F, &h->c_F, h->nF, false},
+           {h->d_rdr, &h->c_rdr, h->d_rdr ? (size_t)h->rd_bins + 1 : 0, false}};
+  bool fresh = false;
+  for (T& x : t) {
+    if (!x.s || x.n == 0) continue;
+    if (!*x.c) {
+      NMC_CUDA(h, cudaMalloc((void**)x.c, x.n * sizeof(double)));
+      NMC_CUDA(h, cudaMemsetAsync(*x.c, 0, x.n * sizeof(double), h->stream));
+      fresh = true;
+    }
+    const int block = 256;
+    const int grid = (int)std::min<size_t>((x.n + block - 1) / block, (size_t)h->nsm * 8);
+    if (x.u32)
+      fold_u32<<<grid, block, 0, h->stream>>>((unsigned int*)x.s, *x.c, x.n);
+    else
+      fold_u64<<<grid, block, 0, h->stream>>>((unsigned long long*)x.s, *x.c, x.n);
+    NMC_CUDA(h, cudaGetLastError());
+  }
+  fold_sums<<<1, 1, 0, h->stream>>>(h->d_sums);
+  NMC_CUDA(h, cudaGetLastError());
+  if (fresh) {
+    NMC_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (ReduceGraph& g : h->graphs) cudaGraphExecDestroy(g.exec);
+    h->graphs.clear();
+  }
+  h->since_fold = 0;
   return NMC_OK;
 }
 
@@ -583,10 +688,24 @@ nmc_status nmc_reset(nmc_handle* h) {
   if (h->d_Det) NMC_CUDA(h, cudaMemsetAsync(h->d_Det, 0, h->n2d * 4, h->stream));
   if (h->d_slots) NMC_CUDA(h, cudaMemsetAsync(h->d_slots, 0, h->nslots * 8, h->stream));
   if (h->d_rdr) NMC_CUDA(h, cudaMemsetAsync(h->d_rdr, 0, ((size_t)h->rd_bins + 1) * 8, h->stream));
+  const std::pair<double*, size_t> carries[] = {{h->c_F3D, h->nvox}, {h->c_Rd2D, h->n2d}, {h->c_Det, h->n2d},
+                                                {h->c_slots, h->nslots}, {h->c_J, h->nJ}, {h->c_F, h->nF},
+                                                {h->c_rdr, (size_t)h->rd_bins + 1}};
+  for (const auto& c : carries)
+    if (c.first) NMC_CUDA(h, cudaMemsetAsync(c.first, 0, c.second * sizeof(double), h->stream));
+  h->since_fold = 0;
   h->kernel_ms = 0.0;
   h->launches = 0;
   h->seen_flags = 0;
   return wait_stream(h);
+}
+
+nmc_status nmc_set_fold_interval(nmc_handle* h, uint64_t photons) {
+  if (!h) return NMC_EINVAL;
+  if (photons < 1 || photons > (1ull << 31))
+    return fail(h, NMC_EINVAL, "the fold interval must be in [1, 2^31] photons");
+  h->fold_every = photons;
+  return NMC_OK;
 }
 
 nmc_status nmc_set_num_runs_seed(nmc_handle* h, int32_t run, float time_seed) {
@@ -748,10 +867,19 @@ nmc_status nmc_get_tally_f64(nmc_handle* h, int32_t which, double* out, size_t n
   if (want == 0 || n != want) return fail(h, NMC_EINVAL, "tally not produced by this kind, or wrong size");
   nmc_status st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  const double* carry = which == NMC_TALLY_J ? h->c_J
+                        : which == NMC_TALLY_F ? h->c_F
+                        : which == NMC_TALLY_F3D ? h->c_F3D
+                        : which == NMC_TALLY_RD2D ? h->c_Rd2D
+                        : which == NMC_TALLY_DETPHOT2D ? h->c_Det
+                        : which == NMC_TALLY_RD_R  ? h->c_rdr
+                                                   : h->c_slots;
+  std::vector<double> c(carry ? n : 0);
+  if (carry) NMC_CUDA(h, cudaMemcpy(c.data(), carry, n * sizeof(double), cudaMemcpyDeviceToHost));
   if (which == NMC_TALLY_DETPHOT2D) {
     std::vector<unsigned int> tmp(n);
     NMC_CUDA(h, cudaMemcpy(tmp.data(), h->d_Det, n * 4, cudaMemcpyDeviceToHost));
-    for (size_t k = 0; k < n; ++k) out[k] = tmp[k];
+    for (size_t k = 0; k < n; ++k) out[k] = (double)tmp[k] + (carry ? c[k] : 0.0);
     return NMC_OK;
   }
   const unsigned long long* src = which == NMC_TALLY_J ? h->d_J
@@ -762,7 +890,7 @@ nmc_status nmc_get_tally_f64(nmc_handle* h, int32_t which, double* out, size_t n
                                                              : h->d_slots;
   std::vector<unsigned long long> tmp(n);
   NMC_CUDA(h, cudaMemcpy(tmp.data(), src, n * 8, cudaMemcpyDeviceToHost));
-  for (size_t k = 0; k < n; ++k) out[k] = (double)tmp[k] * nmc::kUnfix;
+  for (size_t k = 0; k < n; ++k) out[k] = (double)tmp[k] * nmc::kUnfix + (carry ? c[k] : 0.0);
   return NMC_OK;
 }
 
@@ -802,9 +930,9 @@ nmc_status nmc_get_compute_results(nmc_handle* h, float* J, float* F, float* F3D
     if (k == kStSums) {
       DevSums s;
       std::memcpy(&s, src, sizeof s);
-      SAE[0] += (float)(s.S * nmc::kUnfix);
-      SAE[1] += (float)(s.A * nmc::kUnfix);
-      SAE[2] += (float)(s.E * nmc::kUnfix);
+      SAE[0] += (float)(s.S * nmc::kUnfix + s.carry[0]);
+      SAE[1] += (float)(s.A * nmc::kUnfix + s.carry[1]);
+      SAE[2] += (float)(s.E * nmc::kUnfix + s.carry[2]);
     } else if (k == kStDet) {
       const unsigned int* c = reinterpret_cast<const unsigned int*>(src);
       for (size_t i = 0; i < n; ++i) DetPhot2D[i] += (int32_t)c[i];
@@ -827,10 +955,10 @@ nmc_status nmc_get_summary(nmc_handle* h, nmc_summary* out) {
   out->photons = s.photons;
   out->substeps = s.substeps;
   out->scatters = s.scatters;
-  out->S = s.S * nmc::kUnfix;
-  out->A = s.A * nmc::kUnfix;
-  out->E = s.E * nmc::kUnfix;
-  out->rd_sum = s.rd * nmc::kUnfix;
+  out->S = s.S * nmc::kUnfix + s.carry[0];
+  out->A = s.A * nmc::kUnfix + s.carry[1];
+  out->E = s.E * nmc::kUnfix + s.carry[2];
+  out->rd_sum = s.rd * nmc::kUnfix + s.carry[3];
   out->rd_sumsq = s.rd_sumsq;
   out->kernel_ms = h->kernel_ms;
   out->launches = h->launches;
@@ -1134,6 +1262,7 @@ nmc_status nmc_set_radial_tally(nmc_handle* h, int32_t bins, float dr) {
   nmc_status st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
   dfree(h->d_rdr);
+  dfree(h->c_rdr);
   NMC_CUDA(h, cudaMalloc((void**)&h->d_rdr, ((size_t)bins + 1) * 8));
   NMC_CUDA(h, cudaMemset(h->d_rdr, 0, ((size_t)bins + 1) * 8));
   h->rd_bins = bins;

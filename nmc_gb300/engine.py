@@ -58,6 +58,7 @@ def lib() -> C.CDLL:
         L.nmc_get_compute_results.argtypes = [H] + [_P] * 16
         L.nmc_get_summary.argtypes = [H, C.POINTER(abi.Summary)]
         L.nmc_get_tally_f64.argtypes = [H, C.c_int32, _P, C.c_size_t]
+        L.nmc_set_fold_interval.argtypes = [H, C.c_uint64]
         L.nmc_tally_size.argtypes = [H, C.c_int32]
         L.nmc_tally_size.restype = C.c_size_t
         L.nmc_reset.argtypes = [H]
@@ -208,6 +209,10 @@ class Engine:
 
     def reset(self):
         self._check(self._L.nmc_reset(self._h), "nmc_reset")
+
+    def set_fold_interval(self, photons: int):
+        """Photons between folds of the fixed-point tallies into FP64 (default 2^31)."""
+        self._check(self._L.nmc_set_fold_interval(self._h, int(photons)), "nmc_set_fold_interval")
 
     def run_sweep(self, sets, with_J: bool = False) -> dict:
         """Batched sweep (mcsub handle): `sets` is a sequence of abi.SweepSet.

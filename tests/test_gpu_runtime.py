@@ -81,3 +81,40 @@ def test_reduction_graph_returns_the_tallies(gpu, kind):
         e._check(L.nmc_get_compute_results(e._h, *[_ptr(a) for a in args]), "nmc_get_compute_results")
         for k in acc:
             np.testing.assert_allclose(acc[k], 2 * r1[k], rtol=1e-6)
+
+
+@pytest.mark.parametrize("kind", ["mcsub", "mcxyz"])
+def test_folded_tallies_equal_unfolded(gpu, kind):
+    # folding the fixed-point tallies into FP64 (here every 7,000 photons,
+    # which also splits each run into launches of 7,000) changes no result:
+    # every folded part is exact in FP64 at these sizes
+    if kind == "mcsub":
+        rp, tp, ext = cases.mcsub_case()
+        sim, v, which = abi.SIM_MCSUB, None, (abi.TALLY_J, abi.TALLY_F)
+    else:
+        rp, tp, v, ext = cases.skin_vessel_case(N=48)
+        sim, which = abi.SIM_MCXYZ, (abi.TALLY_F3D, abi.TALLY_RD2D, abi.TALLY_DETPHOT2D, abi.TALLY_RD_SLOTS)
+    n = 50_000
+    out = []
+    for interval in (None, 7_000):
+        with gpu.Engine(sim, 0, ext) as e:
+            e.prepare_data(rp, tp, v)
+            if interval:
+                e.set_fold_interval(interval)
+            e.run(0, n // 2)
+            e.run(n // 2, n - n // 2)
+            s = e.summary()
+            out.append((s, [e.tally(w) for w in which], e.get_compute_results()))
+    (s0, t0, r0), (s1, t1, r1) = out
+    assert s1["launches"] > s0["launches"]
+    for k in ("photons", "substeps", "scatters", "S", "A", "E", "rd_sum"):
+        assert s0[k] == s1[k], k
+    for a, b in zip(t0, t1):
+        np.testing.assert_array_equal(a, b)
+    for k in r0:
+        np.testing.assert_array_equal(np.asarray(r0[k]), np.asarray(r1[k]), err_msg=k)
+    with gpu.Engine(sim, 0, ext) as e:
+        with pytest.raises(gpu.NMCError):
+            e.set_fold_interval(0)
+        with pytest.raises(gpu.NMCError):
+            e.set_fold_interval(2 ** 31 + 1)
