@@ -522,7 +522,8 @@ enum {
   NMC_LAY_INTERACTIONS, NMC_LAY_FIELDS
 };
 
-/* Photons [first, first + photons) through the stack on `device`; out holds
+/* Photons [first, first + photons) through the stack on `device` (at most
+ * 2^31 per call; results add up over calls); out holds
  * NMC_LAY_FIELDS doubles; rd_r, tt_r (nr+1), a_z (nz+1), a_rz ((nr+1)*(nz+1),
  * index ir*(nz+1) + iz) and a_layer (n_layers) are added to (+=) and may be
  * NULL.  Host pointers. */
@@ -602,7 +603,8 @@ enum {
  * the sets).  Photons of set s use Philox key (seed lo, seed hi + s), so set
  * s reproduces a plain run with seed + (s << 32).  `out` holds n_sets *
  * NMC_SWEEP_FIELDS doubles; `J` (optional) n_sets * (BINS+1) doubles of the
- * escaping flux J[ir] per set (un-normalised).  The launch hands the sets
+ * escaping flux J[ir] per set (un-normalised).  At most 2^31 photons per set
+ * and call (the per-set fixed-point sums stay below 2^63).  The launch hands the sets
  * out in decreasing estimated cost per photon (mu_t / mu_a), which shortens
  * its tail and changes no result. */
 nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_sets, double* out,
@@ -619,7 +621,8 @@ nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_set
  * (NMC-samples/example3.ipynb cell 5).  `out` holds n_sets *
  * NMC_SWEEP_FIELDS doubles: HOPS counts voxel sub-steps, S is 0, E the
  * detected weight, RD = E / photons (the run's Total Rd, main.m:294-305).
- * No map tallies (F3D, Rd2D) are kept.  The launch hands the sets out in
+ * No map tallies (F3D, Rd2D) are kept.  At most 2^31 photons per set and
+ * call.  The launch hands the sets out in
  * decreasing estimated cost per photon (sum over the map's tissues of
  * voxels * (mus + 1/d) / mua), which shortens its tail and changes no
  * result. */

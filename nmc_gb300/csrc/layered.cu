@@ -256,6 +256,9 @@ nmc_status layered_impl(int32_t device, const nmc_layered_config* cfg, const nmc
   const bool adj = g_rd || g_tt;
   if (!cfg || !layers || !out) return NMC_EINVAL;
   if (adj && cfg->n_layers > kMaxAdjLayers) return NMC_EINVAL;
+  // fixed-point tallies of one call stay below 2^63; more photons take more
+  // calls (first += photons), whose results add up in the caller's arrays
+  if (photons > (1ull << 31)) return NMC_EINVAL;
   const nmc_layered_config& c = *cfg;
   if (c.n_layers < 1 || c.n_layers > kMaxLayers || c.nr < 1 || c.nr > 65536 || c.nz < 1 || c.nz > 65536 ||
       !(c.dr > 0.f) || !(c.dz > 0.f) || !(c.n_above > 0.f) || !(c.n_below > 0.f) || !std::isfinite(c.n_above) ||

@@ -995,6 +995,8 @@ nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_set
       if (!std::isfinite(v)) return fail(h, NMC_EINVAL, "sweep set with a non-finite parameter");
     if (q.mua < 0.f || q.mus < 0.f || !(q.mua + q.mus > 0.f) || !(q.n1 > 0.f) || !(q.n2 > 0.f))
       return fail(h, NMC_EINVAL, "sweep set needs mua, mus >= 0, mua + mus > 0 and n1, n2 > 0");
+    if (q.photons > (1ull << 31))  // per-set fixed-point sums stay below 2^63
+      return fail(h, NMC_EINVAL, "at most 2^31 photons per sweep set and call");
     nmc_tissue_params tp{};
     tp.muav[1] = q.mua;
     tp.musv[1] = q.mus;
@@ -1136,6 +1138,8 @@ nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables,
   const double inv_d = 1.0 / std::min(h->rp.dx, std::min(h->rp.dy, h->rp.dz));
   for (int s = 0; s < n_sets; ++s) {
     if ((st = check_tissues(h, &tables[s], h->tiss_used, s)) != NMC_OK) return st;
+    if (photons[s] > (1ull << 31))  // per-set fixed-point sums stay below 2^63
+      return fail(h, NMC_EINVAL, "at most 2^31 photons per sweep set and call");
     nmc::XyzParams tmp{};
     nmc::fill_xyz(tmp, h->rp, tables[s], h->ext, h->sim);
     for (int t = 0; t < NMC_NTISS; ++t) {
