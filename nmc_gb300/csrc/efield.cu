@@ -94,11 +94,11 @@ struct EfParams {
   unsigned long long total;
   uint32_t k0, k1;
   double* sums;  // nsets * NMC_EF_FIELDS
-  float* sep;    // nsets * 2 * sep_n^2 complex, or null
+  double* sep;   // nsets * 2 * sep_n^2 complex (FP64 sums: no stagnation in long runs), or null
   int sep_n;
   float sep_inv, sep_half;
   double* pvs;   // nsets * 4 * (NMC_EF_MAX_ORDER + 1), or null
-  float* maps;   // nsets * NMC_EF_MAPS * map_n^2, or null
+  double* maps;  // nsets * NMC_EF_MAPS * map_n^2 (FP64 sums, returned as float), or null
   int map_n;
   float map_inv;
   double* depth;  // nsets * depth_bins, or null
@@ -169,6 +169,11 @@ struct PathSum {
   }
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
+
+__global__ void to_f32(const double* __restrict__ s, float* __restrict__ d, size_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    d[k] = (float)s[k];
+}
 
 // A unit vector perpendicular to u (the s direction z x u, or y for u along z).
 __device__ __forceinline__ void perp_of(float ux, float uy, float uz, float& px, float& py, float& pz) {
@@ -423,12 +428,12 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
         const int i = (int)floorf((lx - fx + P.sep_half) * P.sep_inv);
         const int j = (int)floorf((ly - fy + P.sep_half) * P.sep_inv);
         if (i >= 0 && i < P.sep_n && j >= 0 && j < P.sep_n) {
-          float* h0 = P.sep + (((size_t)set * 2) * SN + (size_t)i * P.sep_n + j) * 2;
-          float* h1 = h0 + (size_t)SN * 2;
-          atomicAdd(h0, w * cco.x);
-          atomicAdd(h0 + 1, w * cco.y);
-          atomicAdd(h1, w * ccr.x);
-          atomicAdd(h1 + 1, w * ccr.y);
+          double* h0 = P.sep + (((size_t)set * 2) * SN + (size_t)i * P.sep_n + j) * 2;
+          double* h1 = h0 + (size_t)SN * 2;
+          atomicAdd(h0, (double)(w * cco.x));
+          atomicAdd(h0 + 1, (double)(w * cco.y));
+          atomicAdd(h1, (double)(w * ccr.x));
+          atomicAdd(h1 + 1, (double)(w * ccr.y));
         } else {
           atomicAdd(&sm[NMC_EF_SEP_OUTSIDE], (double)(w * cco.x));
         }
@@ -446,19 +451,19 @@ __global__ void __launch_bounds__(256) efield_kernel(const EfParams P) {
     if (P.maps) {
       const int ix = (int)floorf(x * P.map_inv + 0.5f * P.map_n), iy = (int)floorf(y * P.map_inv + 0.5f * P.map_n);
       if (ix >= 0 && ix < P.map_n && iy >= 0 && iy < P.map_n) {
-        float* m = P.maps + (size_t)set * NMC_EF_MAPS * MN + (size_t)ix * P.map_n + iy;
+        double* m = P.maps + (size_t)set * NMC_EF_MAPS * MN + (size_t)ix * P.map_n + iy;
         const float ph_path = (float)fmod(path.value() * (double)P.med[0].kmed, 6.283185307179586);
         const float a_co = atan2f(Eco.y, Eco.x), a_cr = atan2f(Ecr.y, Ecr.x);
-        atomicAdd(m + NMC_EF_MAP_XX * (size_t)MN, Ixx);
-        atomicAdd(m + NMC_EF_MAP_XY * (size_t)MN, Ixy);
-        atomicAdd(m + NMC_EF_MAP_YX * (size_t)MN, Iyx);
-        atomicAdd(m + NMC_EF_MAP_YY * (size_t)MN, Iyy);
-        atomicAdd(m + NMC_EF_MAP_RD * (size_t)MN, w);
-        atomicAdd(m + NMC_EF_MAP_DET * (size_t)MN, 1.f);
-        atomicAdd(m + NMC_EF_MAP_PHASE0 * (size_t)MN, a_co);
-        atomicAdd(m + NMC_EF_MAP_PHASE1 * (size_t)MN, wrap_pi(ph_path));
-        atomicAdd(m + NMC_EF_MAP_PHASE2 * (size_t)MN, a_cr);
-        atomicAdd(m + NMC_EF_MAP_PHASE3 * (size_t)MN, wrap_pi(a_co + ph_path));
+        atomicAdd(m + NMC_EF_MAP_XX * (size_t)MN, (double)Ixx);
+        atomicAdd(m + NMC_EF_MAP_XY * (size_t)MN, (double)Ixy);
+        atomicAdd(m + NMC_EF_MAP_YX * (size_t)MN, (double)Iyx);
+        atomicAdd(m + NMC_EF_MAP_YY * (size_t)MN, (double)Iyy);
+        atomicAdd(m + NMC_EF_MAP_RD * (size_t)MN, (double)w);
+        atomicAdd(m + NMC_EF_MAP_DET * (size_t)MN, 1.0);
+        atomicAdd(m + NMC_EF_MAP_PHASE0 * (size_t)MN, (double)a_co);
+        atomicAdd(m + NMC_EF_MAP_PHASE1 * (size_t)MN, (double)wrap_pi(ph_path));
+        atomicAdd(m + NMC_EF_MAP_PHASE2 * (size_t)MN, (double)a_cr);
+        atomicAdd(m + NMC_EF_MAP_PHASE3 * (size_t)MN, (double)wrap_pi(a_co + ph_path));
         if (P.spk) {  // the pixel's speckle record (struct SPECKLE, definitions.h:220-229)
           const size_t pix = (size_t)ix * P.map_n + iy;
           const int k = atomicAdd(P.spk_count + (size_t)set * MN + pix, 1);
@@ -731,16 +736,18 @@ extern "C" nmc_status nmc_efield_run(int32_t device, const nmc_efield_config* cf
   unsigned long long* dpre = (unsigned long long*)dalloc(8 * (ns + 1));
   double* dsums = (double*)dalloc(sizeof(double) * ns * NMC_EF_FIELDS);
   unsigned long long* dwork = (unsigned long long*)dalloc(16);
+  double* dsep_d = cone ? (double*)dalloc(sizeof(double) * 2 * 2 * SN * ns) : nullptr;
   float* dsep = cone ? (float*)dalloc(sizeof(float) * 2 * 2 * SN * ns) : nullptr;
   double* dpvs = pol_vs_scatt ? (double*)dalloc(sizeof(double) * 4 * (NMC_EF_MAX_ORDER + 1) * ns) : nullptr;
+  double* dmaps_d = maps ? (double*)dalloc(sizeof(double) * NMC_EF_MAPS * MN * ns) : nullptr;
   float* dmaps = maps ? (float*)dalloc(sizeof(float) * NMC_EF_MAPS * MN * ns) : nullptr;
   double* ddepth = raman_depth ? (double*)dalloc(sizeof(double) * c.depth_bins * ns) : nullptr;
   const bool spk = maps && c.speckle_max > 0 && (speckles || speckle_counts);
   if (spk && c.speckle_max > 100000u) return done(NMC_EINVAL);
   nmc_speckle* dspk = spk ? (nmc_speckle*)dalloc(sizeof(nmc_speckle) * c.speckle_max * MN * ns) : nullptr;
   int* dspkc = spk ? (int*)dalloc(sizeof(int) * MN * ns) : nullptr;
-  if (!dS0 || !dS1 || !dcdf || !dsets || !dpre || !dsums || !dwork || (cone && !dsep) ||
-      (pol_vs_scatt && !dpvs) || (maps && !dmaps) || (raman_depth && !ddepth) || (spk && (!dspk || !dspkc)))
+  if (!dS0 || !dS1 || !dcdf || !dsets || !dpre || !dsums || !dwork || (cone && (!dsep || !dsep_d)) ||
+      (pol_vs_scatt && !dpvs) || (maps && (!dmaps || !dmaps_d)) || (raman_depth && !ddepth) || (spk && (!dspk || !dspkc)))
     return done(NMC_ENOMEM);
   if (cudaMemcpyAsync(dS0, S_primary, sizeof(float4) * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(dS1, raman ? S_raman : S_primary, sizeof(float4) * n, cudaMemcpyHostToDevice, st) !=
@@ -778,12 +785,12 @@ extern "C" nmc_status nmc_efield_run(int32_t device, const nmc_efield_config* cf
   P.k0 = (uint32_t)c.seed;
   P.k1 = (uint32_t)(c.seed >> 32);
   P.sums = dsums;
-  P.sep = dsep;
+  P.sep = dsep_d;
   P.sep_n = c.sep_n;
   P.sep_inv = cone ? (float)(c.sep_n / (2.0 * c.sep_half_width)) : 0.f;
   P.sep_half = c.sep_half_width;
   P.pvs = dpvs;
-  P.maps = dmaps;
+  P.maps = dmaps_d;
   P.map_n = maps ? c.map_n : 1;
   P.map_inv = maps ? (float)(1.0 / c.map_dx) : 0.f;
   P.depth = ddepth;
@@ -812,6 +819,8 @@ extern "C" nmc_status nmc_efield_run(int32_t device, const nmc_efield_config* cf
   void* args[] = {(void*)&P};
   if (P.total > 0 && cudaLaunchKernel(f, dim3((unsigned)grid), dim3(256), args, smem, st) != cudaSuccess)
     return done(NMC_EDEVICE);
+  if (cone) to_f32<<<1024, 256, 0, st>>>(dsep_d, dsep, 2 * 2 * SN * ns);
+  if (maps) to_f32<<<1024, 256, 0, st>>>(dmaps_d, dmaps, NMC_EF_MAPS * MN * ns);
   if (cone) {  // the 2-D Fourier sums, per setting and channel
     const int cn = c.cone_n, sn = c.sep_n;
     float2* W = (float2*)dalloc(sizeof(float2) * cn * sn);
