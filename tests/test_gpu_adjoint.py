@@ -240,3 +240,36 @@ def test_adjoint_costs_at_most_three_forwards(gpu, case):
           f"Rd + absorbed {t_adj_f * 1e3:.1f} ms ({t_adj_f / t_fwd:.2f}x)")
     assert t_adj <= 3.0 * t_fwd
     assert t_adj_f <= 4.0 * t_fwd  # every photon replayed twice
+
+
+def test_adjoint_satisfies_the_scaling_identity(gpu):
+    # A homogeneous semi-infinite medium under a pencil beam has no length
+    # scale of its own, so total Rd is unchanged when every mua and mus is
+    # scaled by the same factor: sum_v (mua_v dRd/dmua_v + mus_v dRd/dmus_v) = 0.
+    # The pathwise mua gradient and the likelihood-ratio mus gradient come from
+    # different estimators and must cancel in that sum, within its statistics.
+    N, d = 48, 0.01
+    rp, tp, v, ext, _, _, _, bins, dr = cases.adjoint_case(N=N, d=d)
+    rp.boundaryflag = 2  # photons beyond the sides and the bottom continue in the edge voxels' medium
+    mua = np.full((N, N, N), 1.0, np.float32)
+    mus = np.full((N, N, N), 100.0, np.float32)
+    g = np.full((N, N, N), 0.85, np.float32)
+    G = np.ones(bins + 1, np.float32)  # the loss is the total detected weight
+    B, per = 8, 200_000
+    a, s = [], []
+    with gpu.Engine(abi.SIM_MCXYZ, 0, ext) as e:
+        e.prepare_data(rp, tp, v)
+        e.set_radial_tally(bins, dr)
+        e.set_voxel_props(mua, mus, g)
+        for b in range(B):
+            e.reset()
+            e.adjoint_forward(b * per, per)
+            ga, gs, _ = e.adjoint_backward(G)
+            a.append(float((mua.ravel() * ga.ravel()).sum()) / per)
+            s.append(float((mus.ravel() * gs.ravel()).sum()) / per)
+    a, s = np.array(a), np.array(s)
+    tot = a + s
+    se = tot.std(ddof=1) / np.sqrt(B)
+    print(f"mua . dRd/dmua {a.mean():.5f}, mus . dRd/dmus {s.mean():.5f}, sum {tot.mean():.2e} +- {se:.1e}")
+    assert abs(tot.mean()) <= 3.5 * se + 1e-5
+    assert abs(a.mean()) >= 20 * se  # each side on its own is far from zero
