@@ -151,3 +151,25 @@ def test_layer_adjoint_matches_crn_finite_differences(gpu):
             assert np.all(np.abs(P - F) <= np.maximum(4.5 * d.std(0, ddof=1) / np.sqrt(B), 1e-3 * np.abs(F)))
         else:
             assert np.all(np.abs(t) <= 4.5)
+
+
+def test_layer_adjoint_satisfies_the_scaling_identity(gpu):
+    # one semi-infinite layer has no length scale: total Rd is unchanged when
+    # mua and mus are scaled alike, so mua dRd/dmua + mus dRd/dmus = 0 (the
+    # pathwise and likelihood-ratio parts cancel, within their statistics)
+    from nmc_gb300 import layered
+
+    lay = [(1.0, 100.0, 0.9, 1.4, math.inf)]
+    nr, B, nb = 40, 8, 200_000
+    G = np.ones(nr + 1, np.float32)
+    a, s = [], []
+    for b in range(B):
+        r = layered.adjoint(lay, nb, G, None, nr=nr, dr=0.05, first=b * nb, seed=4)
+        a.append(1.0 * r["grad_mua"][0] / nb)
+        s.append(100.0 * r["grad_mus"][0] / nb)
+    a, s = np.array(a), np.array(s)
+    tot = a + s
+    se = tot.std(ddof=1) / np.sqrt(B)
+    print(f"mua . dRd/dmua {a.mean():.5f}, mus . dRd/dmus {s.mean():.5f}, sum {tot.mean():.2e} +- {se:.1e}")
+    assert abs(tot.mean()) <= 3.5 * se + 1e-5
+    assert abs(a.mean()) >= 20 * se
