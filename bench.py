@@ -709,6 +709,62 @@ def run_layered_workload(args) -> dict:
     return out
 
 
+def run_speckle_workload(args) -> dict:
+    """CBS speckle mutual-interference post-processing (MetalMC.m:628-742):
+    a 256 x 256 exit map with 64 speckle records per pixel (seeded synthetic
+    maps and records of the E-field kernel's layout), on the GPU through
+    nmc_speckle_mutual (host arrays in and out), against the oracle's
+    single-threaded restatement of the reference's loop on the host."""
+    import math
+
+    import numpy as np
+
+    from nmc_gb300 import abi, build, efield
+
+    build.build()
+    rng = np.random.default_rng(17)
+    nx = ny = 256
+    kmax = 64
+    maps = np.zeros((len(abi.EF_MAPS), nx, ny), np.float32)
+    det = rng.integers(1, 200, (nx, ny)).astype(np.float32)
+    maps[abi.EF_MAPS.index("Det")] = det
+    for k in ("XX", "XY", "YX", "YY", "Rd"):
+        maps[abi.EF_MAPS.index(k)] = rng.uniform(0, 1, (nx, ny)) * det
+    for k in ("Phase0", "Phase1", "Phase2", "Phase3"):
+        maps[abi.EF_MAPS.index(k)] = rng.uniform(-math.pi, math.pi, (nx, ny)) * det
+    rec = np.zeros((kmax, nx, ny), abi.SPECKLE_DTYPE)
+    for f in ("Phase", "Path", "Scatt", "Total"):
+        rec[f] = rng.uniform(-math.pi, math.pi, rec.shape)
+    for f in ("XX", "XY", "Ryx"):
+        rec[f] = rng.uniform(0, 0.2, rec.shape)
+    counts = np.full((nx, ny), kmax, np.int32)
+    lam, lc = 633e-6, 0.05
+    for _ in range(max(args.warmup, 1)):
+        efield.speckle_mutual(maps, rec, counts, lam, lc)
+    best = None
+    for _ in range(max(args.steps, 1)):
+        t0 = time.perf_counter()
+        out = efield.speckle_mutual(maps, rec, counts, lam, lc)
+        t = time.perf_counter() - t0
+        best = t if best is None else min(best, t)
+    n_rec = nx * ny * kmax
+    res = {"metric": "speckle records/s, CBS mutual-interference post-processing", "unit": "records/s",
+           "value": n_rec / best, "seconds": best, "records": n_rec, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"{nx} x {ny} exit map, {kmax} speckle records per pixel, lambda 633 nm, "
+                                  f"coherence length {lc}",
+                      "timing": f"best of {max(args.steps, 1)} host-timed calls (copies in and out included)"}}
+    if not args.no_cpu:
+        from oracle import bindings as orc
+
+        t0 = time.perf_counter()
+        want = orc.speckle_mutual(maps, rec, counts, lam, lc, np.zeros((len(abi.EF_MAPS), nx * ny), np.float32))
+        dt = time.perf_counter() - t0
+        res["max_abs_diff_vs_oracle"] = float(np.abs(out.reshape(want.shape) - want).max())
+        res["cpu_baseline"] = {"value": n_rec / dt, "unit": "records/s", "cores": 1, "kind": "port",
+                               "sample": f"the whole workload, the oracle's restatement, 1 thread, {dt:.2f} s"}
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -725,7 +781,7 @@ def main():
                     help="autotune the launch shape on this many photons before the warm-up (0: defaults)")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warm-up and timed transport launches (for ncu)")
-    ap.add_argument("--workload", default="skinvessel", choices=["skinvessel", "sweep", "sweep_mcsub", "adjoint", "cbs", "layered"])
+    ap.add_argument("--workload", default="skinvessel", choices=["skinvessel", "sweep", "sweep_mcsub", "adjoint", "cbs", "layered", "speckle"])
     args = ap.parse_args()
     if args.workload == "sweep":
         out = run_sweep_workload(args)
@@ -737,6 +793,8 @@ def main():
         out = run_cbs_workload(args)
     elif args.workload == "layered":
         out = run_layered_workload(args)
+    elif args.workload == "speckle":
+        out = run_speckle_workload(args)
     else:
         out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if out:
