@@ -709,16 +709,18 @@ def run_layered_workload(args) -> dict:
     return out
 
 
-def run_notebook0_workload(args) -> dict:
-    """The reference's published throughput workload: NMC-samples/example0
-    (homogeneous 200^3 cube at 0.02, uniform beam of radius 1.2, mua 1,
-    mus 100, g 0.9, n 1.4/1.001), 1e5 photons, run as the notebook runs it:
-    `nmc test` on the files the notebook writes, with the reference's own
-    random streams.  The recorded reference run took 7.09 s of GPU time
-    (14,096 photons/s, AMD Radeon Pro 5500 XT, Metal); `value` is the same
-    "Total execution time (GPU)" measure here, and `wall_s` the whole process
+def run_notebook_workload(args) -> dict:
+    """The reference's published throughput workloads, run as the notebooks
+    run them: `nmc <name>` on the files the notebook writes, with the
+    reference's own random streams.
+      notebook0: example0 (homogeneous 200^3 cube at 0.02, uniform beam of
+        radius 1.2, mua 1, mus 100, g 0.9, n 1.4/1.001), 1e5 photons;
+        recorded 7.09 s of GPU time (14,096 photons/s).
+      notebook2: example2 (skin vessel, 200^3 at 0.0005 cm, 532 nm tissue
+        table), 1e6 photons; recorded 209.0 s (4,783 photons/s).
+    Both on an AMD Radeon Pro 5500 XT under Metal.  `value` is the same
+    "Total execution time (GPU)" measure here; `wall_s` the whole process
     (start-up, file reading and writing included)."""
-    import subprocess
     import tempfile
 
     import numpy as np
@@ -727,14 +729,28 @@ def run_notebook0_workload(args) -> dict:
     from nmc_gb300 import build, mci
 
     build.build()
+    if args.workload == "notebook0":
+        n, base, what = 100_000, 14096.0, "example0: 200^3 x 0.02 homogeneous cube, uniform beam r 1.2, mua 1, " \
+            "mus 100, g 0.9, n 1.4/1.001, 1e5 photons"
+        note = "14,096 photons/s: 1e5 photons in 7.09 s on an AMD Radeon Pro 5500 XT (example0.ipynb)"
+    else:
+        n, base, what = 1_000_000, 4783.0, "example2: skin vessel 200^3 x 0.0005 cm, 532 nm tissues, 1e6 photons"
+        note = "4,783 photons/s: 1e6 photons in 209.0 s on an AMD Radeon Pro 5500 XT (example2.ipynb)"
     walls, kern = [], []
     with tempfile.TemporaryDirectory() as d:
         name = os.path.join(d, "test")
-        cases.write_example0_mci(name + "_H.mci")
-        mci.write_tissue(name, np.ones(200 ** 3, np.uint8))
+        if args.workload == "notebook0":
+            cases.write_example0_mci(name + "_H.mci")
+            mci.write_tissue(name, np.ones(200 ** 3, np.uint8))
+        else:
+            spec = json.load(open(os.path.join(ROOT, "tests", "golden", "spectral_tissues.json")))
+            t532 = next(c for c in spec if c["nm"] == 532)["tissues"]
+            cases.write_notebook_mci(name + "_H.mci", [(round(t532[str(i)]["mua"], 4), round(t532[str(i)]["mus"], 4),
+                                                         round(t532[str(i)]["g"], 4)) for i in range(1, 10)])
+            mci.write_tissue(name, cases.notebook_skinvessel_map())
         for i in range(max(args.warmup, 1) + max(args.steps, 1)):
             t0 = time.perf_counter()
-            r = mci.run_nmc(name)
+            r = mci.run_nmc(name, "--photons", str(n))
             t = time.perf_counter() - t0
             if r.returncode != 0:
                 raise RuntimeError(r.stdout[-1000:] + r.stderr[-1000:])
@@ -743,15 +759,11 @@ def run_notebook0_workload(args) -> dict:
                 walls.append(t)
                 kern.append(rep["kernel_ms"] * 1e-3)
         rd = rep["Rd"]
-    n = 100_000
     k = min(kern)
-    return {"metric": "photons/s, example0 through the nmc program (GPU execution time)", "unit": "photons/s",
-            "value": n / k, "vs_baseline": (n / k) / 14096.0, "kernel_s": k, "wall_s": min(walls),
-            "photons": n, "rd": rd, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "example0: 200^3 x 0.02 homogeneous cube, uniform beam r 1.2, mua 1, mus 100, "
-                                   "g 0.9, n 1.4/1.001, 1e5 photons, reference random streams",
-                       "baseline": "14,096 photons/s: 1e5 photons in 7.09 s on an AMD Radeon Pro 5500 XT "
-                                   "(example0.ipynb)",
+    return {"metric": f"photons/s, {args.workload} through the nmc program (GPU execution time)",
+            "unit": "photons/s", "value": n / k, "vs_baseline": (n / k) / base, "kernel_s": k,
+            "wall_s": min(walls), "photons": n, "rd": rd, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": what + ", reference random streams", "baseline": note,
                        "timing": f"best of {max(args.steps, 1)} runs of the nmc program"}}
 
 
@@ -828,7 +840,7 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warm-up and timed transport launches (for ncu)")
     ap.add_argument("--workload", default="skinvessel", choices=["skinvessel", "sweep", "sweep_mcsub", "adjoint", "cbs", "layered", "speckle",
-                             "notebook0"])
+                             "notebook0", "notebook2"])
     args = ap.parse_args()
     if args.workload == "sweep":
         out = run_sweep_workload(args)
@@ -842,8 +854,8 @@ def main():
         out = run_layered_workload(args)
     elif args.workload == "speckle":
         out = run_speckle_workload(args)
-    elif args.workload == "notebook0":
-        out = run_notebook0_workload(args)
+    elif args.workload in ("notebook0", "notebook2"):
+        out = run_notebook_workload(args)
     else:
         out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if out:
