@@ -409,11 +409,6 @@ __global__ void unfix_f32(const unsigned long long* __restrict__ s, const double
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
     d[k] = (float)((double)s[k] * scale + (c ? c[k] : 0.0));
 }
-__global__ void unfix_f64(const unsigned long long* __restrict__ s, double* __restrict__ d, size_t n,
-                          double scale) {
-  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-    d[k] = (double)s[k] * scale;
-}
 __global__ void u32_to_f32(const unsigned int* __restrict__ s, const double* __restrict__ c,
                            float* __restrict__ d, size_t n) {
   // counts travel as int32 bits (the reference's DetPhot2D is int); saturate
