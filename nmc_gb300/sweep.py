@@ -10,7 +10,6 @@ files and running one `nmc` process per wavelength on the skin-vessel map
 from __future__ import annotations
 
 import copy
-import math
 
 import numpy as np
 

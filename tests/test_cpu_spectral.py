@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-from nmc_gb300 import abi, spectral
+from nmc_gb300 import spectral
 
 GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "spectral_tissues.json")))
 

@@ -4,9 +4,6 @@ and detection modes (kernels.metal:366-463 launch, :556-637 detection,
 exercise: odd and non-cubic grids, non-square voxels.  Same Philox streams
 on both sides; a photon matches when its fate, SPIN count, detected and
 absorbed weight agree (rel 1e-3)."""
-import math
-
-import numpy as np
 import pytest
 
 from nmc_gb300 import abi
