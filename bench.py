@@ -42,6 +42,11 @@ WORKLOAD = "mcxyz skin-vessel 200^3 @0.005 cm, 1e8 photons per GPU per step"
 # per-hop SPIN/roulette share.  Fixed once, not re-counted per build.
 OPS_PER_SUBSTEP = 64.0
 MUFU_PER_SUBSTEP = 3.0
+# Warp instructions the transport kernel issues per voxel sub-step
+# (smsp__inst_executed.sum / sub-steps of the 1e7-photon ncu capture of this
+# workload), and the SM's issue rate (4 warp instructions per clock).
+WARP_INSTR_PER_SUBSTEP = 3.755e11 / 2.557e10
+ISSUE_PER_SM_CLOCK = 4.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 1e8-photon
 # launch of the transport kernel, from one ncu capture of that launch.
 TRAFFIC_BYTES_1E8 = 72_138_240 + 28_571_801_856
@@ -86,6 +91,22 @@ def _clocks_summary(lines: list) -> dict:
                 reasons.add(n)
     return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
             "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _issue_estimate(substeps_per_s, clock_lines) -> dict | None:
+    import torch
+
+    c = _clocks_summary(clock_lines)
+    mhz = c.get("sm_mhz") if isinstance(c, dict) else None
+    if not substeps_per_s or not mhz:
+        return None
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    per_s = substeps_per_s * WARP_INSTR_PER_SUBSTEP
+    peak = sms * ISSUE_PER_SM_CLOCK * mhz * 1e6
+    return {"warp_instr_per_substep": WARP_INSTR_PER_SUBSTEP, "achieved_warp_instr_per_s": per_s,
+            "peak_warp_instr_per_s": peak, "frac": per_s / peak,
+            "source": "instructions per sub-step from ncu (profiles/mcxyz_skinvessel_1e7_full.txt), "
+                      "sub-step rate live, SMs x 4 issues per clock at the median sampled SM clock"}
 
 
 def cpu_sample(seconds: float = 12.0, threads: int | None = None) -> dict:
@@ -276,7 +297,11 @@ def run_ours(args) -> dict:
                      "mufu_peak_tlanes": mufu / 1e12,
                      "peak_source": "of measured FP32 FMA lane rate (nmc_probe_issue_peaks, live)",
                      "hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": hbm_peak, "peak_source": hbm_src,
-                             "frac": (hbm_gbs / hbm_peak) if hbm_gbs else None}},
+                             "frac": (hbm_gbs / hbm_peak) if hbm_gbs else None},
+                     # the instruction-issue ceiling for the instruction stream the kernel
+                     # executes: live sub-step rate x profiled instructions per sub-step
+                     # against 4 issues per SM clock at the sampled SM clock
+                     "issue": _issue_estimate(substeps / kernel_s if kernel_s > 0 else None, clock_lines)},
         "gpu_launches": launches,
         "clocks": _clocks_summary(clock_lines),
     }
