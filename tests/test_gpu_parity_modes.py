@@ -35,6 +35,30 @@ def test_mode_per_photon(gpu, oracle, mode):
     assert s["photons"] == n
 
 
+@pytest.mark.parametrize("mode", [m for m in MODES if m != "gaussian-beam"])
+def test_two_term_mode_per_photon(gpu, oracle, mode):
+    # the two-term kernel (kernels.metal:757-1118; its launch has no Gaussian
+    # branch) over the same launch, boundary and detection modes
+    kw = dict(MODES[mode])
+    grid = {k: kw.pop(k) for k in ("Nx", "Ny", "Nz", "dx", "dy", "dz") if k in kw}
+    rp, tp, v = _medium(**grid, **kw)
+    rp.mckernelflag = abi.SIM_MCXYZ_TT
+    for t in range(1, 4):
+        tp.gf[t], tp.af[t], tp.gb[t], tp.ab[t], tp.CC[t] = 0.9, 0.5, 0.3, 0.5, 0.9
+    ext = abi.ext_defaults(rng=abi.RNG_PHILOX, seed=23)
+    n = 3000
+    with gpu.Engine(abi.SIM_MCXYZ_TT, 0, ext) as e:
+        e.prepare_data(rp, tp, v)
+        recs, _ = e.run_traced(0, n)
+        s = e.summary()
+    o = oracle.run(abi.SIM_MCXYZ_TT, rp, tp, v, ext=ext, n=n, trace=True)
+    frac, _ = cases.match_fraction(recs, o["recs"])
+    print(f"two-term {mode}: per-photon match {frac:.4f}, Rd gpu {s['rd_sum'] / n:.5f} oracle "
+          f"{o['rd_sum'] / n:.5f}")
+    assert frac >= 0.9
+    assert s["photons"] == n
+
+
 @pytest.mark.parametrize("mcflag", [1, 2], ids=["gaussian-focus", "isotropic-point"])
 def test_mcsub_launch_modes_per_photon(gpu, oracle, mcflag):
     rp, tp, ext = cases.mcsub_case(g=0.9, seed=4)
