@@ -313,8 +313,11 @@ def run_ours(args) -> dict:
                                          f"reference's generator ({cs['substeps_per_photon']:.0f} sub-steps/photon), "
                                          f"{cs['seconds']:.1f} s"}
     if rank == 0 and world == 1 and not args.no_extras:
-        out["batched_to_1pct_se"] = batched_to_target_extra()
-        out["adjoint"] = adjoint_extra()
+        for key, fn in (("batched_to_1pct_se", batched_to_target_extra), ("adjoint", adjoint_extra)):
+            try:  # an extra that fails is reported in the line, not in place of it
+                out[key] = fn()
+            except Exception as exc:  # noqa: BLE001
+                out[key] = {"error": f"{type(exc).__name__}: {exc}"}
     if dist:
         dist.destroy_process_group()
     return out if rank == 0 else {}
