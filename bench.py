@@ -306,12 +306,15 @@ def run_ours(args) -> dict:
         "clocks": _clocks_summary(clock_lines),
     }
     if rank == 0 and world == 1 and not args.no_cpu:
-        cs = cpu_sample(12.0)
-        out["cpu_baseline"] = {"value": cs["photons_per_s"], "unit": "photons/s", "cores": cs["threads"],
-                               "kind": "port",
-                               "sample": f"{cs['photons']} photons of the same workload, FP32 restatement with the "
-                                         f"reference's generator ({cs['substeps_per_photon']:.0f} sub-steps/photon), "
-                                         f"{cs['seconds']:.1f} s"}
+        try:
+            cs = cpu_sample(12.0)
+            out["cpu_baseline"] = {"value": cs["photons_per_s"], "unit": "photons/s", "cores": cs["threads"],
+                                   "kind": "port",
+                                   "sample": f"{cs['photons']} photons of the same workload, FP32 restatement with "
+                                             f"the reference's generator ({cs['substeps_per_photon']:.0f} "
+                                             f"sub-steps/photon), {cs['seconds']:.1f} s"}
+        except Exception as exc:  # noqa: BLE001
+            out["cpu_baseline"] = {"value": None, "unit": "photons/s", "error": f"{type(exc).__name__}: {exc}"}
     if rank == 0 and world == 1 and not args.no_extras:
         for key, fn in (("batched_to_1pct_se", batched_to_target_extra), ("adjoint", adjoint_extra)):
             try:  # an extra that fails is reported in the line, not in place of it
