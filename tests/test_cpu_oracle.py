@@ -169,6 +169,32 @@ def test_fp32_oracle_replays_reference_in_every_mode(oracle, mode):
     assert abs(rd_orc - rd_ref) <= 0.02 * rd_ref + 1e-4
 
 
+@pytest.mark.parametrize("mode", [m for m in cases.PARITY_MODES if m != "gaussian-beam"])
+def test_two_term_fp32_oracle_replays_reference_in_every_mode(oracle, mode):
+    """MCXYZKernelTT (kernels.metal:757-1118, whose launch has no Gaussian
+    branch) compiled here against the oracle's FP32 restatement, in each
+    launch and detection mode, with boundaryflag 1: beyond the grid's sides
+    the reference writes Rd2D at an unclamped index (kernels.metal:984)."""
+    if not oracle.ref_available():
+        pytest.skip("reference sources not present")
+    kw = dict(cases.PARITY_MODES[mode])
+    kw["boundaryflag"] = 1
+    rp, tp, v = cases.modes_medium(**kw)
+    rp.mckernelflag = abi.SIM_MCXYZ_TT
+    for t in range(1, 4):
+        tp.gf[t], tp.af[t], tp.gb[t], tp.ab[t], tp.CC[t] = 0.9, 0.5, 0.3, 0.5, 0.9
+    n = 4000
+    ext = abi.ext_defaults(rng=abi.RNG_TAUS_REF, photons_per_dispatch=n, flags=abi.FLAG_TT_REPLAY_RUN1)
+    r = oracle.ref_mcxyz_tt(rp, tp, v, 1, 1, n, replay_run1=True, per_photon=True)
+    o = oracle.run(abi.SIM_MCXYZ_TT, rp, tp, v, ext=ext, n=n, trace=True, real_bits=32)
+    d = np.abs(r["per_photon"] - o["recs"]["detected"])
+    agree = np.mean(d <= 1e-5 + 1e-4 * np.abs(r["per_photon"]))
+    rd_ref, rd_orc = r["rd_slots"].sum() / n, o["rd_sum"] / n
+    print(f"two-term {mode}: per-photon agreement {agree:.4f}, Rd reference {rd_ref:.5f} oracle {rd_orc:.5f}")
+    assert agree >= 0.8
+    assert abs(rd_orc - rd_ref) <= 0.02 * rd_ref + 1e-4
+
+
 def test_notebook_rd_reproduced_by_reference_build(oracle):
     """example0.ipynb cell 5 records Rd = 0.26601276 for 1e5 photons of its
     homogeneous cube (Metal, AMD Radeon Pro 5500 XT).  The reference kernel
