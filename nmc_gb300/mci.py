@@ -7,6 +7,7 @@ mcio.h:16-171 reads them; the tissue map as raw uint8); readers parse what
 """
 from __future__ import annotations
 
+import json
 import os
 import subprocess
 
@@ -98,3 +99,46 @@ def read_mcout(path: str = "mcOUT0.dat") -> dict:
     return {"mua": head[0], "mus": head[1], "g": head[2], "n1": head[3], "n2": head[4], "NR": int(head[11]),
             "dr": head[13], "dz": head[14], "photons": head[15], "S": head[16], "A": head[17], "E": head[18],
             "r": r, "J": J, "z": z, "F": F}
+
+
+def merge_replicas(names, out: str, Nx: int, Ny: int, Nz: int) -> dict:
+    """Combines the outputs of independent `nmc` runs of one voxel problem
+    (replicas on other GPUs or boxes, each with its own Philox seed or photon
+    range) into one run of all their photons, in FP64: _F.bin and _Ryx.dat
+    are photon-weighted means of the per-run normalised values, _DetPhot2D.dat
+    is the sum of the counts, Rd the photon-weighted mean with the standard
+    errors combined as independent.  Reads each <name>_report.json; writes
+    <out>_F.bin, _Rd.dat, _Ryx.dat, _DetPhot2D.dat and _report.json in the
+    formats `nmc` writes (main.m:473-561).  Returns the merged report."""
+    reps = []
+    for n in names:
+        with open(f"{n}_report.json") as f:
+            reps.append(json.load(f))
+    N = np.array([float(r["photons"]) for r in reps])
+    tot = float(N.sum())
+    nv, n2d = Nx * Ny * Nz, Nx * Ny
+    F = np.zeros(nv)
+    ryx = np.zeros((Nx, Ny))
+    det = np.zeros((Nx, Ny), np.int64)
+    for n, w in zip(names, N):
+        F += w * np.fromfile(f"{n}_F.bin", dtype=np.float32, count=nv).astype(np.float64)
+        ryx += w * read_table(f"{n}_Ryx.dat")
+        det += read_table(f"{n}_DetPhot2D.dat", int).astype(np.int64)
+    F /= tot
+    ryx /= tot
+    rd = float(sum(w * r["Rd"] for w, r in zip(N, reps)) / tot)
+    se = float(np.sqrt(sum((w * r["Rd_se"]) ** 2 for w, r in zip(N, reps))) / tot)
+    F.astype(np.float32).tofile(f"{out}_F.bin")
+    with open(f"{out}_Rd.dat", "w") as f:
+        f.write(f"{rd:0.4f}\n")
+    with open(f"{out}_Ryx.dat", "w") as f:
+        for row in ryx:
+            f.write("".join(f"\t {v:1.6e}" for v in row) + "\n")
+    with open(f"{out}_DetPhot2D.dat", "w") as f:
+        for row in det:
+            f.write("".join(f"\t {int(v)}" for v in row) + "\n")
+    merged = {"name": os.path.basename(out), "photons": int(tot), "Rd": rd, "Rd_se": se,
+              "replicas": [{"name": n, "photons": int(w), "rng": r.get("rng")} for n, w, r in zip(names, N, reps)]}
+    with open(f"{out}_report.json", "w") as f:
+        json.dump(merged, f)
+    return merged

@@ -5,6 +5,7 @@ status 1 instead of a crash."""
 import os
 import subprocess
 
+import numpy as np
 import pytest
 
 from nmc_gb300 import abi, mci
@@ -82,3 +83,46 @@ def test_errors_exit_1(cli, tmp_path):
     assert r.returncode == 1
     r = subprocess.run([mci.NMC], capture_output=True, text=True)
     assert r.returncode == 0 and "USAGE" in r.stdout
+
+
+def test_merge_replicas_is_the_photon_weighted_run(tmp_path):
+    # three replica runs of one voxel problem, written in the formats `nmc`
+    # writes; the merge equals one run of all their photons
+    import json
+
+    rng = np.random.default_rng(5)
+    Nx = Ny = 6
+    Nz = 4
+    names, Ns, Fs, R, D, rds, ses = [], [100, 300, 600], [], [], [], [], []
+    for k, n in enumerate(Ns):
+        name = str(tmp_path / f"rep{k}")
+        F = rng.uniform(0, 5, Nx * Ny * Nz).astype(np.float32)
+        ryx = rng.uniform(0, 1, (Nx, Ny))
+        det = rng.integers(0, 50, (Nx, Ny))
+        F.tofile(name + "_F.bin")
+        with open(name + "_Ryx.dat", "w") as f:
+            for row in ryx:
+                f.write("".join(f"\t {v:1.6e}" for v in row) + "\n")
+        with open(name + "_DetPhot2D.dat", "w") as f:
+            for row in det:
+                f.write("".join(f"\t {int(v)}" for v in row) + "\n")
+        rd, se = rng.uniform(0.2, 0.3), rng.uniform(0.001, 0.003)
+        json.dump({"photons": n, "Rd": rd, "Rd_se": se, "rng": "philox4x32-10"}, open(name + "_report.json", "w"))
+        names.append(name)
+        Fs.append(F.astype(np.float64))
+        R.append(np.array([[float(f"{v:1.6e}") for v in row] for row in ryx]))
+        D.append(det)
+        rds.append(rd)
+        ses.append(se)
+    out = str(tmp_path / "merged")
+    m = mci.merge_replicas(names, out, Nx, Ny, Nz)
+    w = np.array(Ns, float)
+    assert m["photons"] == 1000
+    assert m["Rd"] == pytest.approx(float((w * np.array(rds)).sum() / 1000), rel=1e-12)
+    assert m["Rd_se"] == pytest.approx(float(np.sqrt(((w * np.array(ses)) ** 2).sum()) / 1000), rel=1e-12)
+    F = np.fromfile(out + "_F.bin", np.float32)
+    np.testing.assert_allclose(F, (sum(wi * f for wi, f in zip(w, Fs)) / 1000).astype(np.float32), rtol=1e-7)
+    np.testing.assert_allclose(mci.read_table(out + "_Ryx.dat"), sum(wi * r for wi, r in zip(w, R)) / 1000,
+                               rtol=1e-6)
+    np.testing.assert_array_equal(mci.read_table(out + "_DetPhot2D.dat", int), sum(D))
+    assert mci.read_rd(out) == pytest.approx(round(m["Rd"], 4))
