@@ -101,3 +101,28 @@ def test_python_mirrors_of_the_new_structs():
     assert C.sizeof(abi.TuneResult) == 804
     assert abi.SPECKLE_DTYPE.itemsize == 28
     assert C.sizeof(abi.SweepSet) == 64
+
+
+def test_integration_c_snippet_compiles(tmp_path):
+    # the C host binding shown to maintainers compiles against include/nmc_abi.h
+    import re
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    doc = open(os.path.join(root, "INTEGRATION.md")).read()
+    snippet = re.search(r"```c\n(.*?)```", doc, re.S).group(1)
+    body = "\n".join(ln for ln in snippet.splitlines() if not ln.startswith("#include"))
+    src = tmp_path / "host.c"
+    src.write_text(
+        "#include <stdio.h>\n#include <stdint.h>\n#include \"nmc_abi.h\"\n"
+        "void host(nmc_run_params runParams, nmc_tissue_params tissParams, const char* v, int NumGPURuns,\n"
+        "          float t_seed, float* ResJ_GPU, float* ResF_GPU, float* ResF3D_GPU, float* ResSAE_GPU,\n"
+        "          float* ResRd_GPU, float* ResRd2D_GPU, int32_t* ResDetPhotons2D_GPU) {\n"
+        + body + "\n}\n")
+    r = subprocess.run([cc, "-std=c11", "-Wall", "-Werror", "-fsyntax-only", f"-I{os.path.join(root, 'include')}",
+                        str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
