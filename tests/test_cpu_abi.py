@@ -126,3 +126,23 @@ def test_integration_c_snippet_compiles(tmp_path):
     r = subprocess.run([cc, "-std=c11", "-Wall", "-Werror", "-fsyntax-only", f"-I{os.path.join(root, 'include')}",
                         str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_integration_python_snippets_parse():
+    # every Python example shown to maintainers is valid Python and names
+    # functions the package has
+    import ast
+    import importlib
+    import re
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    doc = open(os.path.join(root, "INTEGRATION.md")).read()
+    blocks = re.findall(r"```python\n(.*?)```", doc, re.S)
+    assert blocks
+    for b in blocks:
+        tree = ast.parse(b)
+        for node in ast.walk(tree):
+            if isinstance(node, ast.ImportFrom) and node.module and node.module.startswith("nmc_gb300"):
+                for a in node.names:
+                    mod = importlib.import_module(node.module)
+                    assert hasattr(mod, a.name) or importlib.util.find_spec(f"{node.module}.{a.name}"), a.name
