@@ -118,3 +118,30 @@ def test_folded_tallies_equal_unfolded(gpu, kind):
             e.set_fold_interval(0)
         with pytest.raises(gpu.NMCError):
             e.set_fold_interval(2 ** 31 + 1)
+
+
+def test_handles_on_two_host_threads(gpu):
+    # one handle per host thread: two handles run concurrently from two
+    # threads (each on its own stream) and give the results each gives alone
+    import threading
+
+    rp, tp, v, ext = cases.skin_vessel_case(N=48)
+
+    def run(first, out, key):
+        with gpu.Engine(abi.SIM_MCXYZ, 0, ext) as e:
+            e.prepare_data(rp, tp, v)
+            e.run(first, 30_000)
+            out[key] = (e.summary(), e.tally(abi.TALLY_F3D))
+
+    alone, together = {}, {}
+    run(0, alone, "a")
+    run(10_000_000, alone, "b")
+    th = [threading.Thread(target=run, args=(f, together, k)) for f, k in ((0, "a"), (10_000_000, "b"))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for k in ("a", "b"):
+        for f in ("photons", "substeps", "S", "A", "E", "rd_sum"):
+            assert alone[k][0][f] == together[k][0][f], (k, f)
+        np.testing.assert_array_equal(alone[k][1], together[k][1])
