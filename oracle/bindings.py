@@ -78,6 +78,8 @@ def oracle_lib():
         lib.orc_speckle_mutual.restype = None
         lib.orc_layered_run.restype = C.c_int
         lib.orc_layered_run.argtypes = [C.c_int, _P, _P, C.c_uint64, C.c_uint64, C.c_int, _P, _P, _P, _P, _P]
+        lib.orc_efield_run.restype = C.c_int
+        lib.orc_efield_run.argtypes = [C.c_int, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int, _P]
         _oracle = lib
     return _oracle
 
@@ -263,3 +265,21 @@ def layered(layers, photons: int, n_above: float = 1.0, n_below: float = 1.0, nr
         res[k.lower() + "_se"] = math.sqrt(max(res[k + "2"] / n - m * m, 0.0) / n)
     res.update(rd_r=rd, tt_r=tt, a_z=az, a_layer=al)
     return res
+
+
+def efield(cfg: abi.EfieldConfig, S_primary, settings, S_raman=None, cone: bool = False, real_bits: int = 64,
+           nthreads: int | None = None) -> dict:
+    """The engine's polarised E-field model on the CPU (orc_efield_run): the
+    per-setting sums of nmc_gb300.efield.run (keys abi.EF_FIELDS), each an
+    array over `settings`."""
+    lib = oracle_lib()
+    n = len(settings)
+    arr = (abi.EfieldSetting * n)(*settings)
+    S0 = np.ascontiguousarray(S_primary, np.float32)
+    S1 = None if S_raman is None else np.ascontiguousarray(S_raman, np.float32)
+    out = np.zeros((n, len(abi.EF_FIELDS)), np.float64)
+    st = lib.orc_efield_run(int(real_bits), C.addressof(cfg), _ptr(S0), _ptr(S1), C.addressof(arr), n, int(cone),
+                            int(nthreads or os.cpu_count() or 1), _ptr(out))
+    if st != 0:
+        raise RuntimeError(f"orc_efield_run failed with status {st}")
+    return {k: out[:, i] for i, k in enumerate(abi.EF_FIELDS)}

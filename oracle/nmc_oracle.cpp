@@ -1060,6 +1060,320 @@ void layered_photon(const LayGeom& G, uint64_t pid, LayTally& T) {
   T.s[NMC_LAY_INTERACTIONS] += (double)hop;
 }
 
+// ------------------------------------------------- polarised E-field model
+// The engine's E-field transport behind nmc_efield_run, restated in R (the
+// reference's E-field and Raman kernels are empty, kernels.metal:1122-1202):
+// each photon carries a right-handed frame (e_par, e_perp, u) and a complex
+// 2x2 Jones matrix T (rows par, perp; columns the lab inputs x, y).  theta
+// from the inverse CDF of the unpolarised Mie phase function (linear within a
+// table interval), phi from 1 + beta cos(2 phi - 2 phi0) by a safeguarded
+// Newton inversion of its CDF, then T <- diag(S2, S1) R(phi) T rescaled to
+// |T|_F^2 = 2.  Unpolarised Fresnel escape or mirror at z = 0; Raman
+// conversion to the second table, isotropic and unpolarised; roulette below
+// 1e-4 (chance 0.1).  Random numbers as the engine draws them: Philox4x32-10,
+// key (seed lo, seed hi + setting), counter (photon lo, photon hi, hop,
+// 'EFLD'): x step, y theta (or emission cos), z phi, w Raman choice; the aux
+// block (hop | 2^30) gives x the Fresnel choice and y roulette.
+constexpr uint32_t kEfTag = 0x45464C44u;
+
+struct EfInput {
+  nmc_efield_config c;
+  int n;
+  std::vector<float> S[2];    // 4 floats per angle: S1 re, im, S2 re, im
+  std::vector<float> cdf[2];  // as the engine builds it (FP64 trapezoids, stored as float)
+  double inv_mut[2], surv[2], p_raman[2];
+  float dtheta;
+  bool cone;
+  float sep_inv, sep_half;
+};
+
+bool ef_cdf(const float* S, int n, std::vector<float>& cdf) {
+  std::vector<double> c(n, 0.0);
+  const double dth = 3.14159265358979323846 / (n - 1);
+  auto dens = [&](int j) {
+    const double p = 0.5 * ((double)S[4 * j] * S[4 * j] + (double)S[4 * j + 1] * S[4 * j + 1] +
+                            (double)S[4 * j + 2] * S[4 * j + 2] + (double)S[4 * j + 3] * S[4 * j + 3]);
+    return p * std::sin(dth * j);
+  };
+  for (int j = 1; j < n; ++j) c[j] = c[j - 1] + 0.5 * (dens(j - 1) + dens(j)) * dth;
+  if (!(c[n - 1] > 0.0) || !std::isfinite(c[n - 1])) return false;
+  cdf.resize(n);
+  for (int j = 0; j < n; ++j) cdf[j] = (float)(c[j] / c[n - 1]);
+  cdf[0] = 0.f;
+  cdf[n - 1] = 1.f;
+  return true;
+}
+
+template <class R>
+struct Cx {
+  R re, im;
+};
+template <class R>
+Cx<R> cmul(Cx<R> a, Cx<R> b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <class R>
+R cnorm(Cx<R> a) {
+  return a.re * a.re + a.im * a.im;
+}
+
+// phi with CDF (phi + beta/2 (sin(2 phi - tp0) + sin tp0)) / (2 pi) = u; s0, c0 = sin, cos tp0
+template <class R>
+R ef_phi(R u, R beta, R s0, R c0) {
+  const R two_pi = R(2.0 * 3.14159265358979323846);
+  const R target = two_pi * u;
+  if (std::fabs(beta) < R(1e-6)) return target;
+  R lo = 0, hi = two_pi, phi = target;
+  for (int it = 0; it < 40; ++it) {
+    const R s2 = std::sin(R(2) * phi), c2 = std::cos(R(2) * phi);
+    const R sa = s2 * c0 - c2 * s0, ca = c2 * c0 + s2 * s0;
+    const R G = phi + R(0.5) * beta * (sa + s0) - target;
+    if (std::fabs(G) < R(2e-6)) break;
+    if (G > 0)
+      hi = phi;
+    else
+      lo = phi;
+    const R dG = R(1) + beta * ca;
+    R nx = dG > R(1e-6) ? phi - G / dG : R(0.5) * (lo + hi);
+    if (!(nx > lo && nx < hi)) nx = R(0.5) * (lo + hi);
+    phi = nx;
+  }
+  return phi;
+}
+
+template <class R>
+void ef_perp(R ux, R uy, R& px, R& py, R& pz) {
+  const R n2 = ux * ux + uy * uy;
+  if (n2 < R(1e-12)) {
+    px = 0;
+    py = 1;
+  } else {
+    const R r = R(1) / std::sqrt(n2);
+    px = -uy * r;
+    py = ux * r;
+  }
+  pz = 0;
+}
+
+template <class R>
+void ef_photon(const EfInput& in, const nmc_efield_setting& q, uint32_t set, uint64_t pid, double* o) {
+  const nmc_efield_config& c = in.c;
+  const uint32_t k0 = (uint32_t)c.seed, k1 = (uint32_t)(c.seed >> 32) + set;
+  const uint32_t c0 = (uint32_t)pid, c1 = (uint32_t)(pid >> 32);
+  auto block = [&](uint32_t c2, uint32_t* out) {
+    uint32_t b[4] = {c0, c1, c2, kEfTag};
+    philox10(b, k0, k1);
+    std::memcpy(out, b, sizeof b);
+  };
+  auto u01 = [](uint32_t x) { return R(x >> 9) * R(1.0 / 8388608.0) + R(1.0 / 16777216.0); };
+  // launch: refracted direction, its s direction, initial T (the engine's host set-up)
+  const double st_ = std::sin((double)q.theta_in) * c.n_outside / c.n_medium, ct_ = std::sqrt(1.0 - st_ * st_);
+  R ux = R(st_ * std::cos((double)q.phi_in)), uy = R(st_ * std::sin((double)q.phi_in)), uz = R(ct_);
+  R px, py, pz;
+  if (st_ < 1e-9) {
+    px = 0;
+    py = 1;
+    pz = 0;
+  } else {
+    ef_perp<R>(ux, uy, px, py, pz);
+  }
+  Cx<R> T00, T01, T10, T11;
+  {
+    const R qx = py * uz - pz * uy, qy = pz * ux - px * uz, qz = px * uy - py * ux;
+    R t[2][2], f = 0;
+    for (int b = 0; b < 2; ++b) {
+      R bx = b == 0 ? 1 : 0, by = b == 0 ? 0 : 1, bz = 0;
+      const R du = bx * ux + by * uy + bz * uz;
+      bx -= du * ux;
+      by -= du * uy;
+      bz -= du * uz;
+      t[0][b] = bx * qx + by * qy + bz * qz;
+      t[1][b] = bx * px + by * py + bz * pz;
+      f += t[0][b] * t[0][b] + t[1][b] * t[1][b];
+    }
+    const R sc = std::sqrt(R(2) / f);
+    T00 = {t[0][0] * sc, 0};
+    T01 = {t[0][1] * sc, 0};
+    T10 = {t[1][0] * sc, 0};
+    T11 = {t[1][1] * sc, 0};
+  }
+  R dummy;
+  const R w0 = R(1) - rfresnel<R>(R(c.n_outside), R(c.n_medium), R(std::cos((double)q.theta_in)), &dummy);
+  o[NMC_EF_PHOTONS] += 1.0;
+  o[NMC_EF_SPECULAR] += (double)(R(1) - w0);
+  R x = 0, y = 0, z = 0, w = w0, fx = 0, fy = 0, lx = 0, ly = 0;
+  int med = 0;
+  uint32_t nsc = 0, hop = 0;
+  bool alive = true, escaped = false;
+  while (alive) {
+    uint32_t r[4];
+    block(hop, r);
+    const R s = -std::log(u01(r[0])) * R(in.inv_mut[med]);
+    if (uz < 0 && z + s * uz < 0) {  // reaches the surface
+      const R d = -z / uz;
+      x += d * ux;
+      y += d * uy;
+      z = 0;
+      R uzt;
+      const R rsp = rfresnel<R>(R(c.n_medium), R(c.n_outside), -uz, &uzt);
+      uint32_t a[4];
+      block(hop | 0x40000000u, a);
+      if (u01(a[0]) > rsp) {
+        escaped = true;
+        break;
+      }
+      uz = -uz;
+      px = -px;
+      py = -py;
+      T10 = {-T10.re, -T10.im};
+      T11 = {-T11.re, -T11.im};
+      const R rest = s - d;
+      x += rest * ux;
+      y += rest * uy;
+      z = rest * uz;
+    } else {
+      x += s * ux;
+      y += s * uy;
+      z += s * uz;
+    }
+    w *= R(in.surv[med]);
+    if (med == 0 && u01(r[3]) < R(in.p_raman[0])) {  // Raman conversion
+      med = 1;
+      o[NMC_EF_RAMAN_N] += 1.0;
+      const R ct = R(2) * u01(r[1]) - R(1), st = std::sqrt(std::max(R(0), R(1) - ct * ct));
+      const R ps = R(2.0 * 3.14159265358979323846) * u01(r[2]);
+      ux = st * std::cos(ps);
+      uy = st * std::sin(ps);
+      uz = ct;
+      ef_perp<R>(ux, uy, px, py, pz);
+      T00 = {1, 0};
+      T01 = {0, 0};
+      T10 = {0, 0};
+      T11 = {1, 0};
+    } else {  // scattering
+      const std::vector<float>& cdf = in.cdf[med];
+      const std::vector<float>& S = in.S[med];
+      const R uth = u01(r[1]);
+      int a0 = 0, a1 = in.n - 1;
+      while (a1 - a0 > 1) {
+        const int mid = (a0 + a1) >> 1;
+        if (R(cdf[mid]) <= uth) a0 = mid; else a1 = mid;
+      }
+      const R q0 = cdf[a0], q1 = cdf[a1];
+      const R fr = q1 > q0 ? std::min(std::max((uth - q0) / (q1 - q0), R(0)), R(1)) : R(0.5);
+      const R th = (R(a0) + fr) * R(in.dtheta);
+      const R sth = std::sin(th), cth = std::cos(th);
+      auto lerp = [&](int k) { return R(S[4 * a0 + k]) + fr * (R(S[4 * a1 + k]) - R(S[4 * a0 + k])); };
+      const Cx<R> S1 = {lerp(0), lerp(1)}, S2 = {lerp(2), lerp(3)};
+      const R Pp = cnorm(T00) + cnorm(T01), Qp = cnorm(T10) + cnorm(T11);
+      const R Cp = T00.re * T10.re + T00.im * T10.im + T01.re * T11.re + T01.im * T11.im;
+      const R s1 = cnorm(S1), s2 = cnorm(S2), hd = R(0.5) * (Pp - Qp);
+      const R rho = std::sqrt(hd * hd + Cp * Cp), den = (s1 + s2) * R(0.5) * (Pp + Qp);
+      const R beta = den > 0 ? std::min(std::max((s2 - s1) * rho / den, R(-1)), R(1)) : R(0);
+      const R irho = rho > 0 ? R(1) / rho : R(0);
+      const R phi = ef_phi<R>(u01(r[2]), beta, Cp * irho, hd * irho);
+      const R sph = std::sin(phi), cph = std::cos(phi);
+      const R qx = py * uz - pz * uy, qy = pz * ux - px * uz, qz = px * uy - py * ux;  // e_par
+      const R e1x = cph * qx + sph * px, e1y = cph * qy + sph * py, e1z = cph * qz + sph * pz;
+      R e2x = -sph * qx + cph * px, e2y = -sph * qy + cph * py, e2z = -sph * qz + cph * pz;
+      R nux = cth * ux + sth * e1x, nuy = cth * uy + sth * e1y, nuz = cth * uz + sth * e1z;
+      const R ru = R(1) / std::sqrt(nux * nux + nuy * nuy + nuz * nuz);
+      nux *= ru;
+      nuy *= ru;
+      nuz *= ru;
+      const R dp = e2x * nux + e2y * nuy + e2z * nuz;
+      e2x -= dp * nux;
+      e2y -= dp * nuy;
+      e2z -= dp * nuz;
+      const R rp = R(1) / std::sqrt(e2x * e2x + e2y * e2y + e2z * e2z);
+      ux = nux;
+      uy = nuy;
+      uz = nuz;
+      px = e2x * rp;
+      py = e2y * rp;
+      pz = e2z * rp;
+      const Cx<R> b00 = {cph * T00.re + sph * T10.re, cph * T00.im + sph * T10.im};
+      const Cx<R> b01 = {cph * T01.re + sph * T11.re, cph * T01.im + sph * T11.im};
+      const Cx<R> b10 = {-sph * T00.re + cph * T10.re, -sph * T00.im + cph * T10.im};
+      const Cx<R> b11 = {-sph * T01.re + cph * T11.re, -sph * T01.im + cph * T11.im};
+      T00 = cmul(S2, b00);
+      T01 = cmul(S2, b01);
+      T10 = cmul(S1, b10);
+      T11 = cmul(S1, b11);
+      const R fn = cnorm(T00) + cnorm(T01) + cnorm(T10) + cnorm(T11);
+      const R sc = fn > 0 ? std::sqrt(R(2) / fn) : R(0);
+      for (Cx<R>* t : {&T00, &T01, &T10, &T11}) {
+        t->re *= sc;
+        t->im *= sc;
+      }
+      if (med == 0) {
+        if (nsc == 0) {
+          fx = x;
+          fy = y;
+        }
+        lx = x;
+        ly = y;
+      }
+      ++nsc;
+    }
+    if (w < R(1e-4)) {
+      uint32_t a[4];
+      block(hop | 0x40000000u, a);
+      if (u01(a[1]) <= R(0.1))
+        w *= R(10);
+      else
+        alive = false;
+    }
+    if (++hop >= 20000000u) alive = false;
+  }
+  o[NMC_EF_SCATTERS] += nsc;
+  if (!escaped) return;
+  const R qx = py * uz - pz * uy, qy = pz * ux - px * uz, qz = px * uy - py * ux;  // e_par
+  Cx<R> A[2][2];
+  for (int a = 0; a < 2; ++a) {
+    R ax = a == 0 ? 1 : 0, ay = a == 0 ? 0 : 1, az = 0;
+    const R du = ax * ux + ay * uy;
+    ax -= du * ux;
+    ay -= du * uy;
+    az -= du * uz;
+    const R ra = R(1) / std::sqrt(std::max(ax * ax + ay * ay + az * az, R(1e-20)));
+    const R cpar = (ax * qx + ay * qy + az * qz) * ra, cperp = (ax * px + ay * py + az * pz) * ra;
+    A[a][0] = {T00.re * cpar + T10.re * cperp, T00.im * cpar + T10.im * cperp};
+    A[a][1] = {T01.re * cpar + T11.re * cperp, T01.im * cpar + T11.im * cperp};
+  }
+  const R ex = R(std::cos(q.pol_angle)), ey = R(std::sin(q.pol_angle));
+  const Cx<R> Fx = {A[0][0].re * ex + A[0][1].re * ey, A[0][0].im * ex + A[0][1].im * ey};
+  const Cx<R> Fy = {A[1][0].re * ex + A[1][1].re * ey, A[1][0].im * ex + A[1][1].im * ey};
+  const Cx<R> Eco = {ex * Fx.re + ey * Fy.re, ex * Fx.im + ey * Fy.im};
+  const Cx<R> Ecr = {-ey * Fx.re + ex * Fy.re, -ey * Fx.im + ex * Fy.im};
+  const R Ico = w * cnorm(Eco), Icr = w * cnorm(Ecr);
+  if (med == 1) {
+    o[NMC_EF_RAMAN_RD] += (double)w;
+    o[NMC_EF_RAMAN_CO] += (double)Ico;
+    o[NMC_EF_RAMAN_CROSS] += (double)Icr;
+    return;
+  }
+  o[NMC_EF_RD] += (double)w;
+  o[NMC_EF_RD2] += (double)w * (double)w;
+  o[NMC_EF_CO] += (double)Ico;
+  o[NMC_EF_CROSS] += (double)Icr;
+  if (nsc >= 2) {  // the time-reversed partner: the transposed lab-frame amplitude
+    const Cx<R> Gx = {-A[0][0].re * ey + A[0][1].re * ex, -A[0][0].im * ey + A[0][1].im * ex};
+    const Cx<R> Gy = {-A[1][0].re * ey + A[1][1].re * ex, -A[1][0].im * ey + A[1][1].im * ex};
+    const Cx<R> Er = {ex * Gx.re + ey * Gy.re, ex * Gx.im + ey * Gy.im};
+    const R cco = cnorm(Eco), ccr = Ecr.re * Er.re + Ecr.im * Er.im;  // Re(Ecr conj(Er))
+    o[NMC_EF_MULTI_CO] += (double)Ico;
+    o[NMC_EF_MULTI_CROSS] += (double)Icr;
+    o[NMC_EF_INTERF_CO] += (double)(w * cco);
+    o[NMC_EF_INTERF_CROSS] += (double)(w * ccr);
+    if (in.cone) {
+      const int i = (int)std::floor((double)((lx - fx + R(in.sep_half)) * R(in.sep_inv)));
+      const int j = (int)std::floor((double)((ly - fy + R(in.sep_half)) * R(in.sep_inv)));
+      if (!(i >= 0 && i < c.sep_n && j >= 0 && j < c.sep_n)) o[NMC_EF_SEP_OUTSIDE] += (double)(w * cco);
+    }
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -1157,6 +1471,55 @@ double orc_tt_costheta(double gf, double af, double gb, double ab, double cc, do
 }
 
 double orc_hg_costheta(double g, double u) { return hg_costheta<double>(g, u); }
+
+int orc_efield_run(int real_bits, const nmc_efield_config* cfg, const float* S_primary, const float* S_raman,
+                   const nmc_efield_setting* settings, int n_settings, int cone, int nthreads, double* out) {
+  if (!cfg || !S_primary || !settings || !out || n_settings < 1 || (real_bits != 32 && real_bits != 64))
+    return NMC_EINVAL;
+  EfInput in;
+  in.c = *cfg;
+  const nmc_efield_config& c = in.c;
+  in.n = c.n_angles;
+  if (in.n < 2 || !(c.mua + c.mus > 0.f)) return NMC_EINVAL;
+  const bool raman = c.mu_raman > 0.f;
+  if (raman && (!S_raman || !(c.raman_mua + c.raman_mus > 0.f))) return NMC_EINVAL;
+  in.S[0].assign(S_primary, S_primary + 4 * (size_t)in.n);
+  in.S[1].assign(raman ? S_raman : S_primary, (raman ? S_raman : S_primary) + 4 * (size_t)in.n);
+  if (!ef_cdf(in.S[0].data(), in.n, in.cdf[0]) || !ef_cdf(in.S[1].data(), in.n, in.cdf[1])) return NMC_EINVAL;
+  const double mut0 = (double)c.mua + c.mus + c.mu_raman;
+  in.inv_mut[0] = (float)(1.0 / mut0);  // the engine's per-medium constants (floats)
+  in.surv[0] = (float)((c.mus + c.mu_raman) / mut0);
+  in.p_raman[0] = (c.mus + c.mu_raman) > 0.f ? (float)(c.mu_raman / ((double)c.mus + c.mu_raman)) : 0.f;
+  const double mut1 = raman ? (double)c.raman_mua + c.raman_mus : mut0;
+  in.inv_mut[1] = (float)(1.0 / mut1);
+  in.surv[1] = raman ? (float)(c.raman_mus / mut1) : in.surv[0];
+  in.p_raman[1] = 0.0;
+  in.dtheta = (float)(3.14159265358979323846 / (in.n - 1));
+  in.cone = cone != 0;
+  in.sep_inv = in.cone ? (float)(c.sep_n / (2.0 * c.sep_half_width)) : 0.f;
+  in.sep_half = c.sep_half_width;
+  if (nthreads < 1) nthreads = 1;
+  for (int set = 0; set < n_settings; ++set) {
+    const nmc_efield_setting& q = settings[set];
+    const uint64_t n = q.photons;
+    const int nt = (int)std::min<uint64_t>((uint64_t)nthreads, std::max<uint64_t>(n, 1));
+    std::vector<std::vector<double>> part(nt, std::vector<double>(NMC_EF_FIELDS, 0.0));
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&, t] {
+        for (uint64_t i = n * t / nt; i < n * (t + 1) / nt; ++i) {
+          if (real_bits == 64)
+            ef_photon<double>(in, q, (uint32_t)set, i, part[t].data());
+          else
+            ef_photon<float>(in, q, (uint32_t)set, i, part[t].data());
+        }
+      });
+    for (auto& x : th) x.join();
+    for (int t = 0; t < nt; ++t)
+      for (int k = 0; k < NMC_EF_FIELDS; ++k) out[(size_t)set * NMC_EF_FIELDS + k] += part[t][k];
+  }
+  return 0;
+}
 
 int orc_layered_run(int real_bits, const nmc_layered_config* cfg, const nmc_layer* layers, uint64_t first,
                     uint64_t n, int nthreads, double* out, double* rd_r, double* tt_r, double* a_z,

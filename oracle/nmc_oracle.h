@@ -70,6 +70,13 @@ int orc_layered_run(int real_bits, const nmc_layered_config* cfg, const nmc_laye
                     uint64_t n, int nthreads, double* out, double* rd_r, double* tt_r, double* a_z,
                     double* a_layer);
 
+/* The engine's polarised E-field model (nmc_efield_run) restated on the CPU,
+ * same Philox layout: per setting the NMC_EF_FIELDS sums into `out` (+=;
+ * n_settings * NMC_EF_FIELDS doubles; SEP_OUTSIDE only with `cone`).
+ * Returns 0 or NMC_EINVAL. */
+int orc_efield_run(int real_bits, const nmc_efield_config* cfg, const float* S_primary, const float* S_raman,
+                   const nmc_efield_setting* settings, int n_settings, int cone, int nthreads, double* out);
+
 /* MetalMC.m:628-742 speckle mutual interference (see nmc_speckle_mutual). */
 void orc_speckle_mutual(int nx, int ny, const float* maps, const nmc_speckle* rec, const int32_t* counts,
                         int kmax, float lambda, float lc, float* out);
