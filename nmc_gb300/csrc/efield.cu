@@ -710,7 +710,8 @@ extern "C" nmc_status nmc_efield_run(int32_t device, const nmc_efield_config* cf
     d.first = 0;
     prefix[s + 1] = prefix[s] + q.photons;
   }
-  if (cudaSetDevice(device) != cudaSuccess) return NMC_EDEVICE;
+  nmc::DeviceScope dev(device);
+  if (!dev.ok) return NMC_EDEVICE;
   cudaStream_t st = nullptr;
   if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return NMC_EDEVICE;
   std::vector<void*> allocs;
@@ -871,7 +872,8 @@ extern "C" nmc_status nmc_speckle_mutual(int32_t device, int32_t nx, int32_t ny,
       !std::isfinite(lambda) || !std::isfinite(lc))
     return NMC_EINVAL;
   const size_t np = (size_t)nx * ny, nm = (size_t)NMC_EF_MAPS * np, nr = (size_t)max_records * np;
-  if (cudaSetDevice(device) != cudaSuccess) return NMC_EDEVICE;
+  nmc::DeviceScope dev(device);
+  if (!dev.ok) return NMC_EDEVICE;
   cudaStream_t st = nullptr;
   if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return NMC_EDEVICE;
   float *dm = nullptr, *dout = nullptr;

@@ -11,6 +11,24 @@
 
 namespace nmc {
 
+// Makes `device` current for the life of an entry point and gives the
+// caller's current device back on exit, so a handle on one GPU works from a
+// thread whose current device is another, and the library never changes the
+// caller's current device.
+struct DeviceScope {
+  int prev = -1;
+  bool ok = false;
+  explicit DeviceScope(int device) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    ok = cudaSetDevice(device) == cudaSuccess;
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  DeviceScope(const DeviceScope&) = delete;
+  DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
 // One detection event recorded by the adjoint's forward pass.
 struct AdjEvent {
   unsigned int photon;  // photon index within the launch

@@ -286,7 +286,8 @@ nmc_status layered_impl(int32_t device, const nmc_layered_config* cfg, const nmc
     tp.gv[1] = q.g;
     d.ph = phase_const(tp, 1);
   }
-  if (cudaSetDevice(device) != cudaSuccess) return NMC_EDEVICE;
+  nmc::DeviceScope dev(device);
+  if (!dev.ok) return NMC_EDEVICE;
   cudaStream_t st = nullptr;
   if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return NMC_EDEVICE;
   std::vector<void*> allocs;

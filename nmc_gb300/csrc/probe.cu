@@ -4,6 +4,7 @@
 // with CUDA events.  Measurement support; no counterpart in the reference.
 #include <cuda_runtime.h>
 
+#include "engine.h"
 #include "nmc_abi.h"
 
 namespace {
@@ -49,7 +50,8 @@ __global__ void __launch_bounds__(256) mufu_probe(float* out, int iters) {
 extern "C" nmc_status nmc_probe_issue_peaks(int32_t device, double* ffma_lanes_per_s,
                                             double* mufu_lanes_per_s) {
   if (!ffma_lanes_per_s || !mufu_lanes_per_s) return NMC_EINVAL;
-  if (cudaSetDevice(device) != cudaSuccess) return NMC_EDEVICE;
+  nmc::DeviceScope dev(device);
+  if (!dev.ok) return NMC_EDEVICE;
   int nsm = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
   float* out = nullptr;

@@ -112,6 +112,11 @@ nmc_status cuda_fail(nmc_handle* h, cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
   } while (0)
 
+// The handle's device is current for the rest of the entry point.
+#define NMC_ON_DEVICE(h)                      \
+  nmc::DeviceScope on_device_((h)->device); \
+  if (!on_device_.ok) return fail((h), NMC_EDEVICE, "cudaSetDevice failed")
+
 template <class T>
 void dfree(T*& p) {
   if (p) cudaFree((void*)p);
@@ -308,7 +313,6 @@ nmc_status launch(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_record* 
     return NMC_OK;
   }
   if (h->since_fold + n > h->fold_every) {
-    NMC_CUDA(h, cudaSetDevice(h->device));
     const nmc_status st = fold(h);
     if (st != NMC_OK) return st;
   }
@@ -318,7 +322,6 @@ nmc_status launch(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_record* 
     return fail(h, NMC_EUNSUPPORTED, "per-voxel media use the one-term HG kernel (NMC_SIM_MCXYZ)");
   if (h->voxel_mode && h->ext.rng != NMC_RNG_PHILOX)
     return fail(h, NMC_EUNSUPPORTED, "per-voxel media use the Philox streams");
-  NMC_CUDA(h, cudaSetDevice(h->device));
   NMC_CUDA(h, cudaMemsetAsync(&h->d_sums->work, 0, sizeof(unsigned long long), h->stream));
   const bool trace = d_recs != nullptr;
   nmc::TraceParams tr{d_recs, d_events, d_events ? k_events : 0u};
@@ -578,8 +581,8 @@ nmc_status nmc_create(int32_t sim_type, int32_t device, nmc_handle** out) {
   h->sim = sim_type;
   h->device = device;
   nmc_ext_defaults(&h->ext);
-  if (cudaSetDevice(device) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+  nmc::DeviceScope dev(device);
+  if (!dev.ok || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
       cudaMalloc((void**)&h->d_sums, sizeof(DevSums)) != cudaSuccess ||
       cudaMemset(h->d_sums, 0, sizeof(DevSums)) != cudaSuccess) {
@@ -594,6 +597,7 @@ nmc_status nmc_create(int32_t sim_type, int32_t device, nmc_handle** out) {
 
 nmc_status nmc_set_ext(nmc_handle* h, const nmc_ext* ext) {
   if (!h || !ext) return NMC_EINVAL;
+  NMC_ON_DEVICE(h);
   if (ext->size != sizeof(nmc_ext)) return fail(h, NMC_EINVAL, "nmc_ext.size does not match this library");
   const bool reprepare = h->prepared;
   h->ext = *ext;
@@ -610,9 +614,9 @@ nmc_status nmc_set_ext(nmc_handle* h, const nmc_ext* ext) {
 nmc_status nmc_prepare(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue_params* tp,
                        const uint8_t* v) {
   if (!h || !rp || !tp) return fail(h, NMC_EINVAL, "null argument");
+  NMC_ON_DEVICE(h);
   nmc_status st = validate(h, rp, tp, v);
   if (st != NMC_OK) return st;
-  NMC_CUDA(h, cudaSetDevice(h->device));
   st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
   free_buffers(h);
@@ -655,6 +659,7 @@ nmc_status nmc_prepare(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue
 
 nmc_status nmc_set_tissue_params(nmc_handle* h, const nmc_tissue_params* tp) {
   if (!h || !tp) return fail(h, NMC_EINVAL, "null argument");
+  NMC_ON_DEVICE(h);
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   nmc_status st;
   if (h->sim == NMC_SIM_MCSUB) {
@@ -672,6 +677,7 @@ nmc_status nmc_set_tissue_params(nmc_handle* h, const nmc_tissue_params* tp) {
 
 nmc_status nmc_reset(nmc_handle* h) {
   if (!h) return NMC_EINVAL;
+  NMC_ON_DEVICE(h);
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   nmc_status st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
@@ -713,33 +719,37 @@ nmc_status nmc_set_num_runs_seed(nmc_handle* h, int32_t run, float time_seed) {
 
 nmc_status nmc_send_compute_command(nmc_handle* h) {
   if (!h) return NMC_EINVAL;
+  NMC_ON_DEVICE(h);
   const uint64_t b = h->ext.photons_per_dispatch;
   return nmc_run(h, (uint64_t)(h->run - 1) * b, b);
 }
 
 nmc_status nmc_run_async(nmc_handle* h, uint64_t first, uint64_t n) {
   if (!h) return NMC_EINVAL;
+  NMC_ON_DEVICE(h);
   return launch(h, first, n, nullptr, nullptr, 0);
 }
 
 nmc_status nmc_synchronize(nmc_handle* h) {
   if (!h) return NMC_EINVAL;
+  NMC_ON_DEVICE(h);
   return sync_all(h);
 }
 
 nmc_status nmc_run(nmc_handle* h, uint64_t first, uint64_t n) {
   nmc_status st = nmc_run_async(h, first, n);
   if (st != NMC_OK) return st;
+  NMC_ON_DEVICE(h);
   return sync_all(h);
 }
 
 nmc_status nmc_run_traced(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_record* recs,
                           float* events, uint32_t k_events) {
   if (!h || !recs) return fail(h, NMC_EINVAL, "null argument");
+  NMC_ON_DEVICE(h);
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   nmc_photon_record* d_recs = nullptr;
   float4* d_ev = nullptr;
-  NMC_CUDA(h, cudaSetDevice(h->device));
   NMC_CUDA(h, cudaMalloc((void**)&d_recs, n * sizeof(nmc_photon_record)));
   const size_t nev = events ? (size_t)n * k_events : 0;
   if (nev) {
@@ -765,6 +775,7 @@ nmc_status nmc_run_traced(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_
 
 nmc_status nmc_autotune(nmc_handle* h, uint64_t photons, nmc_tune_result* out) {
   if (!h || !out) return fail(h, NMC_EINVAL, "null argument");
+  NMC_ON_DEVICE(h);
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   if (photons == 0) return fail(h, NMC_EINVAL, "photons must be > 0");
   nmc_status st = sync_all(h);
@@ -857,6 +868,7 @@ size_t nmc_tally_size(nmc_handle* h, int32_t which) {
 
 nmc_status nmc_get_tally_f64(nmc_handle* h, int32_t which, double* out, size_t n) {
   if (!h || !out) return fail(h, NMC_EINVAL, "null argument");
+  NMC_ON_DEVICE(h);
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   const size_t want = nmc_tally_size(h, which);
   if (want == 0 || n != want) return fail(h, NMC_EINVAL, "tally not produced by this kind, or wrong size");
@@ -896,6 +908,7 @@ nmc_status nmc_get_compute_results(nmc_handle* h, float* J, float* F, float* F3D
   (void)PolXX, (void)PolXY, (void)PolYX, (void)PolYY, (void)Phase0, (void)Phase1, (void)Phase2,
       (void)Phase3, (void)PolVsScatt;
   if (!h) return NMC_EINVAL;
+  NMC_ON_DEVICE(h);
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   nmc_status st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
@@ -941,6 +954,7 @@ nmc_status nmc_get_compute_results(nmc_handle* h, float* J, float* F, float* F3D
 
 nmc_status nmc_get_summary(nmc_handle* h, nmc_summary* out) {
   if (!h || !out) return fail(h, NMC_EINVAL, "null argument");
+  NMC_ON_DEVICE(h);
   std::memset(out, 0, sizeof *out);
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   nmc_status st = sync_all(h);
@@ -964,6 +978,7 @@ nmc_status nmc_get_summary(nmc_handle* h, nmc_summary* out) {
 nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_sets, double* out,
                          double* J) {
   if (!h || !sets || !out) return fail(h, NMC_EINVAL, "null argument");
+  NMC_ON_DEVICE(h);
   if (h->sim != NMC_SIM_MCSUB) return fail(h, NMC_EINVAL, "sweeps run on an NMC_SIM_MCSUB handle");
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   if (n_sets < 1 || n_sets > 1024) return fail(h, NMC_EINVAL, "n_sets must be in [1, 1024]");
@@ -1110,6 +1125,7 @@ nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_set
 nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables, const uint64_t* photons,
                                  const uint64_t* first_photon, int32_t n_sets, double* out) {
   if (!h || !tables || !photons || !out) return fail(h, NMC_EINVAL, "null argument");
+  NMC_ON_DEVICE(h);
   if (h->sim != NMC_SIM_MCXYZ && h->sim != NMC_SIM_MCXYZ_TT)
     return fail(h, NMC_EINVAL, "tissue sweeps run on an NMC_SIM_MCXYZ or NMC_SIM_MCXYZ_TT handle");
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
@@ -1229,6 +1245,7 @@ nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables,
 
 nmc_status nmc_set_voxel_props(nmc_handle* h, const float* mua, const float* mus, const float* g) {
   if (!h || !mua || !mus) return fail(h, NMC_EINVAL, "null argument");
+  NMC_ON_DEVICE(h);
   if (h->sim != NMC_SIM_MCXYZ) return fail(h, NMC_EINVAL, "per-voxel media need an NMC_SIM_MCXYZ handle");
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   nmc_status st = sync_all(h);
@@ -1254,6 +1271,7 @@ nmc_status nmc_set_voxel_props(nmc_handle* h, const float* mua, const float* mus
 
 nmc_status nmc_set_radial_tally(nmc_handle* h, int32_t bins, float dr) {
   if (!h) return NMC_EINVAL;
+  NMC_ON_DEVICE(h);
   if (h->sim == NMC_SIM_MCSUB) return fail(h, NMC_EINVAL, "the radial tally is for voxel kinds (mcsub has J)");
   if (!h->prepared) return fail(h, NMC_ESTATE, "nmc_prepare has not been called");
   if (bins < 1 || bins > 65536 || !(dr > 0.f) || !std::isfinite(dr))
@@ -1271,6 +1289,7 @@ nmc_status nmc_set_radial_tally(nmc_handle* h, int32_t bins, float dr) {
 
 nmc_status nmc_adjoint_forward(nmc_handle* h, uint64_t first, uint64_t n, uint64_t event_capacity) {
   if (!h) return NMC_EINVAL;
+  NMC_ON_DEVICE(h);
   if (!h->prepared || !h->voxel_mode) return fail(h, NMC_ESTATE, "the adjoint needs nmc_set_voxel_props");
   if (h->rd_bins < 1) return fail(h, NMC_ESTATE, "the adjoint differentiates the radial tally: nmc_set_radial_tally");
   if (n >= 0xFFFFFFFFull || event_capacity == 0 || event_capacity >= 0xFFFFFFFFull)
@@ -1307,6 +1326,7 @@ nmc_status nmc_adjoint_forward(nmc_handle* h, uint64_t first, uint64_t n, uint64
 nmc_status nmc_adjoint_backward_ex(nmc_handle* h, const float* grad_rd_r, const float* grad_absorbed,
                                    double* grad_mua, double* grad_mus, double* grad_g) {
   if (!h || (!grad_rd_r && !grad_absorbed)) return fail(h, NMC_EINVAL, "null argument");
+  NMC_ON_DEVICE(h);
   if (!h->adj_ready) return fail(h, NMC_ESTATE, "nmc_adjoint_forward has not completed");
   nmc_status st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
@@ -1372,7 +1392,7 @@ const char* nmc_last_error(const nmc_handle* h) { return h ? h->err.c_str() : "n
 
 void nmc_destroy(nmc_handle* h) {
   if (!h) return;
-  cudaSetDevice(h->device);
+  nmc::DeviceScope dev(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   free_buffers(h);
   if (h->d_sums) cudaFree(h->d_sums);

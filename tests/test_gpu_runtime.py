@@ -145,3 +145,26 @@ def test_handles_on_two_host_threads(gpu):
         for f in ("photons", "substeps", "S", "A", "E", "rd_sum"):
             assert alone[k][0][f] == together[k][0][f], (k, f)
         np.testing.assert_array_equal(alone[k][1], together[k][1])
+
+
+def test_current_device_is_kept(gpu):
+    # every entry point makes the handle's device current and gives the
+    # caller's back; with two GPUs a handle on the second one runs while the
+    # first is current and gives the results it gives with its own current
+    import torch
+
+    dev = torch.cuda.device_count() - 1
+    rp, tp, v, ext = cases.skin_vessel_case(N=32)
+    res = {}
+    for cur in sorted({0, dev}):
+        torch.cuda.set_device(cur)
+        with gpu.Engine(abi.SIM_MCXYZ, dev, ext) as e:
+            e.prepare_data(rp, tp, v)
+            e.run(0, 20_000)
+            assert torch.cuda.current_device() == cur
+            res[cur] = (e.summary(), e.tally(abi.TALLY_F3D))
+        assert torch.cuda.current_device() == cur
+    a, b = res[0], res[dev]
+    for f in ("photons", "substeps", "S", "A", "E", "rd_sum"):
+        assert a[0][f] == b[0][f], f
+    np.testing.assert_array_equal(a[1], b[1])
