@@ -114,15 +114,21 @@ def test_integration_c_snippet_compiles(tmp_path):
         pytest.skip("no C compiler")
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     doc = open(os.path.join(root, "INTEGRATION.md")).read()
-    snippet = re.search(r"```c\n(.*?)```", doc, re.S).group(1)
-    body = "\n".join(ln for ln in snippet.splitlines() if not ln.startswith("#include"))
+    snippets = re.findall(r"```c\n(.*?)```", doc, re.S)
+    assert len(snippets) >= 2
+
+    def body(snippet):
+        return "\n".join(ln for ln in snippet.splitlines() if not ln.startswith("#include"))
+
+    # the first replaces main.m's calls; later ones run on an existing handle
     src = tmp_path / "host.c"
     src.write_text(
-        "#include <stdio.h>\n#include <stdint.h>\n#include \"nmc_abi.h\"\n"
+        "#include <stdio.h>\n#include <stdint.h>\n#include <stdlib.h>\n#include \"nmc_abi.h\"\n"
         "void host(nmc_run_params runParams, nmc_tissue_params tissParams, const char* v, int NumGPURuns,\n"
         "          float t_seed, float* ResJ_GPU, float* ResF_GPU, float* ResF3D_GPU, float* ResSAE_GPU,\n"
         "          float* ResRd_GPU, float* ResRd2D_GPU, int32_t* ResDetPhotons2D_GPU) {\n"
-        + body + "\n}\n")
+        + body(snippets[0]) + "\n}\n"
+        + "".join(f"void extra{k}(nmc_handle* h) {{\n{body(b)}\n}}\n" for k, b in enumerate(snippets[1:])))
     r = subprocess.run([cc, "-std=c11", "-Wall", "-Werror", "-fsyntax-only", f"-I{os.path.join(root, 'include')}",
                         str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
