@@ -71,6 +71,11 @@ struct nmc_handle {
   double *c_F3D = nullptr, *c_Rd2D = nullptr, *c_Det = nullptr, *c_slots = nullptr, *c_J = nullptr,
          *c_F = nullptr, *c_rdr = nullptr;
   uint64_t since_fold = 0, fold_every = 1ull << 31;
+  // Grow-only device scratch of the synchronous calls (sweeps, adjoint
+  // backward).  Each of them waits for the handle's earlier work before it
+  // writes here and for its own before it returns.
+  char* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
   float* d_stage = nullptr;  // conversion buffer for results (floats)
   float* h_stage = nullptr;  // pinned host copy
   size_t stage_elems = 0;
@@ -143,6 +148,8 @@ void free_buffers(nmc_handle* h) {
   dfree(h->c_J);
   dfree(h->c_F);
   dfree(h->c_rdr);
+  dfree(h->d_scratch);
+  h->scratch_bytes = 0;
   h->since_fold = 0;
   for (ReduceGraph& g : h->graphs) cudaGraphExecDestroy(g.exec);
   h->graphs.clear();
@@ -156,6 +163,20 @@ void free_buffers(nmc_handle* h) {
 }
 
 bool finite_nonneg(float v) { return std::isfinite(v) && v >= 0.f; }
+
+// The handle's scratch with at least `bytes`: reused across calls, so a sweep
+// pays no cudaMalloc, and no cudaFree (which waits for the whole device)
+// holds up other handles' streams.
+nmc_status scratch(nmc_handle* h, size_t bytes, char** out) {
+  if (bytes > h->scratch_bytes) {
+    dfree(h->d_scratch);
+    h->scratch_bytes = 0;
+    NMC_CUDA(h, cudaMalloc((void**)&h->d_scratch, bytes));
+    h->scratch_bytes = bytes;
+  }
+  *out = h->d_scratch;
+  return NMC_OK;
+}
 
 nmc_status build_xyz(nmc_handle* h) {
   nmc::XyzParams& p = h->xp;
@@ -1056,7 +1077,7 @@ nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_set
                b_J = J ? 8 * (size_t)nJ * n_sets : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t total_b = al(b_sets) + al(b_pre) + al(b_sums) + al(b_e2) + al(b_work) + al(b_J);
-  NMC_CUDA(h, cudaMalloc((void**)&base, total_b));
+  if ((st = scratch(h, total_b, &base)) != NMC_OK) return st;
   char* cur = base;
   auto take = [&](size_t b) {
     char* r = cur;
@@ -1069,40 +1090,36 @@ nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_set
   p.e2 = (double*)take(b_e2);
   p.work = (unsigned long long*)take(b_work);
   p.J = J ? (unsigned long long*)take(b_J) : nullptr;
-  auto cleanup = [&](nmc_status s) {
-    cudaFree(base);
-    return s;
-  };
   if (cudaMemcpyAsync((void*)p.sets, hs.data(), b_sets, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
       cudaMemcpyAsync((void*)p.prefix, prefix.data(), b_pre, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
       // sums, e2, counter and J are contiguous: clear them together
       cudaMemsetAsync(p.sums, 0, al(b_sums) + al(b_e2) + al(b_work) + al(b_J), h->stream) != cudaSuccess)
-    return cleanup(fail(h, NMC_EDEVICE, "sweep buffer set-up"));
+    return fail(h, NMC_EDEVICE, "sweep buffer set-up");
   const int block = h->ext.block_size > 0 ? h->ext.block_size : 256;
   int per_sm = 0;
   if (nmc::sweep_occupancy(p, block, &per_sm) != cudaSuccess || per_sm < 1)
-    return cleanup(fail(h, NMC_EDEVICE, "sweep kernel does not fit on an SM"));
+    return fail(h, NMC_EDEVICE, "sweep kernel does not fit on an SM");
   if (h->ext.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)h->ext.blocks_per_sm);
   uint64_t grid = (uint64_t)h->nsm * per_sm;
   grid = std::max<uint64_t>(1, std::min<uint64_t>(grid, (p.total + block - 1) / block));
   EventPair ev = get_pair(h);
   cudaEventRecord(ev.a, h->stream);
   if (p.total > 0 && nmc::launch_sweep(p, (int)grid, block, h->stream) != cudaSuccess)
-    return cleanup(fail(h, NMC_EDEVICE, "sweep launch"));
+    return fail(h, NMC_EDEVICE, "sweep launch");
   cudaEventRecord(ev.b, h->stream);
   h->pending.push_back(ev);
   ++h->launches;
   st = sync_all(h);
-  if (st != NMC_OK && st != NMC_ESTEPCAP) return cleanup(st);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
   std::vector<unsigned long long> sums(5 * (size_t)n_sets);
   std::vector<double> e2(n_sets);
   if (cudaMemcpy(sums.data(), p.sums, b_sums, cudaMemcpyDeviceToHost) != cudaSuccess ||
       cudaMemcpy(e2.data(), p.e2, b_e2, cudaMemcpyDeviceToHost) != cudaSuccess)
-    return cleanup(fail(h, NMC_EDEVICE, "sweep results"));
+    return fail(h, NMC_EDEVICE, "sweep results");
   if (J) {
     std::vector<unsigned long long> hj((size_t)nJ * n_sets);
     if (cudaMemcpy(hj.data(), p.J, b_J, cudaMemcpyDeviceToHost) != cudaSuccess)
-      return cleanup(fail(h, NMC_EDEVICE, "sweep J"));
+      return fail(h, NMC_EDEVICE, "sweep J");
     for (size_t k = 0; k < hj.size(); ++k) J[k] = (double)hj[k] * nmc::kUnfix;
   }
   for (int s = 0; s < n_sets; ++s) {
@@ -1119,7 +1136,7 @@ nmc_status nmc_run_sweep(nmc_handle* h, const nmc_sweep_set* sets, int32_t n_set
     o[NMC_SWEEP_RD] = n > 0 ? (o[NMC_SWEEP_S] + o[NMC_SWEEP_E]) / n : 0.0;
     o[NMC_SWEEP_RD_SE] = n > 1 ? std::sqrt(std::max(0.0, e2[s] / n - me * me) / n) : 0.0;
   }
-  return cleanup(st);
+  return st;
 }
 
 nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables, const uint64_t* photons,
@@ -1174,8 +1191,11 @@ nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables,
                b_order = 4 * (size_t)n_sets;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   char* base = nullptr;
-  NMC_CUDA(h, cudaMalloc((void**)&base,
-                         al(b_core) + al(b_ph) + al(b_pre) + al(b_first) + al(b_sums) + al(b_order)));
+  {
+    const nmc_status sc =
+        scratch(h, al(b_core) + al(b_ph) + al(b_pre) + al(b_first) + al(b_sums) + al(b_order), &base);
+    if (sc != NMC_OK) return sc;
+  }
   char* cur = base;
   auto take = [&](size_t b) {
     char* r = cur;
@@ -1192,10 +1212,6 @@ nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables,
   p.first = 0;
   p.n = prefix[n_sets];
   p.trace = nmc::TraceParams{nullptr, nullptr, 0u};
-  auto cleanup = [&](nmc_status s) {
-    cudaFree(base);
-    return s;
-  };
   if (cudaMemcpyAsync((void*)p.sw_core, core.data(), b_core, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
       cudaMemcpyAsync((void*)p.sw_phase, phase.data(), b_ph, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
       cudaMemcpyAsync((void*)p.sw_prefix, prefix.data(), b_pre, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
@@ -1205,27 +1221,27 @@ nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables,
           cudaSuccess ||
       cudaMemsetAsync(p.sw_sums, 0, b_sums, h->stream) != cudaSuccess ||
       cudaMemsetAsync(&h->d_sums->work, 0, sizeof(unsigned long long), h->stream) != cudaSuccess)
-    return cleanup(fail(h, NMC_EDEVICE, "sweep buffer set-up"));
+    return fail(h, NMC_EDEVICE, "sweep buffer set-up");
   const bool tt = h->sim == NMC_SIM_MCXYZ_TT;
   const int block = h->ext.block_size > 0 ? h->ext.block_size : 256;
   int per_sm = 0;
   if (nmc::mcxyz_sweep_occupancy(tt, block, &per_sm) != cudaSuccess || per_sm < 1)
-    return cleanup(fail(h, NMC_EDEVICE, "sweep kernel does not fit on an SM"));
+    return fail(h, NMC_EDEVICE, "sweep kernel does not fit on an SM");
   if (h->ext.blocks_per_sm > 0) per_sm = std::min(per_sm, (int)h->ext.blocks_per_sm);
   uint64_t grid = (uint64_t)h->nsm * per_sm;
   grid = std::max<uint64_t>(1, std::min<uint64_t>(grid, (p.n + block - 1) / block));
   EventPair ev = get_pair(h);
   cudaEventRecord(ev.a, h->stream);
   if (p.n > 0 && nmc::launch_mcxyz_sweep(p, tt, (int)grid, block, h->stream) != cudaSuccess)
-    return cleanup(fail(h, NMC_EDEVICE, "sweep launch"));
+    return fail(h, NMC_EDEVICE, "sweep launch");
   cudaEventRecord(ev.b, h->stream);
   h->pending.push_back(ev);
   ++h->launches;
   st = sync_all(h);
-  if (st != NMC_OK && st != NMC_ESTEPCAP) return cleanup(st);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
   std::vector<nmc::XyzSweepSums> sums(n_sets);
   if (cudaMemcpy(sums.data(), p.sw_sums, b_sums, cudaMemcpyDeviceToHost) != cudaSuccess)
-    return cleanup(fail(h, NMC_EDEVICE, "sweep results"));
+    return fail(h, NMC_EDEVICE, "sweep results");
   for (int s = 0; s < n_sets; ++s) {
     double* o = out + (size_t)s * NMC_SWEEP_FIELDS;
     const nmc::XyzSweepSums& u = sums[s];
@@ -1240,7 +1256,7 @@ nmc_status nmc_run_sweep_tissues(nmc_handle* h, const nmc_tissue_params* tables,
     o[NMC_SWEEP_RD] = me;
     o[NMC_SWEEP_RD_SE] = n > 1 ? std::sqrt(std::max(0.0, u.rd2 / n - me * me) / n) : 0.0;
   }
-  return cleanup(st);
+  return st;
 }
 
 nmc_status nmc_set_voxel_props(nmc_handle* h, const float* mua, const float* mus, const float* g) {
@@ -1336,48 +1352,44 @@ nmc_status nmc_adjoint_backward_ex(nmc_handle* h, const float* grad_rd_r, const 
   const size_t bD = h->adj_n * 4, bG = nb * 4, bF = grad_absorbed ? nv * 4 : 0, bg = nv * 8;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   char* base = nullptr;
-  NMC_CUDA(h, cudaMalloc((void**)&base, al(bD) + al(bG) + al(bF) + 3 * al(bg)));
+  if ((st = scratch(h, al(bD) + al(bG) + al(bF) + 3 * al(bg), &base)) != NMC_OK) return st;
   float* D = (float*)base;
   float* G = (float*)(base + al(bD));
   float* GF = grad_absorbed ? (float*)(base + al(bD) + al(bG)) : nullptr;
   double* gL = (double*)(base + al(bD) + al(bG) + al(bF));
   double* gM = (double*)((char*)gL + al(bg));
   double* gQ = (double*)((char*)gM + al(bg));
-  auto done = [&](nmc_status s) {
-    cudaFree(base);
-    return s;
-  };
   bool ok = cudaMemsetAsync(gL, 0, 3 * al(bg), h->stream) == cudaSuccess;
   ok = ok && (grad_rd_r ? cudaMemcpyAsync(G, grad_rd_r, bG, cudaMemcpyHostToDevice, h->stream)
                         : cudaMemsetAsync(G, 0, bG, h->stream)) == cudaSuccess;
   if (GF) ok = ok && cudaMemcpyAsync(GF, grad_absorbed, bF, cudaMemcpyHostToDevice, h->stream) == cudaSuccess;
-  if (!ok) return done(fail(h, NMC_EDEVICE, "adjoint set-up"));
+  if (!ok) return fail(h, NMC_EDEVICE, "adjoint set-up");
   if (GF) {
     // deposits score too: a first replay gives every photon its total score
     AdjArgs a{2, D, G, GF, nullptr, nullptr, nullptr};
     st = launch(h, h->adj_first, h->adj_n, nullptr, nullptr, 0, &a);
-    if (st != NMC_OK) return done(st);
+    if (st != NMC_OK) return st;
   } else {
     // detection scores only: from the events the record pass kept
     if (cudaMemsetAsync(D, 0, bD, h->stream) != cudaSuccess ||
         nmc::launch_adjoint_scores(h->d_ev, (unsigned int)cnt, G, D, h->stream) != cudaSuccess)
-      return done(fail(h, NMC_EDEVICE, "adjoint scores"));
+      return fail(h, NMC_EDEVICE, "adjoint scores");
   }
   AdjArgs a{1, D, G, GF, gL, gM, gQ};
   st = launch(h, h->adj_first, h->adj_n, nullptr, nullptr, 0, &a);
   if (st == NMC_OK) st = sync_all(h);
-  if (st != NMC_OK && st != NMC_ESTEPCAP) return done(st);
+  if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
   std::vector<double> L(nv), M(nv), Q(nv);
   if (cudaMemcpy(L.data(), gL, bg, cudaMemcpyDeviceToHost) != cudaSuccess ||
       cudaMemcpy(M.data(), gM, bg, cudaMemcpyDeviceToHost) != cudaSuccess ||
       cudaMemcpy(Q.data(), gQ, bg, cudaMemcpyDeviceToHost) != cudaSuccess)
-    return done(fail(h, NMC_EDEVICE, "adjoint results"));
+    return fail(h, NMC_EDEVICE, "adjoint results");
   for (size_t k = 0; k < nv; ++k) {
     if (grad_mua) grad_mua[k] = -L[k];
     if (grad_mus) grad_mus[k] = M[k];
     if (grad_g) grad_g[k] = Q[k];
   }
-  return done(st);
+  return st;
 }
 
 nmc_status nmc_adjoint_backward(nmc_handle* h, const float* grad_rd_r, double* grad_mua, double* grad_mus,
