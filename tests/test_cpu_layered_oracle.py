@@ -1,11 +1,13 @@
 """The oracle's restatement of the layered model (orc_layered_run) against
 closed forms, on the CPU: a clear absorbing slab transmits exp(-mua d) of
 the weight (Beer-Lambert), a clear non-absorbing slab between two index
-steps transmits (1 - r)/(1 + r) (incoherent multiple reflections), and
-weight is conserved up to Russian roulette."""
+steps transmits (1 - r)/(1 + r) (incoherent multiple reflections), weight
+is conserved up to Russian roulette, and one semi-infinite layer gives the
+mcsub restatement's Rd."""
 import math
 
 import numpy as np
+import pytest
 
 
 def test_beer_lambert_slab(oracle):
@@ -41,3 +43,20 @@ def test_weight_conserved(oracle):
     assert abs(total - 1.0) <= 0.01  # roulette is unbiased, not exact
     assert np.isclose(r["rd_r"].sum(), r["Rd"]) and np.isclose(r["a_z"].sum(), r["A"])
     assert np.isclose(r["a_layer"].sum(), r["A"]) and r["tt"] == 0.0
+
+
+def test_one_semi_infinite_layer_is_mcsub(oracle):
+    # one semi-infinite layer is the mcsub medium: the same specular weight
+    # exactly, and Rd within 3 combined standard errors of the oracle's
+    # mcsub restatement (independent streams)
+    import nmc_cases as cases
+    from nmc_gb300 import abi
+
+    n = 50_000
+    r = oracle.layered([(1.0, 100.0, 0.9, 1.37, math.inf)], n, n_above=1.0, seed=3)
+    rp, tp, ext = cases.mcsub_case(seed=9)
+    m = oracle.run(abi.SIM_MCSUB, rp, tp, ext=ext, n=n, tallies=False)
+    rd_m = m["E"] / n
+    se_m = math.sqrt(max(m["rd_sumsq"] / n - rd_m ** 2, 0) / n)
+    assert r["specular"] == pytest.approx(m["S"], rel=1e-12)
+    assert abs(r["rd"] - rd_m) <= 3 * math.hypot(r["rd_se"], se_m), (r["rd"], r["rd_se"], rd_m, se_m)
