@@ -1,7 +1,8 @@
 """Polarised E-field transport, CBS cone and Raman conversion (efield.cu).
 
 No reference semantics exist (the reference's kernels are empty), so parity
-is unpinned; the tests check what the physics fixes:
+against the reference is unpinned (test_gpu_efield_oracle.py pins the kernel
+to its CPU restatement); these tests check what the physics fixes:
   * the scalar limit: with S1 = S2 = sqrt(p_HG) the escaped weight equals the
     mcsub kernel's for the same medium within 3 combined standard errors;
   * reciprocity: the co-polarised channel's interference term equals its
