@@ -50,3 +50,20 @@ def test_fp32_follows_fp64_on_short_paths(oracle):
     # reciprocity: the time-reversed partner of a co-polarised path has the same amplitude
     np.testing.assert_allclose(a["interf_co"], a["multi_co"], rtol=1e-9)
     assert np.all(a["interf_cross"] < a["multi_cross"])
+
+
+def test_separation_overflow_shrinks_with_the_histogram_width(oracle):
+    # CBS partners farther apart than the separation histogram reaches are
+    # counted in sep_outside: almost all of the co-polarised interference for
+    # a tiny histogram, less as it widens, almost none once it spans the
+    # walk (mua 10 /cm: paths of ~0.1 cm)
+    out = []
+    for w in (1e-5, 0.005, 0.05, 0.5):
+        cfg, s633, _, st = cases.cbs_case(n_settings=1, photons=5_000, mu_raman=0.0, sep_half_width=w)
+        cfg.mua = 10.0
+        r = oracle.efield(cfg, s633, st, cone=True)
+        out.append(r["sep_outside"][0])
+        interf = r["interf_co"][0]
+    assert out[0] >= 0.99 * interf
+    assert all(a > b for a, b in zip(out, out[1:]))
+    assert out[-1] <= 1e-3 * interf
