@@ -35,6 +35,12 @@
 
 namespace {
 
+// Start of thread t's share when n photons are split over nt threads (the
+// first n % nt threads take one photon more); overflow-free for any n.
+uint64_t share_begin(uint64_t n, int t, int nt) {
+  return n / (uint64_t)nt * (uint64_t)t + std::min<uint64_t>((uint64_t)t, n % (uint64_t)nt);
+}
+
 // ---------------------------------------------------------------- constants
 constexpr double kPI = 3.1415926;               // definitions.h:60 PI
 constexpr double kLS = 10E-8;                   // definitions.h:59 ls
@@ -1398,7 +1404,7 @@ int orc_run(int sim_type, int real_bits, const nmc_run_params* rp, const nmc_tis
   std::vector<Tally> T(nthreads);
   std::vector<std::thread> th;
   for (int t = 0; t < nthreads; ++t) {
-    const uint64_t lo = n * t / nthreads, hi = n * (t + 1) / nthreads;
+    const uint64_t lo = share_begin(n, t, nthreads), hi = share_begin(n, t + 1, nthreads);
     th.emplace_back([&, t, lo, hi] {
       Tally& tl = T[t];
       if (!xyz) {
@@ -1507,7 +1513,7 @@ int orc_efield_run(int real_bits, const nmc_efield_config* cfg, const float* S_p
     std::vector<std::thread> th;
     for (int t = 0; t < nt; ++t)
       th.emplace_back([&, t] {
-        for (uint64_t i = n * t / nt; i < n * (t + 1) / nt; ++i) {
+        for (uint64_t i = share_begin(n, t, nt), e = share_begin(n, t + 1, nt); i < e; ++i) {
           if (real_bits == 64)
             ef_photon<double>(in, q, (uint32_t)set, i, part[t].data());
           else
@@ -1552,7 +1558,7 @@ int orc_layered_run(int real_bits, const nmc_layered_config* cfg, const nmc_laye
   std::vector<LayTally> T(nthreads);
   std::vector<std::thread> th;
   for (int t = 0; t < nthreads; ++t) {
-    const uint64_t lo = n * t / nthreads, hi = n * (t + 1) / nthreads;
+    const uint64_t lo = share_begin(n, t, nthreads), hi = share_begin(n, t + 1, nthreads);
     th.emplace_back([&, t, lo, hi] {
       LayTally& tl = T[t];
       if (rd_r) tl.rd.assign((size_t)c.nr + 1, 0.0);
