@@ -467,7 +467,9 @@ static_assert(sizeof(nmc_speckle) == 28, "nmc_speckle layout (struct SPECKLE)");
  *   pol_vs_scatt[(s*4 + ch)*(NMC_EF_MAX_ORDER+1) + n]: XX, XY, YX, YY
  *     intensity escaping after n scatterings (n capped);
  *   maps[(s*NMC_EF_MAPS + m)*map_n*map_n + ...];
- *   raman_depth[s*depth_bins + b]: weight converted at depth b*dz. */
+ *   raman_depth[s*depth_bins + b]: weight converted at depth b*dz.
+ * At most 2^53 photons over all settings (counts are summed in FP64);
+ * NMC_EINVAL beyond. */
 nmc_status nmc_efield_run(int32_t device, const nmc_efield_config* cfg, const float* S_primary,
                           const float* S_raman, const nmc_efield_setting* settings, int32_t n_settings,
                           double* out, float* cone, double* pol_vs_scatt, float* maps, double* raman_depth,

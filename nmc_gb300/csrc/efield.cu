@@ -708,6 +708,8 @@ extern "C" nmc_status nmc_efield_run(int32_t device, const nmc_efield_config* cf
     d.t[3] = make_float2((float)(t[1][1] * sc), 0.f);
     d.w0 = (float)(1.0 - host_rfresnel(c.n_outside, c.n_medium, std::cos((double)q.theta_in)));
     d.first = 0;
+    // photon counts are summed in FP64: keep the whole run exact there
+    if (q.photons > (1ull << 53) - prefix[s]) return NMC_EINVAL;
     prefix[s + 1] = prefix[s] + q.photons;
   }
   nmc::DeviceScope dev(device);

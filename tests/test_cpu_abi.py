@@ -152,3 +152,20 @@ def test_integration_python_snippets_parse():
                 for a in node.names:
                     mod = importlib.import_module(node.module)
                     assert hasattr(mod, a.name) or importlib.util.find_spec(f"{node.module}.{a.name}"), a.name
+
+
+def test_photon_limits_refused_before_any_device_call():
+    # the functional entry points check their limits on the host before they
+    # touch a device, so the refusals are testable without a GPU
+    import math
+
+    import nmc_cases as cases
+    from nmc_gb300 import efield, engine, layered
+
+    cfg, s633, s700, st = cases.cbs_case(n_settings=2, photons=2 ** 52 + 1, cone_n=8, sep_n=8)
+    with pytest.raises(engine.NMCError) as e:  # 2^53 + 2 photons in all: beyond exact FP64 counts
+        efield.run(cfg, s633, st, S_raman=s700)
+    assert abi.STATUS[e.value.status] == "NMC_EINVAL"
+    with pytest.raises(engine.NMCError) as e:
+        layered.run([(0.1, 100.0, 0.9, 1.4, math.inf)], photons=2 ** 31 + 1)
+    assert abi.STATUS[e.value.status] == "NMC_EINVAL"
