@@ -169,3 +169,25 @@ def test_photon_limits_refused_before_any_device_call():
     with pytest.raises(engine.NMCError) as e:
         layered.run([(0.1, 100.0, 0.9, 1.4, math.inf)], photons=2 ** 31 + 1)
     assert abi.STATUS[e.value.status] == "NMC_EINVAL"
+
+
+def test_refusals_without_a_device():
+    # status codes for calls that fail before any device work: kinds the
+    # reference leaves empty, unknown kinds, null handles and outputs
+    import ctypes as C
+
+    from nmc_gb300 import engine
+
+    L = engine.lib()
+    h = C.c_void_p()
+    code = {v: k for k, v in abi.STATUS.items()}
+    assert L.nmc_create(abi.SIM_MCXYZ, 0, None) == code["NMC_EINVAL"]
+    for kind in (3, 4, 5):  # polarisation / Raman / Mueller kernels are empty in the reference
+        assert L.nmc_create(kind, 0, C.byref(h)) == code["NMC_EUNSUPPORTED"] and not h.value
+    assert L.nmc_create(99, 0, C.byref(h)) == code["NMC_EINVAL"] and not h.value
+    assert L.nmc_run(None, C.c_uint64(0), C.c_uint64(1)) == code["NMC_EINVAL"]
+    assert L.nmc_prepare(None, None, None, None) == code["NMC_EINVAL"]
+    assert L.nmc_set_fold_interval(None, C.c_uint64(1)) == code["NMC_EINVAL"]
+    L.nmc_last_error.restype = C.c_char_p
+    assert L.nmc_last_error(None) == b"null handle"
+    L.nmc_destroy(None)  # a no-op
