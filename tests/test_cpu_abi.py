@@ -191,3 +191,32 @@ def test_refusals_without_a_device():
     L.nmc_last_error.restype = C.c_char_p
     assert L.nmc_last_error(None) == b"null handle"
     L.nmc_destroy(None)  # a no-op
+
+
+def test_invalid_configurations_refused_before_any_device_call():
+    import math
+
+    import numpy as np
+
+    import nmc_cases as cases
+    from nmc_gb300 import efield, engine, layered
+
+    def refused(f, *a, **kw):
+        with pytest.raises(engine.NMCError) as e:
+            f(*a, **kw)
+        assert abi.STATUS[e.value.status] == "NMC_EINVAL"
+
+    cfg, s633, s700, st = cases.cbs_case(n_settings=1, photons=10, cone_n=8, sep_n=8)
+    cfg.n_angles = 1  # a table needs two angles at least
+    refused(efield.run, cfg, s633[:1], st, S_raman=s700[:1])
+    cfg, s633, s700, st = cases.cbs_case(n_settings=1, photons=10, cone_n=8, sep_n=8)
+    cfg.mua = float("nan")
+    refused(efield.run, cfg, s633, st, S_raman=s700)
+    cfg, s633, s700, st = cases.cbs_case(n_settings=1, photons=10, cone_n=8, sep_n=8)
+    st[0].theta_in = 2.0  # grazing or beyond: no refracted beam
+    refused(efield.run, cfg, s633, st, S_raman=s700)
+    refused(layered.run, [], 10)
+    refused(layered.run, [(0.1, 100.0, 0.9, 1.4, -0.1), (0.1, 100.0, 0.9, 1.4, math.inf)], 10)
+    maps = np.zeros((len(abi.EF_MAPS), 4, 4), np.float32)
+    recs = np.zeros((1, 4, 4), abi.SPECKLE_DTYPE)
+    refused(efield.speckle_mutual, maps, recs, np.zeros((4, 4), np.int32), float("inf"), 1.0)
