@@ -676,7 +676,7 @@ def run_cbs_workload(args) -> dict:
         t = time.perf_counter() - t0
         best = t if best is None else min(best, t)
     n = float(r["photons"].sum())
-    return {
+    out = {
         "metric": "photons/s, polarised E-field transport with CBS cone and Raman, 8 settings",
         "unit": "photons/s", "value": n / best, "seconds": best, "photons": n,
         "scatterings_per_photon": float(r["scatters"].sum() / n),
@@ -692,6 +692,19 @@ def run_cbs_workload(args) -> dict:
                    "timing": f"best of {max(args.steps, 1)} host-timed calls (tables, launch, cone transform, "
                              "result copies)"},
     }
+    if not args.no_cpu:
+        from oracle import bindings as orc
+
+        threads = os.cpu_count() or 1
+        per = 4_000
+        sample = cases.cbs_case(n_settings=8, photons=per)[3]
+        t0 = time.perf_counter()
+        orc.efield(cfg, S633, sample, S_raman=S700, cone=True, real_bits=32, nthreads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 8 * per / dt, "unit": "photons/s", "cores": threads, "kind": "port",
+                               "sample": f"{8 * per} photons of the same 8 settings, FP32 CPU restatement of the "
+                                         f"E-field model (sums only), {dt:.1f} s"}
+    return out
 
 
 def run_layered_workload(args) -> dict:
