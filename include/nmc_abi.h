@@ -640,6 +640,9 @@ nmc_status nmc_probe_issue_peaks(int32_t device, double* ffma_lanes_per_s,
 /* Largest grid nmc_mcxyz_run_noalloc accepts. */
 #define NMC_NOALLOC_MAX_VOXELS 2097152u /* Nx*Ny*Nz, e.g. 128^3 */
 #define NMC_NOALLOC_MAX_MAP 65536u      /* Nx*Ny, e.g. 256^2 */
+/* Most photons nmc_mcxyz_run_noalloc takes in one call (its fixed-point
+ * sums are not folded within a call). */
+#define NMC_NOALLOC_MAX_PHOTONS 2147483648ull /* 2^31 */
 
 /* Voxel transport that allocates no memory.  No counterpart in the
  * reference.
@@ -663,7 +666,12 @@ nmc_status nmc_probe_issue_peaks(int32_t device, double* ffma_lanes_per_s,
  * totals; about 17 MB) is one fixed array in device memory that every GPU
  * loading the library holds until the process exits; grids beyond
  * NMC_NOALLOC_MAX_VOXELS voxels or NMC_NOALLOC_MAX_MAP columns are rejected
- * with NMC_EINVAL.  Every call reuses that array and clears it first, so
+ * with NMC_EINVAL, and so are calls of more than NMC_NOALLOC_MAX_PHOTONS
+ * photons (2^31: the u64 fixed-point sums and u32 counts of one call are
+ * never folded into FP64 the way nmc_run folds them, so a larger call could
+ * wrap) or whose photon ids would pass 2^64; these size checks come before
+ * any device call.  The launch shape follows ext->block_size and
+ * ext->blocks_per_sm as nmc_run's does.  Every call reuses that array and clears it first, so
  * calls whose GPU work overlaps (two streams, two host threads) race and
  * must be serialised by the caller.  The first call on a device looks up the
  * array's device address (once per device, with that device current); make

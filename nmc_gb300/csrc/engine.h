@@ -160,6 +160,10 @@ cudaError_t sweep_occupancy(const SweepParams& p, int block, int* blocks_per_sm)
 // Parameter blocks from the reference's configuration (params.cu); device
 // pointers are left for the caller to set.
 PhaseConst phase_const(const nmc_tissue_params& tp, int t);
+// Tissue t of the table has usable optical properties: finite mua >= 0,
+// finite mus > 0, finite g and finite two-term phase terms (gf, af, gb, ab,
+// CC), the same test for every entry point that takes a tissue table.
+bool tissue_usable(const nmc_tissue_params& tp, int t);
 RngParams rng_params(const nmc_ext& e, int sim);
 void fill_xyz(XyzParams& p, const nmc_run_params& rp, const nmc_tissue_params& tp, const nmc_ext& e,
               int sim);

@@ -19,7 +19,9 @@
 //    zero, and calls whose GPU work overlaps (e.g. on two streams) race.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 
@@ -98,7 +100,11 @@ extern "C" nmc_status nmc_mcxyz_run_noalloc(const nmc_run_params* rp, const nmc_
                                             uint64_t n_photons, float* d_F3D, float* d_Rd2D,
                                             uint32_t* d_DetPhot2D, double* d_totals, void* stream) {
   if (!rp || !tp || !ext || !d_v || !d_F3D) return NMC_EINVAL;
+  // The u64 fixed-point sums and u32 counts of one call are never folded
+  // (nmc_run folds every 2^31 photons), so one call takes at most 2^31.
+  if (n_photons > NMC_NOALLOC_MAX_PHOTONS || first_photon > UINT64_MAX - n_photons) return NMC_EINVAL;
   if (ext->size != sizeof(nmc_ext) || ext->photons_per_dispatch == 0) return NMC_EINVAL;
+  if (ext->block_size < 0 || ext->block_size > 1024 || ext->blocks_per_sm < 0) return NMC_EINVAL;
   if (ext->rng != NMC_RNG_PHILOX && ext->rng != NMC_RNG_TAUS_REF) return NMC_EINVAL;
   if (rp->mckernelflag != NMC_SIM_MCXYZ && rp->mckernelflag != NMC_SIM_MCXYZ_TT) return NMC_EINVAL;
   if (rp->Nx <= 0 || rp->Ny <= 0 || rp->Nz <= 0) return NMC_EINVAL;
@@ -128,10 +134,7 @@ extern "C" nmc_status nmc_mcxyz_run_noalloc(const nmc_run_params* rp, const nmc_
     return NMC_EDEVICE;
   for (int t = 0; t < 32; ++t) {
     if (!(mask & (1u << t))) continue;
-    if (t >= NMC_NTISS) return NMC_EINVAL;
-    if (!std::isfinite(tp->muav[t]) || tp->muav[t] < 0.f || !(tp->musv[t] > 0.f) ||
-        !std::isfinite(tp->musv[t]) || !std::isfinite(tp->gv[t]))
-      return NMC_EINVAL;
+    if (t >= NMC_NTISS || !nmc::tissue_usable(*tp, t)) return NMC_EINVAL;
   }
 
   // the working memory starts at zero on every call
@@ -156,9 +159,12 @@ extern "C" nmc_status nmc_mcxyz_run_noalloc(const nmc_run_params* rp, const nmc_
     p.n = n_photons;
     p.trace = nmc::TraceParams{nullptr, nullptr, 0};
     const bool tt = rp->mckernelflag == NMC_SIM_MCXYZ_TT;
-    const int block = 256;
+    // the launch shape nmc_run takes from the same nmc_ext
+    const int block = ext->block_size > 0 ? ext->block_size : 256;
     int per_sm = 0;
-    if (nmc::mcxyz_occupancy(tt, false, block, &per_sm) != cudaSuccess || per_sm < 1) return NMC_EDEVICE;
+    if (nmc::mcxyz_occupancy(tt, false, block, &per_sm) != cudaSuccess) return NMC_EDEVICE;
+    if (ext->blocks_per_sm > 0) per_sm = std::min(per_sm, (int)ext->blocks_per_sm);
+    if (per_sm < 1) return NMC_EDEVICE;
     uint64_t grid = (uint64_t)nsm * per_sm;
     if (grid > (n_photons + block - 1) / block) grid = (n_photons + block - 1) / block;
     if (nmc::launch_mcxyz(p, tt, false, (int)grid, block, s) != cudaSuccess) return NMC_EDEVICE;

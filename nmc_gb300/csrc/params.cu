@@ -35,6 +35,12 @@ void lattice_split(float zsurf, float dz, int* k, float* f) {
 
 }  // namespace
 
+bool tissue_usable(const nmc_tissue_params& tp, int t) {
+  return std::isfinite(tp.muav[t]) && tp.muav[t] >= 0.f && tp.musv[t] > 0.f && std::isfinite(tp.musv[t]) &&
+         std::isfinite(tp.gv[t]) && std::isfinite(tp.gf[t]) && std::isfinite(tp.af[t]) &&
+         std::isfinite(tp.gb[t]) && std::isfinite(tp.ab[t]) && std::isfinite(tp.CC[t]);
+}
+
 PhaseConst phase_const(const nmc_tissue_params& tp, int t) {
   PhaseConst p{};
   const double g = tp.gv[t];

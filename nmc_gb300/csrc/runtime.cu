@@ -212,9 +212,7 @@ nmc_status build_sub(nmc_handle* h) {
 nmc_status check_tissues(nmc_handle* h, const nmc_tissue_params* tp, uint32_t mask, int set) {
   for (int t = 0; t < NMC_NTISS; ++t) {
     if (!(mask >> t & 1u)) continue;
-    if (!finite_nonneg(tp->muav[t]) || !(tp->musv[t] > 0.f) || !std::isfinite(tp->musv[t]) ||
-        !std::isfinite(tp->gv[t]) || !std::isfinite(tp->gf[t]) || !std::isfinite(tp->af[t]) ||
-        !std::isfinite(tp->gb[t]) || !std::isfinite(tp->ab[t]) || !std::isfinite(tp->CC[t])) {
+    if (!nmc::tissue_usable(*tp, t)) {
       char msg[128];
       if (set >= 0)
         std::snprintf(msg, sizeof msg, "sweep set %d, tissue %d needs finite mua >= 0, mus > 0 and phase terms",

@@ -171,6 +171,29 @@ def test_photon_limits_refused_before_any_device_call():
     assert abi.STATUS[e.value.status] == "NMC_EINVAL"
 
 
+def test_noalloc_photon_limit_refused_before_any_device_call(engine_lib):
+    # nmc_mcxyz_run_noalloc never folds its fixed-point sums, so it takes at
+    # most 2^31 photons per call; the check comes before any CUDA call, and
+    # the device pointers below are never dereferenced
+    import nmc_cases as cases
+
+    L = engine_lib.lib()
+    f = L.nmc_mcxyz_run_noalloc
+    f.restype = C.c_int
+    f.argtypes = [C.POINTER(abi.RunParams), C.POINTER(abi.TissueParams), C.POINTER(abi.Ext), C.c_void_p,
+                  C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    rp, tp, _, ext = cases.skin_vessel_case(N=8)
+    fake = C.c_void_p(0x1000)  # not a device address: only the refusals run
+    code = {v: k for k, v in abi.STATUS.items()}
+    for first, n in ((0, 2 ** 31 + 1), (2 ** 64 - 10, 11), (0, 2 ** 64 - 1)):
+        st = f(C.byref(rp), C.byref(tp), C.byref(ext), fake, first, n, fake, None, None, None, None)
+        assert st == code["NMC_EINVAL"], (first, n)
+    bad = abi.Ext.from_buffer_copy(ext)
+    bad.block_size = 2048
+    st = f(C.byref(rp), C.byref(tp), C.byref(bad), fake, 0, 10, fake, None, None, None, None)
+    assert st == code["NMC_EINVAL"]
+
+
 def test_refusals_without_a_device():
     # status codes for calls that fail before any device work: kinds the
     # reference leaves empty, unknown kinds, null handles and outputs
