@@ -35,12 +35,15 @@ def test_tissue_params_and_sets():
     assert [s.photons for s in sets] == [1000, 2000]
 
 
-# the reference checkout, when one is at hand (NMC_REFERENCE=<path>)
-LIB_PATH = os.path.join(os.environ.get("NMC_REFERENCE", ""), "NMC-samples", "spectralLIB.mat")
+# the reference checkout, when one is at hand: NMC_REFERENCE=<path>, else the
+# checkout the oracle builds the reference kernels from
+from oracle import bindings as _orc  # noqa: E402
+
+REF_ROOT = os.environ.get("NMC_REFERENCE") or os.path.dirname(os.path.dirname(_orc.REF_SRC))
+LIB_PATH = os.path.join(REF_ROOT, "NMC-samples", "spectralLIB.mat")
 
 
-@pytest.mark.skipif(not os.environ.get("NMC_REFERENCE") or not os.path.exists(LIB_PATH),
-                    reason="reference spectral library not present")
+@pytest.mark.skipif(not os.path.exists(LIB_PATH), reason="reference spectral library not present")
 def test_interpolation_in_the_library():
     lib = spectral.load_library(LIB_PATH)
     for case in GOLD:
