@@ -12,7 +12,15 @@ One step = one pass of the transport over the workload's photon budget
             Rd slots, Rd2D, DetPhot2D) inside the timed region
   roofline  the transport kernel against the measured FP32-issue ceiling
   cpu_baseline  the reference algorithm restated on the host cores (FP32,
-            the reference's own generator), a bounded sample of the workload
+            the reference's own generator, fluence tally kept), a bounded
+            sample of the workload, with its sub-steps per photon and the
+            ratio at equal work (sub-steps/s)
+
+Extras in the same line (each with its own rate, its unit-of-work rate
+against the FP32-issue ceiling and a CPU baseline): the 351-wavelength sweep
+to 1 % Rd SE against plain runs, the pMC adjoint against a forward (1e7
+photons, Rd(r) and Rd(r) + fluence losses), C1 (mcsub, 1e6 photons), the
+three-layer stack (1e8 photons) and C5 (E-field / CBS / Raman, 1e8 photons).
 
 --impl reference times that CPU restatement alone on the same workload (the
 reference runs only on Apple Metal; its kernels cannot execute on this machine).
@@ -42,6 +50,16 @@ WORKLOAD = "mcxyz skin-vessel 200^3 @0.005 cm, 1e8 photons per GPU per step"
 # per-hop SPIN/roulette share.  Fixed once, not re-counted per build.
 OPS_PER_SUBSTEP = 64.0
 MUFU_PER_SUBSTEP = 3.0
+# The same count for the other transport kernels' units, fixed once from
+# their loop bodies: one Philox4x32-10 block (~109 integer lane operations:
+# 10 rounds of 4 multiply halves, 4 xors and 2 key adds, plus 3 uniform
+# conversions) per step or scattering, plus the FP32 work of the step.
+OPS_PER_MCSUB_STEP = 164.0     # HOP 5, DROP + F(r,z) index 21, HG + SPIN 24, roulette/loop 5, Philox 109
+MUFU_PER_MCSUB_STEP = 9.0
+OPS_PER_LAYERED_STEP = 170.0   # an mcsub step plus the distance to the layer boundary
+OPS_PER_EF_SCATTER = 320.0     # step 17, theta search 26, S1/S2 12, phi density + Newton 54, frame 43,
+                               # Jones update 51, loop 8, Philox 109
+MUFU_PER_EF_SCATTER = 14.0
 # Warp instructions the transport kernel issues per voxel sub-step
 # (smsp__inst_executed.sum / sub-steps of the 1e7-photon ncu capture of this
 # workload), and the SM's issue rate (4 warp instructions per clock).
@@ -112,7 +130,10 @@ def _issue_estimate(substeps_per_s, clock_lines) -> dict | None:
 def cpu_sample(seconds: float = 12.0, threads: int | None = None) -> dict:
     """The reference algorithm on the host cores: the oracle's FP32 restatement
     with the reference's Tausworthe generator (which reproduces the
-    reference's FP32 voxel walk), on a bounded sample of the workload."""
+    reference's FP32 voxel walk), with its fluence tally (the reference
+    kernel always deposits into F3D), on a bounded sample of the workload.
+    On one host this restatement costs what the reference's own kernel,
+    compiled from its sources, costs per photon (oracle/compare_cost.py)."""
     import nmc_cases as cases
     from nmc_gb300 import abi
     from oracle import bindings
@@ -121,16 +142,18 @@ def cpu_sample(seconds: float = 12.0, threads: int | None = None) -> dict:
     threads = threads or os.cpu_count() or 1
     rp, tp, v, ext = cases.skin_vessel_case(N=200, rng=abi.RNG_TAUS_REF)
     n = 64 * threads
-    t0 = time.perf_counter()
-    r = bindings.run(abi.SIM_MCXYZ, rp, tp, v, ext=ext, n=n, nthreads=threads, real_bits=32, tallies=False)
-    dt = time.perf_counter() - t0
-    n2 = max(threads, int(n * max(seconds - dt, 1.0) / max(dt, 1e-3)))
-    t0 = time.perf_counter()
-    r2 = bindings.run(abi.SIM_MCXYZ, rp, tp, v, ext=ext, first=n, n=n2, nthreads=threads, real_bits=32,
-                      tallies=False)
-    dt2 = time.perf_counter() - t0
-    return {"photons": n2, "seconds": dt2, "photons_per_s": n2 / dt2, "threads": threads,
-            "substeps_per_photon": r2["substeps"] / n2}
+    bindings.run(abi.SIM_MCXYZ, rp, tp, v, ext=ext, n=n, nthreads=threads, real_bits=32, tallies=True)  # warm-up
+    first, photons, secs, subs = n, 0, 0.0, 0
+    while secs < seconds:  # growing runs until the sample holds about `seconds` of work
+        t0 = time.perf_counter()
+        r = bindings.run(abi.SIM_MCXYZ, rp, tp, v, ext=ext, first=first, n=n, nthreads=threads, real_bits=32,
+                         tallies=True)
+        dt = time.perf_counter() - t0
+        first, photons, secs, subs = first + n, photons + n, secs + dt, subs + r["substeps"]
+        rate = photons / secs
+        n = max(threads, min(4 * n, int(rate * max(seconds - secs, 0.5)) + 1))
+    return {"photons": photons, "seconds": secs, "photons_per_s": photons / secs, "threads": threads,
+            "substeps_per_photon": subs / photons}
 
 
 def run_reference(args) -> dict:
@@ -148,6 +171,7 @@ def run_reference(args) -> dict:
     ph = sum(s["photons"] for s in samples)
     sec = sum(s["seconds"] for s in samples)
     v = ph / sec
+    sub = sum(s["substeps_per_photon"] * s["photons"] for s in samples) / max(ph, 1)
     desc = (f"{ph} photons of the 200^3 skin-vessel workload in {args.steps} samples, FP32 restatement with "
             f"the reference's generator, {threads} threads")
     return {
@@ -155,7 +179,8 @@ def run_reference(args) -> dict:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "config": {"workload": WORKLOAD, "photons_per_step_sampled": ph // args.steps},
-        "cpu_baseline": {"value": v, "unit": "photons/s", "cores": threads, "kind": "port", "sample": desc},
+        "cpu_baseline": {"value": v, "unit": "photons/s", "cores": threads, "kind": "port", "sample": desc,
+                         "substeps_per_photon": sub, "substeps_per_s": v * sub},
         "e2e": {"value": v, "unit": "photons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -308,15 +333,26 @@ def run_ours(args) -> dict:
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
             cs = cpu_sample(12.0)
+            gpu_sub_s = value * out["config"]["substeps_per_photon"]
+            cpu_sub_s = cs["photons_per_s"] * cs["substeps_per_photon"]
             out["cpu_baseline"] = {"value": cs["photons_per_s"], "unit": "photons/s", "cores": cs["threads"],
                                    "kind": "port",
                                    "sample": f"{cs['photons']} photons of the same workload, FP32 restatement with "
-                                             f"the reference's generator ({cs['substeps_per_photon']:.0f} "
-                                             f"sub-steps/photon), {cs['seconds']:.1f} s"}
+                                             f"the reference's generator and its fluence tally "
+                                             f"({cs['substeps_per_photon']:.0f} sub-steps/photon), "
+                                             f"{cs['seconds']:.1f} s",
+                                   "substeps_per_photon": cs["substeps_per_photon"], "substeps_per_s": cpu_sub_s,
+                                   # photons/s ratio, and the ratio at equal work: the reference's FP32
+                                   # walk stalls at voxel faces and takes ~4x the sub-steps per photon
+                                   "photons_ratio": value / cs["photons_per_s"],
+                                   "equal_work_ratio": gpu_sub_s / cpu_sub_s}
         except Exception as exc:  # noqa: BLE001
             out["cpu_baseline"] = {"value": None, "unit": "photons/s", "error": f"{type(exc).__name__}: {exc}"}
     if rank == 0 and world == 1 and not args.no_extras:
-        for key, fn in (("batched_to_1pct_se", batched_to_target_extra), ("adjoint", adjoint_extra)):
+        cpu = not args.no_cpu
+        for key, fn in (("batched_to_1pct_se", batched_to_target_extra), ("adjoint", adjoint_extra),
+                        ("mcsub_c1", lambda: mcsub_extra(ffma, cpu)), ("layered", lambda: layered_extra(ffma, cpu)),
+                        ("cbs_c5", lambda: cbs_extra(ffma, cpu))):
             try:  # an extra that fails is reported in the line, not in place of it
                 out[key] = fn()
             except Exception as exc:  # noqa: BLE001
@@ -398,8 +434,10 @@ def batched_to_target_extra() -> dict:
             "workload": "skin-vessel 200^3, 351 wavelengths, two-term HG, to 1% Rd SE"}
 
 
-def adjoint_extra(n: int = 1_000_000) -> dict:
-    """Forward + pMC adjoint against a plain forward, 64^3 per-voxel medium."""
+def adjoint_extra(n: int = 10_000_000) -> dict:
+    """Forward + pMC adjoint against a plain forward on the 64^3 per-voxel
+    medium at 1e7 photons, for a loss on Rd(r) and for a loss on Rd(r) plus
+    the fluence (absorbed weight per voxel)."""
     import numpy as np
 
     import nmc_cases as cases
@@ -407,17 +445,143 @@ def adjoint_extra(n: int = 1_000_000) -> dict:
 
     rp, tp, v, ext, mua, mus, g, bins, dr = cases.adjoint_case()
     G = np.random.default_rng(3).uniform(0.5, 1.5, bins + 1).astype(np.float32)
+    GF = np.random.default_rng(4).uniform(0.5, 1.5, rp.Nx * rp.Ny * rp.Nz).astype(np.float32)
     with engine.Engine(abi.SIM_MCXYZ, 0, ext) as e:
         e.prepare_data(rp, tp, v)
         e.set_radial_tally(bins, dr)
         e.set_voxel_props(mua, mus, g)
         fwd = lambda: (e.reset(), e.run(0, n))  # noqa: E731
         adj = lambda: (e.reset(), e.adjoint_forward(0, n, 8 * n), e.adjoint_backward(G))  # noqa: E731
-        fwd(), adj()
+        adj_f = lambda: (e.reset(), e.adjoint_forward(0, n, 8 * n), e.adjoint_backward(G, GF))  # noqa: E731
+        fwd(), adj(), adj_f()
         t_f = min(_timed(fwd)[1] for _ in range(3))
         t_a = min(_timed(adj)[1] for _ in range(3))
-    return {"forward_s": t_f, "forward_adjoint_s": t_a, "cost_ratio": t_a / t_f, "photons": n,
-            "workload": "64^3 per-voxel medium, gradient of Rd(r) w.r.t. all voxel mua, mus, g"}
+        t_af = min(_timed(adj_f)[1] for _ in range(3))
+    return {"forward_s": t_f, "forward_adjoint_s": t_a, "cost_ratio": t_a / t_f,
+            "forward_adjoint_fluence_s": t_af, "cost_ratio_fluence": t_af / t_f, "photons": n,
+            "workload": "64^3 per-voxel medium, 1e7 photons; gradients w.r.t. all voxel mua, mus, g of a loss on "
+                        "Rd(r) (cost_ratio) and on Rd(r) + fluence (cost_ratio_fluence)",
+            "timing": "best of 3 host-timed synchronised calls each"}
+
+
+def _unit_roofline(units: float, seconds: float, ops_per_unit: float, ffma_lanes_per_s: float, unit: str,
+                   timing: str) -> dict:
+    achieved = units * ops_per_unit / seconds / 1e12
+    peak = ffma_lanes_per_s / 1e12
+    return {"bound": "fp32_issue", "unit_of_work": unit, "units_per_s": units / seconds,
+            "ops_per_unit": ops_per_unit, "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
+            "frac": achieved / peak, "peak_source": "of measured FP32 FMA lane rate (nmc_probe_issue_peaks, live)",
+            "timing": timing}
+
+
+def mcsub_extra(ffma: float, cpu: bool = True) -> dict:
+    """C1: semi-infinite medium (mua 1, mus 100 /cm, HG g 0.9, n 1.37/1.0),
+    normal pencil beam, Rd(r) 100 x 0.01 cm, F(r, z) 100 x 100 x 0.01 cm,
+    1e6 photons per launch (Philox seed 0), device-timed over 10 launches;
+    the CPU baseline runs the full 1e6 photons through the FP32 restatement
+    with the reference's generator on all host cores."""
+    import nmc_cases as cases
+    from nmc_gb300 import abi, engine
+
+    rp, tp, ext = cases.mcsub_case()
+    n, K = 1_000_000, 10
+    with engine.Engine(abi.SIM_MCSUB, 0, ext) as e:
+        e.prepare_data(rp, tp)
+        e.run(0, n)
+        e.reset()
+        s0 = e.summary()
+        (_, wall) = _timed(lambda: [e.run(i * n, n) for i in range(K)])
+        s1 = e.summary()
+    kernel_s = (s1["kernel_ms"] - s0["kernel_ms"]) * 1e-3
+    steps = s1["substeps"] - s0["substeps"]
+    out = {"value": K * n / kernel_s, "unit": "photons/s", "photons": K * n, "kernel_s": kernel_s, "wall_s": wall,
+           "steps_per_photon": steps / (K * n), "rd": s1["rd_sum"] / max(s1["photons"], 1),
+           "roofline": _unit_roofline(steps, kernel_s, OPS_PER_MCSUB_STEP, ffma, "mcsub step",
+                                      "CUDA events around the 10 transport launches"),
+           "workload": "C1 mcsub mua 1, mus 100, g 0.9, n 1.37/1.0, pencil beam, 1e6 photons per launch"}
+    if cpu:
+        from oracle import bindings
+
+        bindings.build(ref=False)
+        threads = os.cpu_count() or 1
+        ext_c = cases.mcsub_case(rng=abi.RNG_TAUS_REF)[2]
+        t0 = time.perf_counter()
+        r = bindings.run(abi.SIM_MCSUB, rp, tp, ext=ext_c, n=n, nthreads=threads, real_bits=32, tallies=True)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / dt, "unit": "photons/s", "cores": threads, "kind": "port",
+                               "sample": f"the full 1e6 photons, FP32 restatement with the reference's generator "
+                                         f"and tallies, {dt:.1f} s",
+                               "steps_per_photon": r["substeps"] / n}
+    return out
+
+
+def layered_extra(ffma: float, cpu: bool = True) -> dict:
+    """Layered media: the three-layer skin stack, 1e8 photons per call."""
+    import nmc_cases as cases
+    from nmc_gb300 import layered
+
+    n = 100_000_000
+    kw = dict(nr=100, dr=0.01, nz=100, dz=0.01, seed=11)
+    layered.run(cases.LAYERED_SKIN3, 1_000_000, **kw)
+    best, r = None, None
+    for _ in range(2):
+        r, t = _timed(lambda: layered.run(cases.LAYERED_SKIN3, n, **kw))
+        best = t if best is None else min(best, t)
+    out = {"value": n / best, "unit": "photons/s", "photons": n, "seconds": best, "rd": r["rd"],
+           "interactions_per_photon": r["interactions"] / n,
+           "roofline": _unit_roofline(r["interactions"], best, OPS_PER_LAYERED_STEP, ffma, "layered interaction",
+                                      "host clock around the call (allocation, launch, tally copies): a lower "
+                                      "bound of the kernel's rate"),
+           "workload": "3 layers: 0.01 cm (mua 3, mus 200, g 0.8, n 1.4), 0.2 cm (0.3, 150, 0.85, 1.4), "
+                       "semi-infinite (0.1, 100, 0.9, 1.44); pencil beam; Rd(r), Tt(r), A(z)"}
+    if cpu:
+        from oracle import bindings as orc
+
+        threads = os.cpu_count() or 1
+        sample = 200_000
+        t0 = time.perf_counter()
+        orc.layered(cases.LAYERED_SKIN3, sample, real_bits=32, nthreads=threads, **kw)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": sample / dt, "unit": "photons/s", "cores": threads, "kind": "port",
+                               "sample": f"{sample} photons of the same stack, FP32 CPU restatement, {dt:.1f} s"}
+    return out
+
+
+def cbs_extra(ffma: float, cpu: bool = True) -> dict:
+    """C5: polarised E-field transport with the CBS cone and Raman, 1e8
+    photons over 8 polarisation / incidence settings in one launch."""
+    import nmc_cases as cases
+    from nmc_gb300 import efield
+
+    total = 100_000_000
+    cfg, S633, S700, settings = cases.cbs_case(n_settings=8, photons=total // 8)
+    warm = cases.cbs_case(n_settings=8, photons=20_000)[3]
+    efield.run(cfg, S633, warm, S_raman=S700)
+    r, t = _timed(lambda: efield.run(cfg, S633, settings, S_raman=S700))
+    n = float(r["photons"].sum())
+    scat = float(r["scatters"].sum())
+    out = {"value": n / t, "unit": "photons/s", "photons": n, "seconds": t, "scatterings_per_photon": scat / n,
+           "rd": float(r["Rd"].sum() / n),
+           "co_enhancement": float(1 + r["interf_co"].sum() / r["multi_co"].sum()),
+           "raman_conversions": float(r["raman_n"].sum()),
+           "roofline": _unit_roofline(scat, t, OPS_PER_EF_SCATTER, ffma, "E-field scattering",
+                                      "host clock around the call (tables, launch, cone transform, copies): a "
+                                      "lower bound of the kernel's rate"),
+           "workload": "spheres 0.5 um 1.59/1.33, 633 nm, mus 100, mua 0.01 /cm; cone 256^2 within +-5 mrad; Raman "
+                       "1e-4 /cm to 700 nm; 8 settings"}
+    if cpu:
+        from oracle import bindings as orc
+
+        threads = os.cpu_count() or 1
+        per = 4_000
+        sample = cases.cbs_case(n_settings=8, photons=per)[3]
+        t0 = time.perf_counter()
+        orc.efield(cfg, S633, sample, S_raman=S700, cone=True, real_bits=32, nthreads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 8 * per / dt, "unit": "photons/s", "cores": threads, "kind": "port",
+                               "sample": f"{8 * per} photons of the same 8 settings, FP32 CPU restatement of the "
+                                         f"E-field model, {dt:.1f} s"}
+    return out
 
 
 def run_sweep_workload(args) -> dict:
@@ -876,7 +1040,7 @@ def main():
     ap.add_argument("--photons", type=int, default=PHOTONS_PER_STEP)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the batched-to-1%%-SE and adjoint comparisons of the default line")
+                    help="skip the extras of the default line (sweep to 1%% SE, adjoint, C1, layered, C5)")
     ap.add_argument("--budget-scale", type=float, default=1.0,
                     help="sweep workload: scale every wavelength's photon budget (profiling on a smaller case)")
     ap.add_argument("--tune", type=int, default=0,
