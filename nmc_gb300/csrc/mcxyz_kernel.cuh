@@ -248,9 +248,13 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
   const float* __restrict__ GF = ADJ ? P.adj_GF : nullptr;
   const int NyNx = P.Ny * P.Nx;
   const unsigned int nvox = (unsigned int)(NyNx * P.Nz);
+  // odd grids step the voxel index at the cell's midpoint; +inf turns the
+  // test off for even grids without a branch
+  const float hdx_e = P.ox ? P.hdx : __int_as_float(0x7f800000), hdy_e = P.oy ? P.hdy : __int_as_float(0x7f800000);
 
   RNG rng;
-  int kx = 0, ky = 0, kz = 0, tiss = 0, depth = 0;
+  int kx = 0, ky = 0, kz = 0, tiss = 0;
+  unsigned int hop_end = 0;  // the sub-step count at which the hop's RAY_DEPTH crossings run out
   float fx = 0.f, fy = 0.f, fz = 0.f, ux = 0.f, uy = 0.f, uz = 1.f;
   float W = 0.f, sleft = 0.f, Rd_loc = 0.f, Atot = 0.f;
   float D = 0.f, Dabs = 0.f;  // adjoint: remaining detected score, sum of |event scores| replayed
@@ -354,7 +358,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
       i = (unsigned int)(iz * NyNx + ix * P.Ny + iy);
       if (!VOX) tiss = idx_ok(i, nvox, &P.sums->flags) ? __ldg(P.V + i) : 0;
       sleft = M::neglog(rng.first_step(k0, k1));  // HOP (:501-502)
-      depth = 0;
+      hop_end = kRAY_DEPTH + 1;
       Rd_loc = Atot = 0.f;
       nsc = nsub = 0;
       if (TRACE) {
@@ -375,12 +379,14 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
                          : (SW ? __ldg(P.sw_core + sbase + tiss) : s_core[tiss]);  // mua, mus, 1/mus, g
     float s = sleft * c.z;
     ++nsub;
-    ++depth;
     // FindVoxelFace2 (helpers.metal:85-114) in cell-local form: path length
     // to the face ahead on each axis
     const float rx = M::rcp(fabsf(ux)), ry = M::rcp(fabsf(uy)), rz = M::rcp(fabsf(uz));
-    const float tx = (ux >= 0.f ? P.dx - fx : fx) * rx;
-    const float ty = (uy >= 0.f ? P.dy - fy : fy) * ry;
+    // offset to the face ahead; it is 0 only for a photon on a lower face
+    // moving down (an upper face is never reached: offsets stay below d)
+    const float dxf = ux >= 0.f ? P.dx - fx : fx, dyf = uy >= 0.f ? P.dy - fy : fy;
+    const float tx = dxf * rx;
+    const float ty = dyf * ry;
     const float tz = (uz >= 0.f ? P.dz - fz : fz) * rz;
     const int ax = (tx <= ty) ? ((tx <= tz) ? 0 : 2) : ((ty <= tz) ? 1 : 2);
     // SameVoxel (helpers.metal:27-39): the end point stays in the cell, upper
@@ -392,8 +398,8 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
     // on two cells' mus through a moving support, which the likelihood-ratio
     // adjoint cannot differentiate.  The two differ only for photons exactly
     // on a lower face (a beam launched on a voxel face).
-    const float sx = (!VOX && ux < 0.f && fx == 0.f) ? P.dx * rx : tx;
-    const float sy = (!VOX && uy < 0.f && fy == 0.f) ? P.dy * ry : ty;
+    const float sx = (!VOX && dxf == 0.f) ? P.dx * rx : tx;
+    const float sy = (!VOX && dyf == 0.f) ? P.dy * ry : ty;
     const bool sv = s <= fminf(sx, fminf(sy, tz));
     if (!sv) s = kLS + fminf(tx, fminf(ty, tz));
     float s_mus = s;  // adjoint: the hop length whose probability depends on mus
@@ -519,7 +525,11 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
         }
         // offsets leave [0, d) only when a point lands on a face (an upper
         // face of the same-voxel end point, a tie between faces)
-        if (fx < 0.f || fx >= P.dx || fy < 0.f || fy >= P.dy || fz < 0.f || fz >= P.dz) {
+        // (one unsigned compare per axis: a negative offset has the sign bit
+        // set and compares above d; -0 and NaN enter, and norm_axis leaves
+        // them as they are)
+        if ((__float_as_uint(fx) >= __float_as_uint(P.dx)) | (__float_as_uint(fy) >= __float_as_uint(P.dy)) |
+            (__float_as_uint(fz) >= __float_as_uint(P.dz))) {
           norm_axis(kx, fx, P.dx, P.dxmax);
           norm_axis(ky, fy, P.dy, P.dymax);
           norm_axis(kz, fz, P.dz, P.dzmax);
@@ -529,8 +539,8 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
     if (back && !fixed_before) adj.M = fmaf(-D_in, s_mus, adj.M);
     if (!sv) {
       // voxel index (:641-643): inside the grid this is the cell plus N/2
-      int ix = P.hx + kx + (P.ox ? (int)(fx >= P.hdx) : 0);
-      int iy = P.hy + ky + (P.oy ? (int)(fy >= P.hdy) : 0);
+      int ix = P.hx + kx + (int)(fx >= hdx_e);
+      int iy = P.hy + ky + (int)(fy >= hdy_e);
       int iz = kz;
       const bool inside = (unsigned)ix < (unsigned)P.Nx && (unsigned)iy < (unsigned)P.Ny &&
                           (unsigned)iz < (unsigned)P.Nz;
@@ -584,7 +594,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
       atomicOr(&P.sums->flags, (unsigned int)NMC_DEVFLAG_STEPCAP);
       continue;
     }
-    if (depth <= kRAY_DEPTH && sleft > 0.f) continue;  // :685
+    if (nsub < hop_end && sleft > 0.f) continue;  // at most RAY_DEPTH crossings per hop (:685)
 
     // ---- SPIN (:688-731 / :1046-1097), ROULETTE (:733-748), next HOP (:501)
     const bool need_roul = W < kTHRESHOLD;
@@ -621,7 +631,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
       ++nev;
     }
     sleft = M::neglog(d.step);
-    depth = 0;
+    hop_end = nsub + kRAY_DEPTH + 1;
   }
 
   __syncthreads();
