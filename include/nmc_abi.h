@@ -151,7 +151,18 @@ enum {
   NMC_FLAG_SKIP_FLUENCE = 1u << 3,
   /* mcsub: deposit F(r,z) and J(r) straight into the global u64 tallies
    * instead of privatising them per block in shared memory. */
-  NMC_FLAG_GLOBAL_TALLIES = 1u << 4
+  NMC_FLAG_GLOBAL_TALLIES = 1u << 4,
+  /* Layered runs: draw from the reference's generator in MCSubKernel's
+   * order (kernels.metal:91-95 seeding; a launch draw, then per hop the step,
+   * the Fresnel choice at a boundary, cos theta, psi and, below THRESHOLD,
+   * the roulette draw: :113-290).  Photon p is (run p / batch + 1, index
+   * p % batch) of the reference's dispatch loop, with batch = the config's
+   * `seed` (PHOTON_BATCH = 10000, definitions.h:17, in the reference).  With
+   * one semi-infinite layer these are the reference kernel's own photons. */
+  NMC_FLAG_LAYERED_REF_STREAMS = 1u << 5,
+  /* Layered runs: isotropic scattering, which is what MCSubKernel samples
+   * (kernels.metal:252 overwrites its Henyey-Greenstein cos theta). */
+  NMC_FLAG_LAYERED_ISOTROPIC = 1u << 6
 };
 
 typedef struct nmc_ext {
@@ -510,8 +521,10 @@ typedef struct nmc_layered_config {
   float dr;
   int32_t nz;                  /* A(z): nz bins of dz + one overflow bin */
   float dz;
-  uint32_t flags;              /* NMC_FLAG_PRECISE_MATH */
-  uint64_t seed;
+  uint32_t flags;              /* NMC_FLAG_PRECISE_MATH, NMC_FLAG_LAYERED_REF_STREAMS,
+                                  NMC_FLAG_LAYERED_ISOTROPIC */
+  uint64_t seed;               /* Philox key; the dispatch batch with
+                                  NMC_FLAG_LAYERED_REF_STREAMS */
 } nmc_layered_config;
 #ifdef __cplusplus
 static_assert(sizeof(nmc_layer) == 20, "nmc_layer layout");

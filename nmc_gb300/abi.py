@@ -42,6 +42,8 @@ FLAG_NO_HARD_KILL = 1 << 1
 FLAG_PRECISE_MATH = 1 << 2
 FLAG_SKIP_FLUENCE = 1 << 3
 FLAG_GLOBAL_TALLIES = 1 << 4
+FLAG_LAYERED_REF_STREAMS = 1 << 5
+FLAG_LAYERED_ISOTROPIC = 1 << 6
 
 FATE_ALIVE, FATE_ESCAPED, FATE_ROULETTE, FATE_MINWEIGHT, FATE_MAXSCATT, FATE_BOUNDARY, FATE_STEPCAP = range(7)
 

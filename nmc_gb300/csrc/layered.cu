@@ -23,6 +23,12 @@
 // key (seed lo, seed hi), counter (photon lo, photon hi, interaction,
 // 'LAYR'): x step, y cos theta, z psi, w roulette; boundary events draw their
 // Fresnel choice from counter (photon lo, photon hi, event | 2^31, 'LAYR').
+// With NMC_FLAG_LAYERED_REF_STREAMS the draws come from the reference's
+// generator in MCSubKernel's order instead (seeding kernels.metal:91-95; a
+// launch draw :113, then per hop the step :183, the Fresnel choice :191,
+// cos theta :244, psi :255, the roulette draw :290), and with
+// NMC_FLAG_LAYERED_ISOTROPIC cos theta = 2 xi - 1 as the reference samples
+// it (:252): one semi-infinite layer then replays MCSubKernel's photons.
 //
 // Adjoint (ADJ): a photon scores once, when it escapes (G_rd[r bin] or
 // G_tt[r bin] times its weight), so the per-layer derivatives of the loss
@@ -81,9 +87,12 @@ struct LayParams {
   const float* g_rd;  // nr + 1 upstream gradient of rd_r (may be null)
   const float* g_tt;  // nr + 1 upstream gradient of tt_r (may be null)
   double* grad;       // 3 * nl: d/dmua, d/dmus, d/dg
+  // reference streams (REF kernels): photon p = (run p / batch + 1, index p % batch)
+  unsigned long long batch;
+  int iso;            // isotropic scattering (the reference's mcsub sampling)
 };
 
-template <bool FAST, bool ADJ>
+template <bool FAST, bool ADJ, bool REF>
 __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
   using M = Math<FAST>;
   __shared__ LayDev s_lay[kMaxLayers];
@@ -118,10 +127,17 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
     float score = 0.f;
     if (ADJ)
       for (int l = 0; l < P.nl; ++l) aL[l] = aN[l] = aQ[l] = 0.f;
-    uint4 r = philox4x32_10(make_uint4(c0, c1, 0u, kLayTag), P.k0, P.k1);
+    TausRng tr;
+    uint4 r = make_uint4(0u, 0u, 0u, 0u);
+    if (REF) {
+      tr.init_photon(pid, P.batch, false, false);
+      tr.next();  // the launch draw (radius 0: the beam stays on the axis)
+    } else {
+      r = philox4x32_10(make_uint4(c0, c1, 0u, kLayTag), P.k0, P.k1);
+    }
     while (alive) {
       const LayDev& Ly = s_lay[L];
-      if (sleft <= 0.f) sleft = M::neglog(u01(r.x));
+      if (sleft <= 0.f) sleft = M::neglog(REF ? tr.step_draw() : u01(r.x));
       // distance to the layer boundary ahead
       const float db = uz > 0.f ? (Ly.z1 - z) / uz : (uz < 0.f ? (Ly.z0 - z) / uz : INFINITY);
       const float s = Ly.inv_mut > 0.f ? sleft * Ly.inv_mut : INFINITY;
@@ -136,9 +152,10 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
         const float nt = Ln < 0 ? P.n_above : (Ln >= P.nl ? P.n_below : s_lay[Ln].n);
         float uzt = 0.f;
         const float R = rfresnel(Ly.n, nt, fabsf(uz), &uzt);
-        const uint4 a = philox4x32_10(make_uint4(c0, c1, ev | 0x80000000u, kLayTag), P.k0, P.k1);
+        const float uf =
+            REF ? tr.next() : u01(philox4x32_10(make_uint4(c0, c1, ev | 0x80000000u, kLayTag), P.k0, P.k1).x);
         ++ev;
-        if (u01(a.x) <= R) {
+        if (uf <= R) {
           uz = -uz;  // reflected
         } else if (Ln < 0 || Ln >= P.nl) {  // escapes
           const float rr = sqrtf(x * x + y * y);
@@ -193,11 +210,12 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
             atomicAdd(P.a_rz + (size_t)ir * (P.nz + 1) + iz, fa);
         }
       }
-      const float cth = hg_sample<FAST>(Ly.ph, u01(r.y));
+      const float ucos = REF ? tr.next() : u01(r.y);
+      const float cth = P.iso ? 2.f * ucos - 1.f : hg_sample<FAST>(Ly.ph, ucos);
       if (ADJ && Ly.ph.hg_mode == 0) aQ[L] += dln_hg_dg(Ly.g, cth);
-      spin<FAST>(cth, u01(r.z), ux, uy, uz);
+      spin<FAST>(cth, REF ? tr.next() : u01(r.z), ux, uy, uz);
       if (w < kTHRESHOLD) {
-        if (u01(r.w) <= kCHANCE)
+        if ((REF ? tr.next() : u01(r.w)) <= kCHANCE)
           w /= kCHANCE;
         else
           alive = false;
@@ -207,7 +225,7 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
         atomicOr(P.flags, (unsigned int)NMC_DEVFLAG_STEPCAP);
         alive = false;
       }
-      r = philox4x32_10(make_uint4(c0, c1, hop, kLayTag), P.k0, P.k1);
+      if (!REF) r = philox4x32_10(make_uint4(c0, c1, hop, kLayTag), P.k0, P.k1);
     }
     if (dep_w > 0.f && idx_ok(dep_l, (unsigned)P.nl, P.flags)) atomicAdd(s_al + dep_l, to_fix(dep_w));
     atomicAdd(&s_sum[NMC_LAY_PHOTONS], 1.0);
@@ -256,6 +274,11 @@ nmc_status layered_impl(int32_t device, const nmc_layered_config* cfg, const nmc
   const bool adj = g_rd || g_tt;
   if (!cfg || !layers || !out) return NMC_EINVAL;
   if (adj && cfg->n_layers > kMaxAdjLayers) return NMC_EINVAL;
+  const bool ref = (cfg->flags & NMC_FLAG_LAYERED_REF_STREAMS) != 0;
+  const bool iso = (cfg->flags & NMC_FLAG_LAYERED_ISOTROPIC) != 0;
+  // the gradients follow the Philox streams and the Henyey-Greenstein phase
+  if (adj && (ref || iso)) return NMC_EUNSUPPORTED;
+  if (ref && cfg->seed == 0) return NMC_EINVAL;  // the dispatch batch
   // fixed-point tallies of one call stay below 2^63; more photons take more
   // calls (first += photons), whose results add up in the caller's arrays
   if (photons > (1ull << 31)) return NMC_EINVAL;
@@ -350,9 +373,13 @@ nmc_status layered_impl(int32_t device, const nmc_layered_config* cfg, const nmc
   P.g_rd = dgrd;
   P.g_tt = dgtt;
   P.grad = dgrad;
+  P.batch = ref ? c.seed : 1;
+  P.iso = iso ? 1 : 0;
   const bool fast = !(c.flags & NMC_FLAG_PRECISE_MATH);
-  const void* f = adj ? (fast ? (const void*)layered_kernel<true, true> : (const void*)layered_kernel<false, true>)
-                      : (fast ? (const void*)layered_kernel<true, false> : (const void*)layered_kernel<false, false>);
+  const void* f =
+      adj ? (fast ? (const void*)layered_kernel<true, true, false> : (const void*)layered_kernel<false, true, false>)
+      : ref ? (fast ? (const void*)layered_kernel<true, false, true> : (const void*)layered_kernel<false, false, true>)
+            : (fast ? (const void*)layered_kernel<true, false, false> : (const void*)layered_kernel<false, false, false>);
   // A(z) joins the per-layer sums in shared memory while both fit in 16 KB
   P.smem_az = (size_t)(c.n_layers + nz1) * 8 <= 16384 ? 1 : 0;
   const size_t smem = (size_t)(c.n_layers + (P.smem_az ? nz1 : 0)) * 8;

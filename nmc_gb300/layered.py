@@ -30,16 +30,18 @@ def _bind():
 
 def run(layers, photons: int, n_above: float = 1.0, n_below: float = 1.0, nr: int = 100, dr: float = 0.01,
         nz: int = 100, dz: float = 0.01, seed: int = 0, first: int = 0, a_rz: bool = False, device: int = 0,
-        precise: bool = False) -> dict:
+        precise: bool = False, flags: int = 0) -> dict:
     """`layers`: sequence of (mua, mus, g, n, thickness) (cm^-1, cm; the last
     thickness may be math.inf).  Returns the sums (abi.LAY_FIELDS), Rd and Tt
     per launched photon with their standard errors, and the tallies
     (un-normalised weights: rd_r, tt_r with nr+1 bins, a_z with nz+1, a_layer,
-    a_rz if asked)."""
+    a_rz if asked).  `flags` may add abi.FLAG_LAYERED_REF_STREAMS (the
+    reference's generator and draw order; `seed` is then the dispatch batch)
+    and abi.FLAG_LAYERED_ISOTROPIC (the reference's isotropic scattering)."""
     L = _bind()
     arr = (abi.Layer * len(layers))(*[abi.Layer(*map(float, q)) for q in layers])
     cfg = abi.LayeredConfig(n_layers=len(layers), n_above=n_above, n_below=n_below, nr=nr, dr=dr, nz=nz, dz=dz,
-                            flags=abi.FLAG_PRECISE_MATH if precise else 0, seed=seed)
+                            flags=(abi.FLAG_PRECISE_MATH if precise else 0) | flags, seed=seed)
     out = np.zeros(len(abi.LAY_FIELDS), np.float64)
     rd, tt, az = np.zeros(nr + 1), np.zeros(nr + 1), np.zeros(nz + 1)
     al = np.zeros(len(layers))

@@ -77,7 +77,7 @@ def oracle_lib():
         lib.orc_speckle_mutual.argtypes = [C.c_int, C.c_int, _P, _P, _P, C.c_int, C.c_float, C.c_float, _P]
         lib.orc_speckle_mutual.restype = None
         lib.orc_layered_run.restype = C.c_int
-        lib.orc_layered_run.argtypes = [C.c_int, _P, _P, C.c_uint64, C.c_uint64, C.c_int, _P, _P, _P, _P, _P]
+        lib.orc_layered_run.argtypes = [C.c_int, _P, _P, C.c_uint64, C.c_uint64, C.c_int, _P, _P, _P, _P, _P, _P]
         lib.orc_efield_run.restype = C.c_int
         lib.orc_efield_run.argtypes = [C.c_int, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int, _P]
         _oracle = lib
@@ -244,17 +244,20 @@ def speckle_mutual(maps, records, counts, lam, lc, out):
 
 def layered(layers, photons: int, n_above: float = 1.0, n_below: float = 1.0, nr: int = 100, dr: float = 0.01,
             nz: int = 100, dz: float = 0.01, seed: int = 0, first: int = 0, real_bits: int = 64,
-            nthreads: int | None = None) -> dict:
+            nthreads: int | None = None, flags: int = 0, per_photon: bool = False) -> dict:
     """The engine's layered model on the CPU (orc_layered_run), with the
-    arguments and the result keys of nmc_gb300.layered.run."""
+    arguments and the result keys of nmc_gb300.layered.run; per_photon adds
+    `per_photon` (photons x 3: escaped up, escaped down, absorbed)."""
     lib = oracle_lib()
     arr = (abi.Layer * len(layers))(*[abi.Layer(*map(float, q)) for q in layers])
     cfg = abi.LayeredConfig(n_layers=len(layers), n_above=n_above, n_below=n_below, nr=nr, dr=dr, nz=nz, dz=dz,
-                            flags=0, seed=seed)
+                            flags=flags, seed=seed)
     out = np.zeros(len(abi.LAY_FIELDS), np.float64)
     rd, tt, az, al = np.zeros(nr + 1), np.zeros(nr + 1), np.zeros(nz + 1), np.zeros(len(layers))
+    pp = np.zeros((photons, 3)) if per_photon else None
     st = lib.orc_layered_run(int(real_bits), C.addressof(cfg), C.addressof(arr), int(first), int(photons),
-                             int(nthreads or os.cpu_count() or 1), _ptr(out), _ptr(rd), _ptr(tt), _ptr(az), _ptr(al))
+                             int(nthreads or os.cpu_count() or 1), _ptr(out), _ptr(rd), _ptr(tt), _ptr(az), _ptr(al),
+                             _ptr(pp))
     if st != 0:
         raise RuntimeError(f"orc_layered_run failed with status {st}")
     res = {k: out[i] for i, k in enumerate(abi.LAY_FIELDS)}
@@ -264,6 +267,8 @@ def layered(layers, photons: int, n_above: float = 1.0, n_below: float = 1.0, nr
         res[k.lower()] = m
         res[k.lower() + "_se"] = math.sqrt(max(res[k + "2"] / n - m * m, 0.0) / n)
     res.update(rd_r=rd, tt_r=tt, a_z=az, a_layer=al)
+    if pp is not None:
+        res["per_photon"] = pp
     return res
 
 

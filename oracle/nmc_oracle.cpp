@@ -952,7 +952,12 @@ bool valid_inputs(const Cfg& c) {
 // Random numbers, as the engine draws them: Philox4x32-10, key (seed lo,
 // seed hi), counter (photon lo, photon hi, interaction, 'LAYR'): x step,
 // y cos theta, z psi, w roulette; boundary events draw their Fresnel choice
-// from counter (photon lo, photon hi, event | 2^31, 'LAYR').
+// from counter (photon lo, photon hi, event | 2^31, 'LAYR').  With
+// NMC_FLAG_LAYERED_REF_STREAMS they come from the reference's generator in
+// MCSubKernel's order (kernels.metal:91-95 seeding, a launch draw :113, then
+// per hop the step :183, the Fresnel choice :191, cos theta :244, psi :255
+// and the roulette draw :290), photon p = (run p / seed + 1, index p % seed);
+// NMC_FLAG_LAYERED_ISOTROPIC samples cos theta as 2 xi - 1 (:252).
 constexpr uint32_t kLayTag = 0x4C415952u;
 constexpr uint32_t kLayStepCap = 20000000u;
 
@@ -970,7 +975,7 @@ struct LayGeom {
 };
 
 template <class R>
-void layered_photon(const LayGeom& G, uint64_t pid, LayTally& T) {
+void layered_photon(const LayGeom& G, uint64_t pid, LayTally& T, double* per_photon) {
   const uint32_t c0 = (uint32_t)pid, c1 = (uint32_t)(pid >> 32);
   const uint32_t k0 = (uint32_t)G.c.seed, k1 = (uint32_t)(G.c.seed >> 32);
   auto block = [&](uint32_t c2, uint32_t* out) {
@@ -979,18 +984,31 @@ void layered_photon(const LayGeom& G, uint64_t pid, LayTally& T) {
     std::memcpy(out, q, sizeof q);
   };
   auto u = [](uint32_t x) { return R(x >> 9) * R(1.0 / 8388608.0) + R(1.0 / 16777216.0); };
+  const bool ref = (G.c.flags & NMC_FLAG_LAYERED_REF_STREAMS) != 0;
+  const bool iso = (G.c.flags & NMC_FLAG_LAYERED_ISOTROPIC) != 0;
+  TausStream g = taus_for(NMC_SIM_MCSUB, pid, ref ? G.c.seed : 1, false);
+  if (ref) g.next_f();  // the launch draw (kernels.metal:113; radius 0 puts the beam on the axis)
   const int nl = G.c.n_layers, nr = G.c.nr, nz = G.c.nz;
   const R idr = R(1) / R(G.c.dr), idz = R(1) / R(G.c.dz);
-  R x = 0, y = 0, z = 0, ux = 0, uy = 0, uz = 1, w = R(G.w0), sleft = 0, rd = 0, tt = 0;
+  R x = 0, y = 0, z = 0, ux = 0, uy = 0, uz = 1, w = R(G.w0), sleft = 0, rd = 0, tt = 0, atot = 0;
   int L = 0;
   uint32_t hop = 0, ev = 0;
   bool alive = true;
   uint32_t r[4];
-  block(0u, r);
+  if (!ref) block(0u, r);
   while (alive) {
     const nmc_layer& Ly = G.lay[L];
     const R mut = R(Ly.mua) + R(Ly.mus);
-    if (sleft <= R(0)) sleft = -std::log(u(r[0]));
+    if (sleft <= R(0)) {
+      if (ref) {
+        float v;
+        while ((v = g.next_f()) <= 0.f) {
+        }
+        sleft = -std::log(R(v));
+      } else {
+        sleft = -std::log(u(r[0]));
+      }
+    }
     const R db = uz > R(0) ? (R(G.z1[L]) - z) / uz : (uz < R(0) ? (R(G.z0[L]) - z) / uz : R(INFINITY));
     const R s = mut > R(0) ? sleft / mut : R(INFINITY);
     if (s >= db) {  // CROSS
@@ -1003,10 +1021,16 @@ void layered_photon(const LayGeom& G, uint64_t pid, LayTally& T) {
       const R nt = Ln < 0 ? R(G.c.n_above) : (Ln >= nl ? R(G.c.n_below) : R(G.lay[Ln].n));
       R uzt = 0;
       const R Rf = rfresnel<R>(R(Ly.n), nt, std::fabs(uz), &uzt);
-      uint32_t a[4];
-      block(ev | 0x80000000u, a);
+      R uf;
+      if (ref) {
+        uf = R(g.next_f());
+      } else {
+        uint32_t a[4];
+        block(ev | 0x80000000u, a);
+        uf = u(a[0]);
+      }
       ++ev;
-      if (u(a[0]) <= Rf) {
+      if (uf <= Rf) {
         uz = -uz;
       } else if (Ln < 0 || Ln >= nl) {  // escapes
         const int ir = std::min((int)(std::sqrt(x * x + y * y) * idr), nr);
@@ -1038,15 +1062,17 @@ void layered_photon(const LayGeom& G, uint64_t pid, LayTally& T) {
     sleft = 0;
     const R absorb = w * R(Ly.mua) / mut;
     w -= absorb;
+    atot += absorb;
     if (absorb > R(0)) {
       const int iz = std::min(std::max((int)(z * idz), 0), nz);
       if (!T.az.empty()) T.az[iz] += (double)absorb;
       T.al[L] += (double)absorb;
     }
-    const R cth = hg_costheta<R>(R(Ly.g), u(r[1]));
-    spin_u<R>(cth, u(r[2]), ux, uy, uz);
+    const R ucos = ref ? R(g.next_f()) : u(r[1]);
+    const R cth = iso ? R(2) * ucos - R(1) : hg_costheta<R>(R(Ly.g), ucos);
+    spin_u<R>(cth, ref ? R(g.next_f()) : u(r[2]), ux, uy, uz);
     if (w < R(kTHRESHOLD)) {
-      if (u(r[3]) <= R(kCHANCE))
+      if ((ref ? R(g.next_f()) : u(r[3])) <= R(kCHANCE))
         w /= R(kCHANCE);
       else
         alive = false;
@@ -1056,7 +1082,12 @@ void layered_photon(const LayGeom& G, uint64_t pid, LayTally& T) {
       T.capped = true;
       alive = false;
     }
-    block(hop, r);
+    if (!ref) block(hop, r);
+  }
+  if (per_photon) {
+    per_photon[0] = (double)rd;
+    per_photon[1] = (double)tt;
+    per_photon[2] = (double)atot;
   }
   T.s[NMC_LAY_PHOTONS] += 1.0;
   T.s[NMC_LAY_RD] += (double)rd;
@@ -1529,8 +1560,9 @@ int orc_efield_run(int real_bits, const nmc_efield_config* cfg, const float* S_p
 
 int orc_layered_run(int real_bits, const nmc_layered_config* cfg, const nmc_layer* layers, uint64_t first,
                     uint64_t n, int nthreads, double* out, double* rd_r, double* tt_r, double* a_z,
-                    double* a_layer) {
+                    double* a_layer, double* per_photon) {
   if (!cfg || !layers || !out || (real_bits != 32 && real_bits != 64)) return NMC_EINVAL;
+  if ((cfg->flags & NMC_FLAG_LAYERED_REF_STREAMS) && cfg->seed == 0) return NMC_EINVAL;
   LayGeom G;
   G.c = *cfg;
   const nmc_layered_config& c = G.c;
@@ -1566,10 +1598,11 @@ int orc_layered_run(int real_bits, const nmc_layered_config* cfg, const nmc_laye
       if (a_z) tl.az.assign((size_t)c.nz + 1, 0.0);
       tl.al.assign((size_t)c.n_layers, 0.0);
       for (uint64_t i = lo; i < hi; ++i) {
+        double* pp = per_photon ? per_photon + 3 * i : nullptr;
         if (real_bits == 64)
-          layered_photon<double>(G, first + i, tl);
+          layered_photon<double>(G, first + i, tl, pp);
         else
-          layered_photon<float>(G, first + i, tl);
+          layered_photon<float>(G, first + i, tl, pp);
       }
     });
   }

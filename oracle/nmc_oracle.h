@@ -64,11 +64,14 @@ double orc_tt_costheta(double gf, double af, double gb, double ab, double cc,
 double orc_hg_costheta(double g, double u);
 
 /* The engine's multi-layer model (nmc_layered_run) restated on the CPU, same
- * Philox layout; out (NMC_LAY_FIELDS) and the tallies are added to (+=) and
- * may be NULL except out.  Returns 0, NMC_EINVAL or NMC_ESTEPCAP. */
+ * Philox layout, or the reference's streams and isotropic phase under the
+ * config's NMC_FLAG_LAYERED_* flags; out (NMC_LAY_FIELDS) and the tallies are
+ * added to (+=) and may be NULL except out; per_photon (may be NULL) gets
+ * (escaped up, escaped down, absorbed) weight per photon, 3 doubles each.
+ * Returns 0, NMC_EINVAL or NMC_ESTEPCAP. */
 int orc_layered_run(int real_bits, const nmc_layered_config* cfg, const nmc_layer* layers, uint64_t first,
                     uint64_t n, int nthreads, double* out, double* rd_r, double* tt_r, double* a_z,
-                    double* a_layer);
+                    double* a_layer, double* per_photon);
 
 /* The engine's polarised E-field model (nmc_efield_run) restated on the CPU,
  * same Philox layout: per setting the NMC_EF_FIELDS sums into `out` (+=;

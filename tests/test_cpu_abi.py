@@ -240,6 +240,8 @@ def test_invalid_configurations_refused_before_any_device_call():
     refused(efield.run, cfg, s633, st, S_raman=s700)
     refused(layered.run, [], 10)
     refused(layered.run, [(0.1, 100.0, 0.9, 1.4, -0.1), (0.1, 100.0, 0.9, 1.4, math.inf)], 10)
+    # the reference's streams need the dispatch batch (seed) to be > 0
+    refused(layered.run, [(0.1, 100.0, 0.9, 1.4, math.inf)], 10, seed=0, flags=abi.FLAG_LAYERED_REF_STREAMS)
     maps = np.zeros((len(abi.EF_MAPS), 4, 4), np.float32)
     recs = np.zeros((1, 4, 4), abi.SPECKLE_DTYPE)
     refused(efield.speckle_mutual, maps, recs, np.zeros((4, 4), np.int32), float("inf"), 1.0)

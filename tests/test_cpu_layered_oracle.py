@@ -3,7 +3,8 @@ closed forms, on the CPU: a clear absorbing slab transmits exp(-mua d) of
 the weight (Beer-Lambert), a clear non-absorbing slab between two index
 steps transmits (1 - r)/(1 + r) (incoherent multiple reflections), weight
 is conserved up to Russian roulette, and one semi-infinite layer gives the
-mcsub restatement's Rd."""
+mcsub restatement's Rd; on the reference's streams one semi-infinite layer
+is, photon for photon, the reference's own mcsub kernel compiled here."""
 import math
 
 import numpy as np
@@ -60,3 +61,35 @@ def test_one_semi_infinite_layer_is_mcsub(oracle):
     se_m = math.sqrt(max(m["rd_sumsq"] / n - rd_m ** 2, 0) / n)
     assert r["specular"] == pytest.approx(m["S"], rel=1e-12)
     assert abs(r["rd"] - rd_m) <= 3 * math.hypot(r["rd_se"], se_m), (r["rd"], r["rd_se"], rd_m, se_m)
+
+
+def test_one_layer_on_reference_streams_is_the_reference_mcsub_kernel(oracle):
+    # One semi-infinite layer on the reference's generator, in MCSubKernel's
+    # draw order and with its isotropic scattering (kernels.metal:252),
+    # against MCSubKernel itself compiled from the reference's sources
+    # (kernels.metal:59-319), photon for photon: photons (run 1..2, index
+    # 0..9999) of the reference's dispatch loop.  Escaped and absorbed weight
+    # per photon within 1e-3 relative (+1e-6), J(r) within 1e-3 of its total.
+    if not oracle.ref_available():
+        pytest.skip("reference sources not present on this machine")
+    import nmc_cases as cases
+    from nmc_gb300 import abi
+
+    rp, tp, _ = cases.mcsub_case(phase=abi.PHASE_ISOTROPIC_REF, rng=abi.RNG_TAUS_REF, dr=0.002, dz=0.002)
+    batch = 10_000
+    ref = oracle.ref_mcsub(rp, tp, run_lo=1, run_hi=2, batch=batch, per_photon=True)
+    n = 2 * batch
+    lay = oracle.layered([(tp.muav[1], tp.musv[1], 0.9, rp.n1, math.inf)], n, n_above=rp.n2, nr=100, dr=0.002,
+                         seed=batch, flags=abi.FLAG_LAYERED_REF_STREAMS | abi.FLAG_LAYERED_ISOTROPIC,
+                         per_photon=True)
+    pr, pl = ref["per_photon"].astype(np.float64), lay["per_photon"]
+    esc = np.isclose(pl[:, 0], pr[:, 2], rtol=1e-3, atol=1e-6)
+    ab = np.isclose(pl[:, 2], pr[:, 1], rtol=1e-3, atol=1e-6)
+    both = float(np.mean(esc & ab))
+    J = ref["J"][1:]  # J[ir], ir = 1..BINS (BINS = overflow) <-> rd_r[ir - 1]
+    dJ = np.abs(J - lay["rd_r"]).sum() / J.sum()
+    print(f"per-photon agreement {both:.5f}; E {ref['SAE'][2]:.6f} vs {lay['Rd']:.6f}; J L1 {dJ:.2e}")
+    assert both >= 0.99
+    assert abs(lay["Rd"] - ref["SAE"][2]) <= 1e-3 * ref["SAE"][2]
+    assert abs(lay["A"] - ref["SAE"][1]) <= 1e-3 * ref["SAE"][1]
+    assert dJ <= 1e-3

@@ -55,6 +55,29 @@ def test_layered_follows_the_oracle(gpu, oracle, layers, n_below):
             assert z.max() <= 3.0, t
 
 
+def test_one_layer_on_reference_streams_follows_the_pinned_oracle(gpu, oracle):
+    # One semi-infinite layer on the reference's generator in MCSubKernel's
+    # draw order, with its isotropic scattering: the oracle's restatement of
+    # this run is, photon for photon, MCSubKernel compiled from the reference
+    # (tests/test_cpu_layered_oracle.py); the GPU follows the same photons.
+    # Totals within 1e-3, Rd(r) within 1e-3 of its total (L1).
+    from nmc_gb300 import layered
+
+    rp, tp, _ = cases.mcsub_case(phase=abi.PHASE_ISOTROPIC_REF, rng=abi.RNG_TAUS_REF, dr=0.002, dz=0.002)
+    batch, n = 10_000, 100_000
+    lay = [(tp.muav[1], tp.musv[1], 0.9, rp.n1, math.inf)]
+    kw = dict(n_above=rp.n2, nr=100, dr=0.002, seed=batch, first=batch,
+              flags=abi.FLAG_LAYERED_REF_STREAMS | abi.FLAG_LAYERED_ISOTROPIC)
+    g = layered.run(lay, n, **kw)
+    o = oracle.layered(lay, n, **kw)
+    dJ = np.abs(g["rd_r"] - o["rd_r"]).sum() / o["rd_r"].sum()
+    print(f"Rd {g['rd']:.6f} / {o['rd']:.6f}, A {g['A'] / n:.6f} / {o['A'] / n:.6f}, Rd(r) L1 {dJ:.2e}")
+    assert abs(g["Rd"] - o["Rd"]) <= 1e-3 * o["Rd"]
+    assert abs(g["A"] - o["A"]) <= 1e-3 * o["A"]
+    assert abs(g["interactions"] - o["interactions"]) <= 1e-3 * o["interactions"]
+    assert dJ <= 1e-3
+
+
 def test_single_layer_equals_mcsub(gpu):
     from nmc_gb300 import layered
 
