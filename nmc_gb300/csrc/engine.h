@@ -102,7 +102,10 @@ struct XyzParams {
   int sw_nsets;
 };
 
-enum XyzMode { kTissue = 0, kVoxel = 1, kAdjoint = 2, kSweep = 3 };
+// kRecord: kVoxel plus the adjoint's detection-event list (its forward pass);
+// kScore: the adjoint's score replay (per photon total score, no tallies);
+// kAdjoint: the adjoint's accumulating replay.
+enum XyzMode { kTissue = 0, kVoxel = 1, kAdjoint = 2, kSweep = 3, kRecord = 4, kScore = 5 };
 
 // Layered semi-infinite kernel (MCSubKernel kernels.metal:59-319).
 struct SubParams {

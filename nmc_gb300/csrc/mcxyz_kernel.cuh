@@ -5,11 +5,14 @@
 // per-voxel optical properties, forward and adjoint).
 //
 // Modes: kTissue reads a uint8 tissue map and a 19-entry table (the
-// reference's model); kVoxel reads (mua, mus, 1/mus, g) per voxel; kAdjoint
-// is kVoxel plus the perturbation Monte Carlo adjoint: in its record pass it
-// appends every detection event (photon, radial bin, weight) to a list, and
-// in its backward pass it replays each detected photon (the same compiled
-// code and random streams, hence the same trajectory) carrying D = the
+// reference's model); kVoxel reads (mua, mus, 1/mus, g) per voxel; kRecord,
+// kScore and kAdjoint are kVoxel plus the passes of the perturbation Monte
+// Carlo adjoint: the record pass (kRecord) is the forward run that also
+// appends every detection event (photon, radial bin, weight) to a list; the
+// score replay (kScore) gives every photon its total score when deposits
+// score too; the accumulating replay (kAdjoint) replays each scoring photon
+// (the same transport code and random streams, hence the same trajectory;
+// sub-steps are bit-identical across the modes) carrying D = the
 // photon's remaining detected score sum_k G[bin_k] w_k over events not yet
 // passed, and accumulates per voxel v (the voxel whose properties the step
 // used)
@@ -223,8 +226,9 @@ template <bool TT, class RNG, bool TRACE, bool FAST, int MODE>
 __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(const XyzParams P) {
   using M = Math<FAST>;
   constexpr bool SW = MODE == kSweep;  // many tissue tables, one per set
-  constexpr bool VOX = MODE == kVoxel || MODE == kAdjoint;
-  constexpr bool ADJ = MODE == kAdjoint;
+  constexpr bool VOX = MODE == kVoxel || MODE == kAdjoint || MODE == kRecord || MODE == kScore;
+  constexpr bool ADJ = MODE == kAdjoint || MODE == kScore;  // replays
+  constexpr bool REC = MODE == kRecord;
   __shared__ float4 s_core[NMC_NTISS];
   __shared__ PhaseConst s_ph[NMC_NTISS];
   __shared__ unsigned long long s_tot[5];  // photons, substeps, scatters, A, rd
@@ -242,9 +246,9 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
   const uint32_t k0 = P.rng.k0;
   uint32_t k1 = P.rng.k1;  // a sweep set s draws from key (k0, k1 + s)
   const bool hard_kill = !(P.flags & NMC_FLAG_NO_HARD_KILL);
-  const bool back = ADJ && P.adj_pass == 1;   // accumulating replay
-  const bool score = ADJ && P.adj_pass == 2;  // score replay: D[photon] = its total score
-  const bool replay = back || score;          // replays write no tallies
+  constexpr bool back = MODE == kAdjoint;  // accumulating replay
+  constexpr bool score = MODE == kScore;   // score replay: D[photon] = its total score
+  constexpr bool replay = back || score;   // replays write no tallies
   const float* __restrict__ GF = ADJ ? P.adj_GF : nullptr;
   const int NyNx = P.Ny * P.Nx;
   const unsigned int nvox = (unsigned int)(NyNx * P.Nz);
@@ -258,6 +262,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
   float fx = 0.f, fy = 0.f, fz = 0.f, ux = 0.f, uy = 0.f, uz = 1.f;
   float W = 0.f, sleft = 0.f, Rd_loc = 0.f, Atot = 0.f;
   float D = 0.f, Dabs = 0.f;  // adjoint: remaining detected score, sum of |event scores| replayed
+  float gf_i = 0.f;           // adjoint: upstream fluence gradient of voxel i (0 without a fluence loss)
   unsigned int i = 0, slot = 0, nsc = 0, nsub = 0, st = 0;
   unsigned int set = 0, sbase = 0;  // sweep: the photon's set and its table offset
   unsigned long long pidx = 0;
@@ -357,6 +362,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
       const int iz = min(max(lookup_index(kz, fz, 0, 0, 0.f), 0), P.Nz - 1);
       i = (unsigned int)(iz * NyNx + ix * P.Ny + iy);
       if (!VOX) tiss = idx_ok(i, nvox, &P.sums->flags) ? __ldg(P.V + i) : 0;
+      if (ADJ && GF) gf_i = idx_ok(i, nvox, &P.sums->flags) ? __ldg(GF + i) : 0.f;
       sleft = M::neglog(rng.first_step(k0, k1));  // HOP (:501-502)
       hop_end = kRAY_DEPTH + 1;
       Rd_loc = Atot = 0.f;
@@ -411,7 +417,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
       W -= absorb;
       Atot += absorb;
       if (replay) {
-        const float gf = (GF && (st & kBflag)) ? __ldg(GF + i) : 0.f;
+        const float gf = (st & kBflag) ? gf_i : 0.f;
         e_dep = gf * absorb;
         if (score) {
           D += e_dep;
@@ -488,7 +494,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
                   if (P.rd_r && idx_ok(rbin, (unsigned)P.rd_bins + 1u, &P.sums->flags))
                     atomicAdd(P.rd_r + rbin, to_fix(dw));
                 }
-                if (ADJ) {  // record pass: keep (photon, bin, weight) for the backward pass
+                if (REC) {  // record pass: keep (photon, bin, weight) for the backward pass
                   const unsigned long long k = atomicAdd(P.ev_count, 1ull);
                   if (k < P.ev_cap) P.ev[k] = AdjEvent{(unsigned int)pidx, rbin, dw, 0.f};
                 }
@@ -588,6 +594,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
       }
       i = (unsigned int)(iz * NyNx + ix * P.Ny + iy);  // :675-679
       if (!VOX) tiss = idx_ok(i, nvox, &P.sums->flags) ? __ldg(P.V + i) : 0;
+      if (ADJ && GF) gf_i = idx_ok(i, nvox, &P.sums->flags) ? __ldg(GF + i) : 0.f;
     }
     if (nsub >= P.step_cap) {  // device-side cap: not a reference behaviour
       kill(NMC_FATE_STEPCAP);

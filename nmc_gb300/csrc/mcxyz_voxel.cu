@@ -11,6 +11,12 @@ const void* pick_voxel(int mode, bool trace, bool fast) {
   if (mode == kAdjoint)
     return fast ? (const void*)mcxyz_kernel<false, PhiloxRng<false>, false, true, kAdjoint>
                 : (const void*)mcxyz_kernel<false, PhiloxRng<false>, false, false, kAdjoint>;
+  if (mode == kRecord)
+    return fast ? (const void*)mcxyz_kernel<false, PhiloxRng<false>, false, true, kRecord>
+                : (const void*)mcxyz_kernel<false, PhiloxRng<false>, false, false, kRecord>;
+  if (mode == kScore)
+    return fast ? (const void*)mcxyz_kernel<false, PhiloxRng<false>, false, true, kScore>
+                : (const void*)mcxyz_kernel<false, PhiloxRng<false>, false, false, kScore>;
   if (trace)
     return fast ? (const void*)mcxyz_kernel<false, PhiloxRng<false>, true, true, kVoxel>
                 : (const void*)mcxyz_kernel<false, PhiloxRng<false>, true, false, kVoxel>;

@@ -379,7 +379,7 @@ nmc_status launch(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_record* 
     }
     block = h->ext.block_size > 0 ? h->ext.block_size : 256;
     const bool tt = h->sim == NMC_SIM_MCXYZ_TT;
-    const int mode = adj ? nmc::kAdjoint : nmc::kVoxel;
+    const int mode = !adj ? nmc::kVoxel : adj->pass == 0 ? nmc::kRecord : adj->pass == 2 ? nmc::kScore : nmc::kAdjoint;
     if (h->voxel_mode)
       NMC_CUDA(h, nmc::mcxyz_voxel_occupancy(mode, trace, block, &per_sm));
     else
