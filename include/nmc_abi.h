@@ -377,6 +377,19 @@ nmc_status nmc_set_radial_tally(nmc_handle* h, int32_t bins, float dr);
  * (Nx*Ny*Nz doubles each, any may be NULL), the path-length and
  * likelihood-ratio estimator of the same photons. */
 nmc_status nmc_adjoint_forward(nmc_handle* h, uint64_t first, uint64_t n, uint64_t event_capacity);
+/* As nmc_adjoint_forward, and also keeps the deposit list of the photons:
+ * every (voxel, absorbed weight) the run adds to NMC_TALLY_F3D, merged per
+ * visit of a photon to a voxel, room for `deposit_capacity` records of 8
+ * bytes (about 0.7 records per voxel sub-step; 0 keeps none) plus one
+ * 2 KB chunk per thread of the launch.  With the list
+ * a backward with a deposit gradient gets each photon's total score from it
+ * instead of replaying every photon for it.  A list that outgrows its
+ * capacity is dropped, and that backward replays the scores as without one.
+ * No reference counterpart. */
+nmc_status nmc_adjoint_forward_ex(nmc_handle* h, uint64_t first, uint64_t n, uint64_t event_capacity,
+                                  uint64_t deposit_capacity);
+/* 1 if the last adjoint forward kept a complete deposit list, else 0. */
+int32_t nmc_adjoint_deposit_list_complete(nmc_handle* h);
 nmc_status nmc_adjoint_backward(nmc_handle* h, const float* grad_rd_r, double* grad_mua,
                                 double* grad_mus, double* grad_g);
 /* As nmc_adjoint_backward, with the upstream gradient of the absorbed-weight
@@ -384,7 +397,8 @@ nmc_status nmc_adjoint_backward(nmc_handle* h, const float* grad_rd_r, double* g
  * fluence is that tally / (mua * photons * voxel volume), whose chain rule
  * stays with the caller).  Either gradient may be NULL, not both.  With a
  * deposit gradient the detected photons are not enough: every photon is
- * replayed twice (its total score first, then the accumulation). */
+ * replayed, after its total score is summed from the forward's deposit list
+ * (nmc_adjoint_forward_ex) or, without one, from a first replay. */
 nmc_status nmc_adjoint_backward_ex(nmc_handle* h, const float* grad_rd_r, const float* grad_absorbed,
                                    double* grad_mua, double* grad_mus, double* grad_g);
 

@@ -33,11 +33,12 @@ from .engine import Engine
 
 class _Transport(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, mua, mus, g, engine: Engine, first: int, n: int, event_capacity: int | None):
-        ctx.engine, ctx.first, ctx.n, ctx.cap = engine, int(first), int(n), event_capacity
+    def forward(ctx, mua, mus, g, engine: Engine, first: int, n: int, event_capacity: int | None,
+                deposit_capacity: int):
+        ctx.engine, ctx.first, ctx.n, ctx.cap, ctx.dcap = engine, int(first), int(n), event_capacity, deposit_capacity
         ctx.shape = tuple(mua.shape)
         ctx.save_for_backward(mua, mus, g)
-        _forward(engine, mua, mus, g, first, n, event_capacity)
+        _forward(engine, mua, mus, g, first, n, event_capacity, deposit_capacity)
         ctx.token = engine._adj_token
         rd = engine.tally(abi.TALLY_RD_R) / float(n)
         ab = engine.tally(abi.TALLY_F3D) / float(n)
@@ -51,7 +52,7 @@ class _Transport(torch.autograd.Function):
             # the handle ran another forward since: record this one again
             # (same photon streams, so the same events)
             mua, mus, g = ctx.saved_tensors
-            _forward(e, mua, mus, g, ctx.first, ctx.n, ctx.cap)
+            _forward(e, mua, mus, g, ctx.first, ctx.n, ctx.cap, ctx.dcap)
             ctx.token = e._adj_token
 
         def host(t):
@@ -66,7 +67,7 @@ class _Transport(torch.autograd.Function):
         if G is None and GF is None:
             z = torch.zeros_like(mua)
             return (z if need[0] else None, z if need[1] else None, z if need[2] else None,
-                    None, None, None, None)
+                    None, None, None, None, None)
         ga, gs, gg = e.adjoint_backward(G, GF)
 
         def out(a, want):
@@ -74,35 +75,39 @@ class _Transport(torch.autograd.Function):
                 return None
             return torch.as_tensor(a.reshape(ctx.shape), dtype=mua.dtype, device=mua.device)
 
-        return out(ga, need[0]), out(gs, need[1]), out(gg, need[2]), None, None, None, None
+        return out(ga, need[0]), out(gs, need[1]), out(gg, need[2]), None, None, None, None, None
 
 
-def _forward(e: Engine, mua, mus, g, first, n, cap):
+def _forward(e: Engine, mua, mus, g, first, n, cap, dcap):
     def host(t):
         return t.detach().to("cpu", torch.float32).contiguous().numpy().ravel()
 
     e.set_voxel_props(host(mua), host(mus), host(g))
     e.reset()
-    e.adjoint_forward(first, n, cap)
+    e.adjoint_forward(first, n, cap, dcap)
     e._adj_token = getattr(e, "_adj_token", 0) + 1
 
 
 def transport(mua: torch.Tensor, mus: torch.Tensor, g: torch.Tensor, engine: Engine, first: int = 0,
-              n: int = 1_000_000, event_capacity: int | None = None):
+              n: int = 1_000_000, event_capacity: int | None = None, deposit_capacity: int | None = None):
     """(rd_r, absorbed) per launched photon for photons [first, first + n)
     through per-voxel media (arrays of Nz x Nx x Ny or flat, engine voxel
     order), differentiable in mua, mus and g.  `engine` is an NMC_SIM_MCXYZ
     Engine after prepare_data and set_radial_tally; its other tallies hold
-    this forward's photons afterwards."""
+    this forward's photons afterwards.  deposit_capacity (records of 8
+    bytes; default 600 per photon) sizes the forward's deposit list, which
+    spares a backward through `absorbed` its score replay; 0 keeps none."""
     if engine.sim_type != abi.SIM_MCXYZ:
         raise ValueError("transport needs an NMC_SIM_MCXYZ engine")
-    return _Transport.apply(mua, mus, g, engine, first, n, event_capacity)
+    dcap = 600 * int(n) if deposit_capacity is None else int(deposit_capacity)
+    return _Transport.apply(mua, mus, g, engine, first, n, event_capacity, dcap)
 
 
 def radial_reflectance(mua, mus, g, engine: Engine, first: int = 0, n: int = 1_000_000,
                        event_capacity: int | None = None) -> torch.Tensor:
-    """Rd(r) per launched photon (bins + 1 values, last = overflow)."""
-    return transport(mua, mus, g, engine, first, n, event_capacity)[0]
+    """Rd(r) per launched photon (bins + 1 values, last = overflow); no
+    deposit list is kept (only detections score)."""
+    return transport(mua, mus, g, engine, first, n, event_capacity, deposit_capacity=0)[0]
 
 
 def fluence(absorbed: torch.Tensor, mua: torch.Tensor, voxel_volume: float) -> torch.Tensor:

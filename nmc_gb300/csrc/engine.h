@@ -92,6 +92,14 @@ struct XyzParams {
   double* gL;                 // per voxel: sum D * charged path length (absorption)
   double* gM;                 // per voxel: d ln p(path)/dmus terms weighted by D
   double* gQ;                 // per voxel: sum D * dln p_HG / dg over scatterings
+  // record pass with a deposit list (for a fluence loss): every merged
+  // deposit (voxel, weight) of a photon, in chunks of kDepChunk records taken
+  // by the threads from a pool; a chunk starts with a header record
+  // (0xFFFFFFFF, photon index) and every photon's records follow its header
+  uint2* dl_pool;             // dl_chunks * kDepChunk records, or null: no list
+  unsigned int dl_chunks;
+  unsigned int* dl_fill;      // records written per chunk
+  unsigned long long* dl_next;  // chunks taken (may pass dl_chunks: the list is then incomplete)
   // batched sweep over tissue tables (one table per set, e.g. per wavelength)
   const float4* sw_core;               // n_sets * NMC_NTISS (mua, mus, 1/mus, g)
   const PhaseConst* sw_phase;          // n_sets * NMC_NTISS
@@ -105,6 +113,8 @@ struct XyzParams {
 // kRecord: kVoxel plus the adjoint's detection-event list (its forward pass);
 // kScore: the adjoint's score replay (per photon total score, no tallies);
 // kAdjoint: the adjoint's accumulating replay.
+constexpr unsigned int kDepChunk = 256;  // deposit-list records per chunk
+
 enum XyzMode { kTissue = 0, kVoxel = 1, kAdjoint = 2, kSweep = 3, kRecord = 4, kScore = 5 };
 
 // Layered semi-infinite kernel (MCSubKernel kernels.metal:59-319).
@@ -185,6 +195,9 @@ cudaError_t launch_mcxyz_sweep(const XyzParams& p, bool two_term, int grid, int 
 cudaError_t mcxyz_sweep_occupancy(bool two_term, int block, int* blocks_per_sm);
 cudaError_t launch_adjoint_scores(const AdjEvent* ev, unsigned int n_ev, const float* G, float* D,
                                   cudaStream_t stream);
+// D[photon] += sum GF[voxel] * deposit over the record pass's deposit list
+cudaError_t launch_deposit_scores(const uint2* pool, const unsigned int* fill, unsigned int n_chunks,
+                                  const float* GF, float* D, unsigned long long n_photons, cudaStream_t stream);
 
 cudaError_t launch_mcsub(const SubParams& p, bool trace, int grid, int block, cudaStream_t stream);
 cudaError_t mcsub_occupancy(const SubParams& p, bool trace, int block, int* blocks_per_sm);

@@ -223,7 +223,10 @@ __device__ __forceinline__ float dlnhg_dg(float g, float mu) {
 }
 
 template <bool TT, class RNG, bool TRACE, bool FAST, int MODE>
-__global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(const XyzParams P) {
+// 4 blocks of 256 per SM in every mode: the accumulating replay fits 64
+// registers without spills too (left to itself the compiler takes 78 and 3
+// blocks, 7% slower)
+__global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
   using M = Math<FAST>;
   constexpr bool SW = MODE == kSweep;  // many tissue tables, one per set
   constexpr bool VOX = MODE == kVoxel || MODE == kAdjoint || MODE == kRecord || MODE == kScore;
@@ -268,6 +271,30 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
   unsigned long long pidx = 0;
   uint32_t fate = NMC_FATE_ALIVE, ndet = 0, nev = 0;  // trace only
   Deposit dep{0xFFFFFFFFu, 0.f};
+  // record pass: the thread's chunk of the deposit list and its fill
+  constexpr unsigned int kNoChunk = 0xFFFFFFFFu, kDeadChunk = 0xFFFFFFFEu;
+  unsigned int dl_chunk = (REC && P.dl_pool) ? kNoChunk : kDeadChunk, dl_pos = kDepChunk;
+  // the next record goes to a fresh chunk (its header names the photon)
+  // when the current one is full; past the pool's end the list stops
+  auto dl_put = [&](unsigned int a, unsigned int b) {
+    if (dl_chunk == kDeadChunk) return;
+    if (dl_pos >= kDepChunk) {
+      if (dl_chunk != kNoChunk) P.dl_fill[dl_chunk] = dl_pos;
+      const unsigned long long c = atomicAdd(P.dl_next, 1ull);
+      if (c >= P.dl_chunks) {
+        dl_chunk = kDeadChunk;
+        return;
+      }
+      dl_chunk = (unsigned int)c;
+      P.dl_pool[(size_t)dl_chunk * kDepChunk] = make_uint2(0xFFFFFFFFu, (unsigned int)pidx);
+      dl_pos = 1;
+      if (a == 0xFFFFFFFFu) return;  // the chunk's header is the photon's
+    }
+    P.dl_pool[(size_t)dl_chunk * kDepChunk + dl_pos++] = make_uint2(a, b);
+  };
+  auto dl_deposit = [&]() {  // the merged deposit about to be flushed to F3D
+    if (REC && dep.acc > 0.f) dl_put(dep.idx, __float_as_uint(dep.acc));
+  };
   AdjAcc adj{0xFFFFFFFFu, 0.f, 0.f, 0.f};
 
   auto kill = [&](uint32_t why) {
@@ -296,6 +323,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
         }
       }
       if ((st & kHave) && !replay && !SW) {  // retire the finished photon
+        dl_deposit();
         dep.flush(P.F3D, nvox, &P.sums->flags);
         if (Rd_loc > 0.f && idx_ok(slot, P.nslots, &P.sums->flags))
           atomicAdd(P.rd_slots + slot, to_fix(Rd_loc));  // :753
@@ -332,6 +360,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
       }
       if (score) D = 0.f;
       unsigned long long pid = P.first + pidx;
+      if (REC) dl_put(0xFFFFFFFFu, (unsigned int)pidx);  // the photon's deposits follow
       if (SW) {  // the queue slot whose budget holds this photon: last k with prefix[k] <= pidx
         unsigned int lo = 0, hi = (unsigned int)P.sw_nsets;
         while (hi - lo > 1) {
@@ -431,6 +460,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
           Dabs += fabsf(e_dep);
         }
       } else if (!SW && (st & kBflag)) {
+        if (REC && i != dep.idx) dl_deposit();
         dep.add(P.F3D, i, absorb, nvox, &P.sums->flags);
       }
     }
@@ -641,6 +671,7 @@ __global__ void __launch_bounds__(256, MODE == kAdjoint ? 3 : 4) mcxyz_kernel(co
     hop_end = nsub + kRAY_DEPTH + 1;
   }
 
+  if (REC && dl_chunk < kDeadChunk) P.dl_fill[dl_chunk] = dl_pos;
   __syncthreads();
   if (threadIdx.x < 5 && s_tot[threadIdx.x]) {
     unsigned long long* dst = threadIdx.x == 0   ? &P.sums->photons

@@ -33,7 +33,41 @@ __global__ void adjoint_scores_kernel(const AdjEvent* __restrict__ ev, unsigned 
   }
 }
 
+// One thread per chunk of the deposit list: each photon's run of records
+// (from its header to the next header or the chunk's end) adds its
+// sum GF[voxel] * deposit to D[photon] with one atomic.
+__global__ void deposit_scores_kernel(const uint2* __restrict__ pool, const unsigned int* __restrict__ fill,
+                                      unsigned int n_chunks, const float* __restrict__ GF, float* __restrict__ D,
+                                      unsigned long long n_photons) {
+  for (unsigned int c = blockIdx.x * blockDim.x + threadIdx.x; c < n_chunks; c += gridDim.x * blockDim.x) {
+    const uint2* r = pool + (size_t)c * kDepChunk;
+    const unsigned int n = min(fill[c], kDepChunk);
+    unsigned int p = 0xFFFFFFFFu;
+    float sum = 0.f;
+    for (unsigned int k = 0; k < n; ++k) {
+      const uint2 x = r[k];
+      if (x.x == 0xFFFFFFFFu) {
+        if (p < n_photons && sum != 0.f) atomicAdd(D + p, sum);
+        p = x.y;
+        sum = 0.f;
+      } else {
+        sum = fmaf(__ldg(GF + x.x), __uint_as_float(x.y), sum);
+      }
+    }
+    if (p < n_photons && sum != 0.f) atomicAdd(D + p, sum);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_deposit_scores(const uint2* pool, const unsigned int* fill, unsigned int n_chunks,
+                                  const float* GF, float* D, unsigned long long n_photons, cudaStream_t stream) {
+  if (n_chunks == 0) return cudaSuccess;
+  const int block = 256;
+  const unsigned int grid = (n_chunks + block - 1) / block < 8192u ? (n_chunks + block - 1) / block : 8192u;
+  deposit_scores_kernel<<<grid, block, 0, stream>>>(pool, fill, n_chunks, GF, D, n_photons);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_mcxyz_voxel(const XyzParams& p, int mode, bool trace, int grid, int block,
                                cudaStream_t stream) {

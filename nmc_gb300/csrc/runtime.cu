@@ -98,6 +98,14 @@ struct nmc_handle {
   unsigned long long* d_evcount = nullptr;
   uint64_t ev_cap = 0, ev_limit = 0, adj_first = 0, adj_n = 0;  // allocated / requested events
   bool adj_ready = false;
+  // the record pass's deposit list (adjoint of a fluence loss without a score replay)
+  uint2* d_dl = nullptr;
+  unsigned int* d_dlfill = nullptr;
+  unsigned long long* d_dlnext = nullptr;
+  unsigned int dl_chunks = 0;  // allocated chunks
+  unsigned int dl_req = 0;     // chunks the last record pass could use
+  unsigned int dl_used = 0;    // chunks the last record pass filled
+  bool dl_ok = false;          // the last record pass's list is complete
 };
 
 namespace {
@@ -141,6 +149,11 @@ void free_buffers(nmc_handle* h) {
   dfree(h->d_rdr);
   dfree(h->d_ev);
   dfree(h->d_evcount);
+  dfree(h->d_dl);
+  dfree(h->d_dlfill);
+  dfree(h->d_dlnext);
+  h->dl_chunks = 0;
+  h->dl_ok = false;
   dfree(h->c_F3D);
   dfree(h->c_Rd2D);
   dfree(h->c_Det);
@@ -314,6 +327,7 @@ struct AdjArgs {
   double* gL;
   double* gM;
   double* gQ;
+  bool deposit_list = false;  // record pass: also keep the deposit list
 };
 
 nmc_status fold(nmc_handle* h);
@@ -376,6 +390,12 @@ nmc_status launch(nmc_handle* h, uint64_t first, uint64_t n, nmc_photon_record* 
       p.gL = adj->gL;
       p.gM = adj->gM;
       p.gQ = adj->gQ;
+      if (adj->pass == 0 && adj->deposit_list) {
+        p.dl_pool = h->d_dl;
+        p.dl_chunks = h->dl_req;
+        p.dl_fill = h->d_dlfill;
+        p.dl_next = h->d_dlnext;
+      }
     }
     block = h->ext.block_size > 0 ? h->ext.block_size : 256;
     const bool tt = h->sim == NMC_SIM_MCXYZ_TT;
@@ -1301,13 +1321,25 @@ nmc_status nmc_set_radial_tally(nmc_handle* h, int32_t bins, float dr) {
   return build_xyz(h);
 }
 
-nmc_status nmc_adjoint_forward(nmc_handle* h, uint64_t first, uint64_t n, uint64_t event_capacity) {
+nmc_status nmc_adjoint_forward_ex(nmc_handle* h, uint64_t first, uint64_t n, uint64_t event_capacity,
+                                  uint64_t deposit_capacity) {
   if (!h) return NMC_EINVAL;
   NMC_ON_DEVICE(h);
   if (!h->prepared || !h->voxel_mode) return fail(h, NMC_ESTATE, "the adjoint needs nmc_set_voxel_props");
   if (h->rd_bins < 1) return fail(h, NMC_ESTATE, "the adjoint differentiates the radial tally: nmc_set_radial_tally");
   if (n >= 0xFFFFFFFFull || event_capacity == 0 || event_capacity >= 0xFFFFFFFFull)
     return fail(h, NMC_EINVAL, "adjoint runs need n < 2^32 photons and 0 < event_capacity < 2^32");
+  // every thread of the launch holds one chunk at a time: the pool adds one
+  // chunk per thread to the records asked for, so the capacity counts records
+  uint64_t chunks = 0;
+  if (deposit_capacity > 0) {
+    const int block = h->ext.block_size > 0 ? h->ext.block_size : 256;
+    int per_sm = 0;
+    NMC_CUDA(h, nmc::mcxyz_voxel_occupancy(nmc::kRecord, false, block, &per_sm));
+    const uint64_t threads = (uint64_t)h->nsm * (uint64_t)std::max(per_sm, 1) * (uint64_t)block;
+    chunks = (deposit_capacity + nmc::kDepChunk - 1) / nmc::kDepChunk + threads;
+  }
+  if (chunks >= 0xFFFFFFF0ull) return fail(h, NMC_EINVAL, "deposit_capacity too large");
   nmc_status st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
   if (h->ev_cap < event_capacity) {
@@ -1318,7 +1350,28 @@ nmc_status nmc_adjoint_forward(nmc_handle* h, uint64_t first, uint64_t n, uint64
   h->ev_limit = event_capacity;
   if (!h->d_evcount) NMC_CUDA(h, cudaMalloc((void**)&h->d_evcount, sizeof(unsigned long long)));
   NMC_CUDA(h, cudaMemsetAsync(h->d_evcount, 0, sizeof(unsigned long long), h->stream));
+  h->dl_ok = false;
+  bool list = chunks > 0;
+  if (list && chunks > h->dl_chunks) {  // grow-only, like the event list
+    dfree(h->d_dl);
+    dfree(h->d_dlfill);
+    h->dl_chunks = 0;
+    // the list only saves time: without the memory the run keeps none
+    if (cudaMalloc((void**)&h->d_dl, chunks * nmc::kDepChunk * sizeof(uint2)) != cudaSuccess ||
+        cudaMalloc((void**)&h->d_dlfill, chunks * sizeof(unsigned int)) != cudaSuccess) {
+      (void)cudaGetLastError();
+      dfree(h->d_dl);
+      dfree(h->d_dlfill);
+      list = false;
+    } else {
+      h->dl_chunks = (unsigned int)chunks;
+    }
+  }
+  h->dl_req = list ? (unsigned int)chunks : 0;
+  if (list && !h->d_dlnext) NMC_CUDA(h, cudaMalloc((void**)&h->d_dlnext, sizeof(unsigned long long)));
+  if (list) NMC_CUDA(h, cudaMemsetAsync(h->d_dlnext, 0, sizeof(unsigned long long), h->stream));
   AdjArgs a{0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  a.deposit_list = list;
   st = launch(h, first, n, nullptr, nullptr, 0, &a);
   if (st == NMC_OK) st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
@@ -1331,11 +1384,23 @@ nmc_status nmc_adjoint_forward(nmc_handle* h, uint64_t first, uint64_t n, uint64
                   (unsigned long long)h->ev_limit);
     return fail(h, NMC_EINVAL, msg);
   }
+  if (list) {  // a list that ran out of chunks is dropped: the backward replays the scores instead
+    unsigned long long used = 0;
+    NMC_CUDA(h, cudaMemcpy(&used, h->d_dlnext, sizeof used, cudaMemcpyDeviceToHost));
+    h->dl_ok = used <= h->dl_req;
+    h->dl_used = (unsigned int)std::min<unsigned long long>(used, h->dl_req);
+  }
   h->adj_first = first;
   h->adj_n = n;
   h->adj_ready = true;
   return st;
 }
+
+nmc_status nmc_adjoint_forward(nmc_handle* h, uint64_t first, uint64_t n, uint64_t event_capacity) {
+  return nmc_adjoint_forward_ex(h, first, n, event_capacity, 0);
+}
+
+int32_t nmc_adjoint_deposit_list_complete(nmc_handle* h) { return h && h->adj_ready && h->dl_ok ? 1 : 0; }
 
 nmc_status nmc_adjoint_backward_ex(nmc_handle* h, const float* grad_rd_r, const float* grad_absorbed,
                                    double* grad_mua, double* grad_mus, double* grad_g) {
@@ -1362,7 +1427,14 @@ nmc_status nmc_adjoint_backward_ex(nmc_handle* h, const float* grad_rd_r, const 
                         : cudaMemsetAsync(G, 0, bG, h->stream)) == cudaSuccess;
   if (GF) ok = ok && cudaMemcpyAsync(GF, grad_absorbed, bF, cudaMemcpyHostToDevice, h->stream) == cudaSuccess;
   if (!ok) return fail(h, NMC_EDEVICE, "adjoint set-up");
-  if (GF) {
+  if (GF && h->dl_ok) {
+    // deposits score too: each photon's total score from the events and
+    // the record pass's deposit list
+    if (cudaMemsetAsync(D, 0, bD, h->stream) != cudaSuccess ||
+        nmc::launch_adjoint_scores(h->d_ev, (unsigned int)cnt, G, D, h->stream) != cudaSuccess ||
+        nmc::launch_deposit_scores(h->d_dl, h->d_dlfill, h->dl_used, GF, D, h->adj_n, h->stream) != cudaSuccess)
+      return fail(h, NMC_EDEVICE, "adjoint scores");
+  } else if (GF) {
     // deposits score too: a first replay gives every photon its total score
     AdjArgs a{2, D, G, GF, nullptr, nullptr, nullptr};
     st = launch(h, h->adj_first, h->adj_n, nullptr, nullptr, 0, &a);

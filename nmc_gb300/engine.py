@@ -77,13 +77,17 @@ def lib() -> C.CDLL:
         L.nmc_set_voxel_props.argtypes = [H, _P, _P, _P]
         L.nmc_set_radial_tally.argtypes = [H, C.c_int32, C.c_float]
         L.nmc_adjoint_forward.argtypes = [H, C.c_uint64, C.c_uint64, C.c_uint64]
+        L.nmc_adjoint_forward_ex.argtypes = [H, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64]
+        L.nmc_adjoint_deposit_list_complete.argtypes = [H]
+        L.nmc_adjoint_deposit_list_complete.restype = C.c_int32
         L.nmc_adjoint_backward.argtypes = [H, _P, _P, _P, _P]
         L.nmc_adjoint_backward_ex.argtypes = [H, _P, _P, _P, _P, _P]
         for name in ("nmc_create", "nmc_prepare", "nmc_set_ext", "nmc_set_tissue_params", "nmc_set_num_runs_seed",
                      "nmc_send_compute_command", "nmc_run", "nmc_run_async", "nmc_synchronize",
                      "nmc_run_traced", "nmc_get_compute_results", "nmc_get_summary",
                      "nmc_get_tally_f64", "nmc_reset", "nmc_set_voxel_props", "nmc_set_radial_tally",
-                     "nmc_adjoint_forward", "nmc_adjoint_backward", "nmc_adjoint_backward_ex"):
+                     "nmc_adjoint_forward", "nmc_adjoint_forward_ex", "nmc_adjoint_backward",
+                     "nmc_adjoint_backward_ex"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -271,9 +275,17 @@ class Engine:
     def set_radial_tally(self, bins: int, dr: float):
         self._check(self._L.nmc_set_radial_tally(self._h, int(bins), float(dr)), "nmc_set_radial_tally")
 
-    def adjoint_forward(self, first: int, n: int, event_capacity: int | None = None):
+    def adjoint_forward(self, first: int, n: int, event_capacity: int | None = None, deposit_capacity: int = 0):
+        """The record pass of the adjoint; deposit_capacity > 0 also keeps the
+        deposit list (8 bytes a record) that spares a fluence-loss backward
+        its score replay."""
         cap = int(event_capacity) if event_capacity else max(1 << 20, 4 * int(n))
-        self._check(self._L.nmc_adjoint_forward(self._h, int(first), int(n), cap), "nmc_adjoint_forward")
+        self._check(self._L.nmc_adjoint_forward_ex(self._h, int(first), int(n), cap, int(deposit_capacity)),
+                    "nmc_adjoint_forward_ex")
+
+    @property
+    def deposit_list_complete(self) -> bool:
+        return bool(self._L.nmc_adjoint_deposit_list_complete(self._h))
 
     def adjoint_backward(self, grad_rd_r=None, grad_absorbed=None):
         """(grad_mua, grad_mus, grad_g) per voxel for the upstream gradients of

@@ -31,7 +31,7 @@ class LinearEngine:
     def reset(self):
         self.rd = self.ab = None
 
-    def adjoint_forward(self, first, n, cap):
+    def adjoint_forward(self, first, n, cap, deposit_capacity=0):
         self.forwards += 1
         self.n = n
         mua, mus, _ = self.props

@@ -8,7 +8,9 @@ trajectories do not depend on it) and must agree to 1e-3 relative; mus and g
 are likelihood-ratio estimates and must agree within 4.5 standard errors of
 the batch means, voxel by voxel and summed.  Two losses: one on Rd(r) alone
 (the detected photons are replayed once) and one on Rd(r) plus the absorbed
-weight of a block of voxels (every photon is replayed twice).
+weight of a block of voxels (every photon is replayed, after its total score
+is summed from the forward's deposit list or, without one, from a first
+replay).
 """
 import time
 
@@ -115,6 +117,31 @@ def test_adjoint_rd_and_fluence_match_crn_finite_differences(gpu, case):
     _crn_check(gpu, case, voxels, _upstream(case[7]), GF.ravel(), B=16, nb=250_000)
 
 
+def test_deposit_list_gives_the_score_replay_gradients(gpu, case):
+    # With the record pass's deposit list a fluence-loss backward sums each
+    # photon's total score from the list instead of replaying it; the
+    # gradients are those of the score replay up to float summation order.
+    # A list whose capacity runs out is dropped and the backward replays.
+    rng = np.random.default_rng(5)
+    G = _upstream(case[7])
+    GF = rng.uniform(0.5, 1.5, case[0].Nx * case[0].Ny * case[0].Nz).astype(np.float32)
+    n = 100_000
+    with _engine(gpu, case) as e:
+        e.adjoint_forward(0, n)
+        assert not e.deposit_list_complete
+        ref = e.adjoint_backward(G, GF)
+        e.adjoint_forward(0, n, deposit_capacity=800 * n)
+        assert e.deposit_list_complete
+        lst = e.adjoint_backward(G, GF)
+        e.adjoint_forward(0, n, deposit_capacity=1000)  # far too small: dropped
+        assert not e.deposit_list_complete
+        small = e.adjoint_backward(G, GF)
+    for a, b, c in zip(ref, lst, small):
+        scale = np.abs(a).max()
+        np.testing.assert_allclose(b, a, rtol=0, atol=1e-5 * scale)
+        np.testing.assert_allclose(c, a, rtol=0, atol=1e-5 * scale)
+
+
 def test_adjoint_is_linear_in_the_upstream_gradient(gpu, case):
     bins = case[7]
     G1 = _upstream(bins)
@@ -201,7 +228,7 @@ def test_autograd_function(gpu, case):
         ((rd * w).sum() + (ab * wf).sum()).backward()
         e.set_voxel_props(mua, mus, g)
         e.reset()
-        e.adjoint_forward(0, n)
+        e.adjoint_forward(0, n, deposit_capacity=600 * n)  # as transport() records by default
         rd_direct = e.tally(abi.TALLY_RD_R) / n
         ab_direct = e.tally(abi.TALLY_F3D) / n
         ga, gs, gg = e.adjoint_backward((w.numpy() / n).astype(np.float32),
@@ -209,7 +236,9 @@ def test_autograd_function(gpu, case):
     np.testing.assert_allclose(rd.detach().numpy(), rd_direct, rtol=1e-6)
     np.testing.assert_allclose(ab.detach().numpy().ravel(), ab_direct, rtol=1e-6)
     for t, ref in ((ta, ga), (ts, gs), (tg, gg)):
-        np.testing.assert_allclose(t.grad.numpy().ravel(), ref, rtol=1e-5, atol=1e-9 * np.abs(ref).max())
+        # the per-photon scores are float sums whose order varies between
+        # runs (atomics), hence the absolute floor
+        np.testing.assert_allclose(t.grad.numpy().ravel(), ref, rtol=1e-5, atol=1e-6 * np.abs(ref).max())
     # the fluence normalisation differentiates through torch
     ta2 = torch.tensor(mua, dtype=torch.float64, requires_grad=True)
     phi = fluence(ab.detach(), ta2, 0.01 ** 3)
@@ -218,28 +247,33 @@ def test_autograd_function(gpu, case):
 
 
 def test_adjoint_costs_at_most_three_forwards(gpu, case):
+    # forward + adjoint against a plain forward of the same photons, best of
+    # three host-timed calls each: for a loss on Rd(r), and for Rd(r) plus the
+    # absorbed weight (the forward keeps its deposit list, so every photon is
+    # replayed once)
     G = _upstream(case[7])
+    GF = np.ones(case[0].Nx ** 3, np.float32)
     n = 2_000_000
+
+    def best(fn):
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
     with _engine(gpu, case) as e:
-        e.run(0, n)  # warm-up
-        e.adjoint_forward(0, n)
-        e.adjoint_backward(G)
-        t0 = time.perf_counter()
-        e.run(0, n)
-        t_fwd = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        e.adjoint_forward(0, n)
-        e.adjoint_backward(G)
-        t_adj = time.perf_counter() - t0
-        GF = np.ones(case[0].Nx ** 3, np.float32)
-        t0 = time.perf_counter()
-        e.adjoint_forward(0, n)
-        e.adjoint_backward(G, GF)
-        t_adj_f = time.perf_counter() - t0
+        fwd = lambda: e.run(0, n)  # noqa: E731
+        adj = lambda: (e.adjoint_forward(0, n), e.adjoint_backward(G))  # noqa: E731
+        adj_f = lambda: (e.adjoint_forward(0, n, deposit_capacity=600 * n), e.adjoint_backward(G, GF))  # noqa: E731
+        fwd(), adj(), adj_f()  # warm-up (and the lists' first allocation)
+        t_fwd, t_adj, t_adj_f = best(fwd), best(adj), best(adj_f)
+        assert e.deposit_list_complete
     print(f"forward {t_fwd * 1e3:.1f} ms; record + backward: Rd {t_adj * 1e3:.1f} ms ({t_adj / t_fwd:.2f}x), "
           f"Rd + absorbed {t_adj_f * 1e3:.1f} ms ({t_adj_f / t_fwd:.2f}x)")
     assert t_adj <= 3.0 * t_fwd
-    assert t_adj_f <= 4.0 * t_fwd  # every photon replayed twice
+    assert t_adj_f <= 3.0 * t_fwd
 
 
 def test_adjoint_satisfies_the_scaling_identity(gpu):
