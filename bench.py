@@ -1047,7 +1047,7 @@ def main():
                     help="skip the extras of the default line (sweep to 1%% SE, adjoint, C1, layered, C5)")
     ap.add_argument("--budget-scale", type=float, default=1.0,
                     help="sweep workload: scale every wavelength's photon budget (profiling on a smaller case)")
-    ap.add_argument("--tune", type=int, default=0,
+    ap.add_argument("--tune", type=int, default=2_000_000,
                     help="autotune the launch shape on this many photons before the warm-up (0: defaults)")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warm-up and timed transport launches (for ncu)")

@@ -184,7 +184,11 @@ typedef struct nmc_ext {
   int32_t block_size;
   int32_t blocks_per_sm;
   double timeout_s;              /* host wait limit per call */
-  uint32_t reserved[8];
+  /* voxel and mcsub kernels: consecutive photons a thread takes from the
+   * work queue at a time, rounded down to a power of two up to 64 (0 or 1:
+   * one); results do not depend on it */
+  uint32_t photons_per_fetch;
+  uint32_t reserved[7];
 } nmc_ext;
 
 /* Totals since nmc_prepare / nmc_reset.  Sums are un-normalised weights. */
@@ -574,8 +578,9 @@ nmc_status nmc_layered_adjoint(int32_t device, const nmc_layered_config* cfg, co
 /* One launch configuration the autotuner timed. */
 typedef struct nmc_tune_entry {
   int32_t block_size, blocks_per_sm;
-  uint32_t flags; /* NMC_FLAG_GLOBAL_TALLIES or 0 */
-  float ms;       /* kernel time of the tuning run */
+  uint32_t flags;             /* NMC_FLAG_GLOBAL_TALLIES or 0 */
+  uint32_t photons_per_fetch; /* photons a thread takes from the queue at a time */
+  float ms;                   /* kernel time of the tuning run */
 } nmc_tune_entry;
 
 typedef struct nmc_tune_result {
@@ -584,13 +589,14 @@ typedef struct nmc_tune_result {
   nmc_tune_entry tried[48];
 } nmc_tune_result;
 #ifdef __cplusplus
-static_assert(sizeof(nmc_tune_result) == 804, "nmc_tune_result layout");
+static_assert(sizeof(nmc_tune_result) == 1004, "nmc_tune_result layout");
 #endif
 
 /* Times the handle's kernel on photons [0, photons) under each candidate
  * launch configuration (block size; resident blocks per SM, i.e. photons in
- * flight per SM; for mcsub, tallies privatised in shared memory or not), keeps
- * the fastest in the handle's nmc_ext (block_size, blocks_per_sm, flags) and
+ * flight per SM; photons a thread takes from the work queue at a time; for
+ * mcsub, tallies privatised in shared memory or not), keeps the fastest in
+ * the handle's nmc_ext (block_size, blocks_per_sm, photons_per_fetch, flags) and
  * clears the tallies.  Results do not depend on the configuration: every
  * photon's stream is a function of its id only.  No reference counterpart
  * (the reference dispatches 1e4 threads in threadgroups of the pipeline's

@@ -145,7 +145,8 @@ class Ext(C.Structure):
         ("block_size", C.c_int32),
         ("blocks_per_sm", C.c_int32),
         ("timeout_s", C.c_double),
-        ("reserved", C.c_uint32 * 8),
+        ("photons_per_fetch", C.c_uint32),
+        ("reserved", C.c_uint32 * 7),
     ]
 
 
@@ -196,7 +197,8 @@ LAY_FIELDS = ("photons", "specular", "Rd", "Rd2", "Tt", "Tt2", "A", "interaction
 class TuneEntry(C.Structure):
     """nmc_tune_entry."""
 
-    _fields_ = [("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("flags", C.c_uint32), ("ms", C.c_float)]
+    _fields_ = [("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("flags", C.c_uint32),
+                ("photons_per_fetch", C.c_uint32), ("ms", C.c_float)]
 
 
 class TuneResult(C.Structure):

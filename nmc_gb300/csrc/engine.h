@@ -65,6 +65,7 @@ struct XyzParams {
   uint32_t flags;
   int fast_math;              // SFU approximations (Math<true>)
   uint32_t step_cap;
+  uint32_t per_fetch;         // photons a thread takes from the queue at a time (>= 1)
   unsigned long long* F3D;
   unsigned long long* Rd2D;
   unsigned int* Det2D;
@@ -129,6 +130,7 @@ struct SubParams {
   int fast_math;
   int skip_F;        // no F(r,z) tally
   int global_tallies;  // F(r,z), J(r) straight to global memory (no shared-memory privatisation)
+  uint32_t per_fetch;  // photons a thread takes from the queue at a time (>= 1)
   unsigned long long* J;  // fixed point 2^-32, BINS+1
   unsigned long long* F;  // (BINS+1)^2
   DevSums* sums;

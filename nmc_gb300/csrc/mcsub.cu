@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
   float x = 0.f, y = 0.f, z = 0.f, ux = 0.f, uy = 0.f, uz = 1.f, W = 0.f, step_u = 1.f;
   float rsp = 0.f, Atot = 0.f, E = 0.f;
   uint32_t nsc = 0, nsub = 0, fate = NMC_FATE_ALIVE, ndet = 0, nev = 0;
-  unsigned long long pidx = 0;
+  unsigned long long pidx = ~0ull;  // the photon; ~0 before the first (its run of queue indices)
   bool alive = false, have = false;
 
   while (true) {
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
           P.trace.recs[pidx] = r;
         }
       }
-      pidx = next_photon(&P.sums->work);
+      pidx = next_photon_run(&P.sums->work, P.per_fetch, pidx);
       if (pidx >= P.n) break;
       have = true;
       const unsigned long long pid = P.first + pidx;

@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
   float gf_i = 0.f;           // adjoint: upstream fluence gradient of voxel i (0 without a fluence loss)
   unsigned int i = 0, slot = 0, nsc = 0, nsub = 0, st = 0;
   unsigned int set = 0, sbase = 0;  // sweep: the photon's set and its table offset
-  unsigned long long pidx = 0;
+  unsigned long long pidx = ~0ull;  // the photon; ~0 before the first (its run of queue indices)
   uint32_t fate = NMC_FATE_ALIVE, ndet = 0, nev = 0;  // trace only
   Deposit dep{0xFFFFFFFFu, 0.f};
   // record pass: the thread's chunk of the deposit list and its fill
@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
           if (idx_ok(pidx, P.n, &P.sums->flags)) P.trace.recs[pidx] = r;
         }
       }
-      pidx = next_photon(&P.sums->work);
+      pidx = next_photon_run(&P.sums->work, P.per_fetch, pidx);
       if (pidx >= P.n) break;
       if (back) {  // only photons with a score contribute
         D = P.adj_D[pidx];

@@ -398,6 +398,19 @@ __device__ __forceinline__ unsigned long long next_photon(unsigned long long* co
   return base + g.thread_rank();
 }
 
+// The same with runs of `per` consecutive photons per thread (per a power of
+// two): a run starts at a multiple of per, so the thread continues its run
+// while the next index is not one; pidx = ~0 means no run yet.
+__device__ __forceinline__ unsigned long long next_photon_run(unsigned long long* counter, unsigned int per,
+                                                              unsigned long long pidx) {
+  if (pidx != ~0ull && ((pidx + 1) & (per - 1)) != 0) return pidx + 1;
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned long long base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(counter, (unsigned long long)g.size() * per);
+  base = g.shfl(base, 0);
+  return base + (unsigned long long)g.thread_rank() * per;
+}
+
 // Sums a per-thread value over the threads of the warp that are here
 // together (any subset), then one atomic per group.
 __device__ __forceinline__ void warp_add_u64(unsigned long long* dst, unsigned long long v) {

@@ -35,6 +35,14 @@ void lattice_split(float zsurf, float dz, int* k, float* f) {
 
 }  // namespace
 
+// Photons a thread takes from the work queue at a time: the largest power
+// of two not above the request, 1 to 64.
+uint32_t fetch_run(uint32_t want) {
+  uint32_t p = 1;
+  while (p < 64 && 2 * p <= want) p *= 2;
+  return p;
+}
+
 bool tissue_usable(const nmc_tissue_params& tp, int t) {
   return std::isfinite(tp.muav[t]) && tp.muav[t] >= 0.f && tp.musv[t] > 0.f && std::isfinite(tp.musv[t]) &&
          std::isfinite(tp.gv[t]) && std::isfinite(tp.gf[t]) && std::isfinite(tp.af[t]) &&
@@ -136,6 +144,7 @@ void fill_xyz(XyzParams& p, const nmc_run_params& rp, const nmc_tissue_params& t
   p.flags = e.flags;
   p.fast_math = (e.flags & NMC_FLAG_PRECISE_MATH) ? 0 : 1;
   p.step_cap = 4000000u;
+  p.per_fetch = fetch_run(e.photons_per_fetch);
   p.rng = rng_params(e, sim);
 }
 
@@ -169,6 +178,7 @@ void fill_sub(SubParams& p, const nmc_run_params& rp, const nmc_tissue_params& t
   p.global_tallies = (e.flags & NMC_FLAG_GLOBAL_TALLIES) ? 1 : 0;
   p.rng = rng_params(e, NMC_SIM_MCSUB);
   p.step_cap = 10000000u;
+  p.per_fetch = fetch_run(e.photons_per_fetch);
 }
 
 }  // namespace nmc

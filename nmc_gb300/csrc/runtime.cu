@@ -823,10 +823,11 @@ nmc_status nmc_autotune(nmc_handle* h, uint64_t photons, nmc_tune_result* out) {
   const nmc_ext saved = h->ext;
   const bool sub = h->sim == NMC_SIM_MCSUB;
   const bool tt = h->sim == NMC_SIM_MCXYZ_TT;
-  auto apply = [&](int block, int bps, uint32_t priv) {
+  auto apply = [&](int block, int bps, uint32_t priv, uint32_t per) {
     h->ext = saved;
     h->ext.block_size = block;
     h->ext.blocks_per_sm = bps;
+    h->ext.photons_per_fetch = per;
     h->ext.flags = (saved.flags & ~(uint32_t)NMC_FLAG_GLOBAL_TALLIES) | priv;
     return sub ? build_sub(h) : build_xyz(h);
   };
@@ -856,17 +857,19 @@ nmc_status nmc_autotune(nmc_handle* h, uint64_t photons, nmc_tune_result* out) {
   // the defaults, run twice (the first also warms the caches)
   const uint32_t priv0 = saved.flags & NMC_FLAG_GLOBAL_TALLIES;
   float ms = 0.f;
-  if ((st = apply(0, 0, priv0)) != NMC_OK || (st = time_run(&ms)) != NMC_OK || (st = time_run(&ms)) != NMC_OK)
+  if ((st = apply(0, 0, priv0, 0)) != NMC_OK || (st = time_run(&ms)) != NMC_OK || (st = time_run(&ms)) != NMC_OK)
     return restore(st);
-  out->fallback = nmc_tune_entry{0, 0, priv0, ms};
+  out->fallback = nmc_tune_entry{0, 0, priv0, 0, ms};
   out->best = out->fallback;
   const std::vector<int> blocks = sub ? std::vector<int>{128, 256, 512} : std::vector<int>{64, 128, 256};
   std::vector<uint32_t> privs{0u};
   if (sub && !(saved.flags & NMC_FLAG_SKIP_FLUENCE) && nmc::mcsub_smem_bytes(saved.sub_bins) <= 200 * 1024)
     privs.push_back((uint32_t)NMC_FLAG_GLOBAL_TALLIES);
+  // block size x resident blocks x privatisation at one photon per fetch,
+  // then the best shape with runs of 2, 4 and 8 photons per fetch
   for (int block : blocks) {
     for (uint32_t priv : privs) {
-      if ((st = apply(block, 0, priv)) != NMC_OK) return restore(st);
+      if ((st = apply(block, 0, priv, 1)) != NMC_OK) return restore(st);
       int maxb = 0;
       if ((st = max_resident(block, &maxb)) != NMC_OK) return restore(st);
       if (maxb < 1) continue;
@@ -875,16 +878,27 @@ nmc_status nmc_autotune(nmc_handle* h, uint64_t photons, nmc_tune_result* out) {
       cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
       for (int bps : cands) {
         if (out->n_tried >= (int)(sizeof out->tried / sizeof out->tried[0])) break;
-        if ((st = apply(block, bps, priv)) != NMC_OK || (st = time_run(&ms)) != NMC_OK) return restore(st);
-        const nmc_tune_entry t{block, bps, priv, ms};
+        if ((st = apply(block, bps, priv, 1)) != NMC_OK || (st = time_run(&ms)) != NMC_OK) return restore(st);
+        const nmc_tune_entry t{block, bps, priv, 1, ms};
         out->tried[out->n_tried++] = t;
         if (ms < out->best.ms) out->best = t;
       }
     }
   }
+  const nmc_tune_entry shape = out->best;
+  for (uint32_t per : {2u, 4u, 8u}) {
+    if (out->n_tried >= (int)(sizeof out->tried / sizeof out->tried[0])) break;
+    if ((st = apply(shape.block_size, shape.blocks_per_sm, shape.flags, per)) != NMC_OK ||
+        (st = time_run(&ms)) != NMC_OK)
+      return restore(st);
+    const nmc_tune_entry t{shape.block_size, shape.blocks_per_sm, shape.flags, per, ms};
+    out->tried[out->n_tried++] = t;
+    if (ms < out->best.ms) out->best = t;
+  }
   h->ext = saved;
   h->ext.block_size = out->best.block_size;
   h->ext.blocks_per_sm = out->best.blocks_per_sm;
+  h->ext.photons_per_fetch = out->best.photons_per_fetch;
   h->ext.flags = (saved.flags & ~(uint32_t)NMC_FLAG_GLOBAL_TALLIES) | out->best.flags;
   st = sub ? build_sub(h) : build_xyz(h);
   if (st != NMC_OK) return st;

@@ -238,10 +238,12 @@ class Engine:
         self._check(self._L.nmc_autotune(self._h, int(photons), C.byref(r)), "nmc_autotune")
 
         def d(t):
-            return {"block_size": t.block_size, "blocks_per_sm": t.blocks_per_sm, "flags": t.flags, "ms": t.ms}
+            return {"block_size": t.block_size, "blocks_per_sm": t.blocks_per_sm, "flags": t.flags,
+                    "photons_per_fetch": t.photons_per_fetch, "ms": t.ms}
 
         self.ext.block_size = r.best.block_size
         self.ext.blocks_per_sm = r.best.blocks_per_sm
+        self.ext.photons_per_fetch = r.best.photons_per_fetch
         self.ext.flags = (self.ext.flags & ~abi.FLAG_GLOBAL_TALLIES) | r.best.flags
         return {"best": d(r.best), "default": d(r.fallback), "tried": [d(r.tried[i]) for i in range(r.n_tried)]}
 

@@ -98,7 +98,7 @@ def test_python_mirrors_of_the_new_structs():
     assert C.sizeof(abi.EfieldSetting) == 24
     assert C.sizeof(abi.Layer) == 20
     assert C.sizeof(abi.LayeredConfig) == 40
-    assert C.sizeof(abi.TuneResult) == 804
+    assert C.sizeof(abi.TuneResult) == 1004
     assert abi.SPECKLE_DTYPE.itemsize == 28
     assert C.sizeof(abi.SweepSet) == 64
 

@@ -20,6 +20,24 @@ def _tallies(e, which):
     return {w: e.tally(w) for w in which}
 
 
+@pytest.mark.parametrize("per", [2, 8])
+def test_photons_per_fetch_keeps_results(gpu, per):
+    # a thread taking runs of consecutive photons from the queue runs the same
+    # photons: every integer tally is equal
+    rp, tp, v, ext = cases.skin_vessel_case(N=48)
+    out = []
+    for p in (1, per):
+        ext.photons_per_fetch = p
+        with gpu.Engine(abi.SIM_MCXYZ, 0, ext) as e:
+            e.prepare_data(rp, tp, v)
+            e.run(7, 30_001)
+            out.append((_tallies(e, (abi.TALLY_F3D, abi.TALLY_RD2D)), e.summary()))
+    for w in (abi.TALLY_F3D, abi.TALLY_RD2D):
+        np.testing.assert_array_equal(out[0][0][w], out[1][0][w])
+    for k in ("photons", "substeps", "scatters", "rd_sum"):
+        assert out[0][1][k] == out[1][1][k], k
+
+
 @pytest.mark.parametrize("kind", ["mcsub", "mcxyz"])
 def test_autotune_keeps_results(gpu, kind):
     if kind == "mcsub":
@@ -36,6 +54,8 @@ def test_autotune_keeps_results(gpu, kind):
         r = e.autotune(50_000)
         print(kind, "default", r["default"], "best", r["best"], "tried", len(r["tried"]))
         assert len(r["tried"]) >= 3
+        # runs of several photons per queue fetch are among the shapes tried
+        assert {t["photons_per_fetch"] for t in r["tried"]} >= {1, 2, 4, 8}
         assert r["best"]["ms"] <= r["default"]["ms"]
         assert e.summary()["photons"] == 0  # tallies cleared
         e.run(0, n)
