@@ -63,11 +63,13 @@ MUFU_PER_EF_SCATTER = 14.0
 # Warp instructions the transport kernel issues per voxel sub-step
 # (smsp__inst_executed.sum / sub-steps of the 1e7-photon ncu capture of this
 # workload), and the SM's issue rate (4 warp instructions per clock).
-WARP_INSTR_PER_SUBSTEP = 3.755e11 / 2.557e10
+WARP_INSTR_PER_SUBSTEP = 359_269_215_517 / 2.5574e10
 ISSUE_PER_SM_CLOCK = 4.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 1e8-photon
-# launch of the transport kernel, from one ncu capture of that launch.
-TRAFFIC_BYTES_1E8 = 72_138_240 + 28_571_801_856
+# launch of the transport kernel: the 1e7-photon capture's bytes times 10
+# (the tally write-back grows with the launch: 2e6 photons wrote 0.57 GB,
+# 1e7 2.86 GB, and a full-size 1e8 capture of the previous build 28.6 GB).
+TRAFFIC_BYTES_1E8 = (71_999_488 + 2_863_494_912) * 10
 HBM_PEAK_FALLBACK_GBS = 6800.0
 
 
@@ -123,7 +125,7 @@ def _issue_estimate(substeps_per_s, clock_lines) -> dict | None:
     peak = sms * ISSUE_PER_SM_CLOCK * mhz * 1e6
     return {"warp_instr_per_substep": WARP_INSTR_PER_SUBSTEP, "achieved_warp_instr_per_s": per_s,
             "peak_warp_instr_per_s": peak, "frac": per_s / peak,
-            "source": "instructions per sub-step from ncu (profiles/mcxyz_skinvessel_1e7_full.txt), "
+            "source": "instructions per sub-step from ncu (profiles/mcxyz_skinvessel_traffic.txt), "
                       "sub-step rate live, SMs x 4 issues per clock at the median sampled SM clock"}
 
 

@@ -35,24 +35,35 @@ __global__ void adjoint_scores_kernel(const AdjEvent* __restrict__ ev, unsigned 
 
 // One thread per chunk of the deposit list: each photon's run of records
 // (from its header to the next header or the chunk's end) adds its
-// sum GF[voxel] * deposit to D[photon] with one atomic.
+// sum GF[voxel] * deposit to D[photon] with one atomic.  A chunk is 2 KB
+// (256 records, 16-byte aligned) read two records at a time.
 __global__ void deposit_scores_kernel(const uint2* __restrict__ pool, const unsigned int* __restrict__ fill,
                                       unsigned int n_chunks, const float* __restrict__ GF, float* __restrict__ D,
                                       unsigned long long n_photons) {
+  static_assert(kDepChunk % 2 == 0, "records are read in pairs");
   for (unsigned int c = blockIdx.x * blockDim.x + threadIdx.x; c < n_chunks; c += gridDim.x * blockDim.x) {
-    const uint2* r = pool + (size_t)c * kDepChunk;
+    const uint4* r = reinterpret_cast<const uint4*>(pool + (size_t)c * kDepChunk);
     const unsigned int n = min(fill[c], kDepChunk);
     unsigned int p = 0xFFFFFFFFu;
     float sum = 0.f;
-    for (unsigned int k = 0; k < n; ++k) {
-      const uint2 x = r[k];
-      if (x.x == 0xFFFFFFFFu) {
+    auto take = [&](unsigned int a, unsigned int b) {
+      if (a == 0xFFFFFFFFu) {
         if (p < n_photons && sum != 0.f) atomicAdd(D + p, sum);
-        p = x.y;
+        p = b;
         sum = 0.f;
       } else {
-        sum = fmaf(__ldg(GF + x.x), __uint_as_float(x.y), sum);
+        sum = fmaf(__ldg(GF + a), __uint_as_float(b), sum);
       }
+    };
+#pragma unroll 4
+    for (unsigned int k = 0; k < n / 2; ++k) {
+      const uint4 x = __ldg(r + k);
+      take(x.x, x.y);
+      take(x.z, x.w);
+    }
+    if (n & 1u) {
+      const uint2 x = pool[(size_t)c * kDepChunk + n - 1];
+      take(x.x, x.y);
     }
     if (p < n_photons && sum != 0.f) atomicAdd(D + p, sum);
   }
