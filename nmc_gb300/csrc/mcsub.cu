@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
   if (threadIdx.x < 6) s_tot[threadIdx.x] = 0ull;
   if (threadIdx.x == 0) s_rd2 = 0.0;
   __syncthreads();
-  const uint32_t k0 = P.rng.k0, k1 = P.rng.k1;
+  const RoundKeys keys{P.rng.rk};  // Philox round keys of the seed
 
   RNG rng;
   float x = 0.f, y = 0.f, z = 0.f, ux = 0.f, uy = 0.f, uz = 1.f, W = 0.f, step_u = 1.f;
@@ -134,10 +134,10 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
         launch_photon<FAST>(P, d, x, y, z, ux, uy, uz, rsp);
       } else {
         rng.init(pid);
-        LaunchDraws d{rng.block(0xFFFFFFFFu, k0, k1), 0};
+        LaunchDraws d{rng.block(0xFFFFFFFFu, keys), 0};
         launch_photon<FAST>(P, d, x, y, z, ux, uy, uz, rsp);
       }
-      step_u = rng.first_step(k0, k1);
+      step_u = rng.first_step(keys);
       W = 1.f - rsp;  // :166-168
       Atot = 0.f;
       E = 0.f;
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
     ++nsub;
     if (P.boundaryflag == 1 && z <= P.zs) {  // ESCAPE (:190-214)
       float uz1;
-      if (rng.fres_u(k0, k1) > rfresnel(P.n1, P.n2, -uz, &uz1)) {
+      if (rng.fres_u(keys) > rfresnel(P.n1, P.n2, -uz, &uz1)) {
         x = fmaf(-s, ux, x);
         y = fmaf(-s, uy, y);
         z = fmaf(-s, uz, z);
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(512) mcsub_kernel(const SubParams P) {
     }
     // ---- SPIN (:243-279), ROULETTE (:289-294), next HOP's draw
     const bool need_roul = W < kTHRESHOLD;
-    const SpinDraws d = spin_draws<TT>(rng, need_roul, k0, k1);
+    const SpinDraws d = spin_draws<TT>(rng, need_roul, keys);
     float costheta;
     if (PHASE == kPhaseTT)
       costheta = tt_sample<FAST>(P.phase, d.a, d.b);

@@ -248,6 +248,14 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
 
   const uint32_t k0 = P.rng.k0;
   uint32_t k1 = P.rng.k1;  // a sweep set s draws from key (k0, k1 + s)
+  // Philox keys: the host's round-key table of (k0, k1), or in a sweep the
+  // photon's set key (k0, k1 + set)
+  auto keys = [&]() {
+    if constexpr (SW)
+      return SeedKeys{k0, k1};
+    else
+      return RoundKeys{P.rng.rk};
+  };
   const bool hard_kill = !(P.flags & NMC_FLAG_NO_HARD_KILL);
   constexpr bool back = MODE == kAdjoint;  // accumulating replay
   constexpr bool score = MODE == kScore;   // score replay: D[photon] = its total score
@@ -380,7 +388,7 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
         launch_photon<TT, FAST>(P, d, x, y, z, ux, uy, uz, W);
       } else {
         rng.init(pid);
-        LaunchDraws d{rng.block(0xFFFFFFFFu, k0, k1), 0};
+        LaunchDraws d{rng.block(0xFFFFFFFFu, keys()), 0};
         launch_photon<TT, FAST>(P, d, x, y, z, ux, uy, uz, W);
       }
       to_lattice(x, P.dx, P.dxmax, kx, fx);
@@ -392,7 +400,7 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
       i = (unsigned int)(iz * NyNx + ix * P.Ny + iy);
       if (!VOX) tiss = idx_ok(i, nvox, &P.sums->flags) ? __ldg(P.V + i) : 0;
       if (ADJ && GF) gf_i = idx_ok(i, nvox, &P.sums->flags) ? __ldg(GF + i) : 0.f;
-      sleft = M::neglog(rng.first_step(k0, k1));  // HOP (:501-502)
+      sleft = M::neglog(rng.first_step(keys()));  // HOP (:501-502)
       hop_end = kRAY_DEPTH + 1;
       Rd_loc = Atot = 0.f;
       nsc = nsub = 0;
@@ -544,20 +552,21 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
         fy = fmaf(s, uy, fy);
         fz = fmaf(s, uz, fz);
         if (!sv) {
-          // the face the step aims at is crossed by exactly ls*|u| (as in FP64)
-          if (ax == 0) {
-            const bool p = ux >= 0.f;
-            kx += p ? 1 : -1;
-            fx = p ? kLS * ux : fminf(fmaf(kLS, ux, P.dx), P.dxmax);
-          } else if (ax == 1) {
-            const bool p = uy >= 0.f;
-            ky += p ? 1 : -1;
-            fy = p ? kLS * uy : fminf(fmaf(kLS, uy, P.dy), P.dymax);
-          } else {
-            const bool p = uz >= 0.f;
-            kz += p ? 1 : -1;
-            fz = p ? kLS * uz : fminf(fmaf(kLS, uz, P.dz), P.dzmax);
-          }
+          // the face the step aims at is crossed by exactly ls*|u| (as in
+          // FP64): one landing for the crossed axis, its operands selected,
+          // so the lanes of a warp crossing different axes stay together
+          const float ua = ax == 0 ? ux : (ax == 1 ? uy : uz);
+          const float da = ax == 0 ? P.dx : (ax == 1 ? P.dy : P.dz);
+          const float dma = ax == 0 ? P.dxmax : (ax == 1 ? P.dymax : P.dzmax);
+          const bool p = ua >= 0.f;
+          const float fa = p ? kLS * ua : fminf(fmaf(kLS, ua, da), dma);
+          const int step = p ? 1 : -1;
+          kx += ax == 0 ? step : 0;
+          ky += ax == 1 ? step : 0;
+          kz += ax == 2 ? step : 0;
+          fx = ax == 0 ? fa : fx;
+          fy = ax == 1 ? fa : fy;
+          fz = ax == 2 ? fa : fz;
         }
         // offsets leave [0, d) only when a point lands on a face (an upper
         // face of the same-voxel end point, a tie between faces)
@@ -635,7 +644,7 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
 
     // ---- SPIN (:688-731 / :1046-1097), ROULETTE (:733-748), next HOP (:501)
     const bool need_roul = W < kTHRESHOLD;
-    const SpinDraws d = spin_draws<TT>(rng, need_roul, k0, k1);
+    const SpinDraws d = spin_draws<TT>(rng, need_roul, keys());
     float costheta;
     if constexpr (VOX) {
       const float4 cv = __ldg(P.vox + i);  // the voxel the photon scatters in

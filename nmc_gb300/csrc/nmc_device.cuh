@@ -45,17 +45,47 @@ __device__ __forceinline__ unsigned long long to_fix(float v) {
 }
 
 // ----------------------------------------------------------------- Philox
-// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).  Round r (0-based)
+// XORs the key words k0 + r W0 and k1 + r W1 into the state.  SeedKeys
+// derives them round by round from the seed words; RoundKeys reads the ten
+// pairs from a table the host filled (RngParams::rk), which a kernel keeps
+// in its parameter block, so every round's XOR takes a constant operand
+// instead of a key addition.  Both give the same numbers.
+constexpr uint32_t kPhiloxW0 = 0x9E3779B9u, kPhiloxW1 = 0xBB67AE85u;
+
+struct SeedKeys {
+  uint32_t k0, k1;
+  __device__ __forceinline__ uint32_t a(int r) const { return k0 + (uint32_t)r * kPhiloxW0; }
+  __device__ __forceinline__ uint32_t b(int r) const { return k1 + (uint32_t)r * kPhiloxW1; }
+};
+
+struct RoundKeys {
+  const uint32_t* rk;  // rk[2r] = k0 + r W0, rk[2r+1] = k1 + r W1
+  __device__ __forceinline__ uint32_t a(int r) const { return rk[2 * r]; }
+  __device__ __forceinline__ uint32_t b(int r) const { return rk[2 * r + 1]; }
+};
+
+template <class KEYS>
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, const KEYS& k) {
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
     const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
     const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
-    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
-    k0 += 0x9E3779B9u;
-    k1 += 0xBB67AE85u;
+    c = make_uint4(hi1 ^ c.y ^ k.a(r), lo1, hi0 ^ c.w ^ k.b(r), lo0);
   }
   return c;
+}
+
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+  return philox4x32_10(c, SeedKeys{k0, k1});
+}
+
+// The round-key table of seed words (k0, k1), as RoundKeys reads it.
+inline void philox_round_keys(uint32_t k0, uint32_t k1, uint32_t rk[20]) {
+  for (int r = 0; r < 10; ++r) {
+    rk[2 * r] = k0 + (uint32_t)r * kPhiloxW0;
+    rk[2 * r + 1] = k1 + (uint32_t)r * kPhiloxW1;
+  }
 }
 
 // 0 < u < 1, u = (2k+1) 2^-24 from the top 23 bits k of x (exact in float).
@@ -95,8 +125,12 @@ struct LaunchDraws {
 template <bool TT>
 struct PhiloxRng {
   uint32_t plo, phi, hop;
+  template <class KEYS>
+  __device__ __forceinline__ uint4 block(uint32_t c2, const KEYS& k) const {
+    return philox4x32_10(make_uint4(plo, phi, c2, kPhiloxTag), k);
+  }
   __device__ __forceinline__ uint4 block(uint32_t c2, uint32_t k0, uint32_t k1) const {
-    return philox4x32_10(make_uint4(plo, phi, c2, kPhiloxTag), k0, k1);
+    return block(c2, SeedKeys{k0, k1});
   }
   __device__ __forceinline__ void init(uint64_t photon) {
     plo = (uint32_t)photon;
@@ -108,25 +142,33 @@ struct PhiloxRng {
     LaunchDraws d{block(0xFFFFFFFFu, k0, k1), 0};
     use(d);
   }
-  __device__ __forceinline__ float first_step(uint32_t k0, uint32_t k1) {
+  template <class KEYS>
+  __device__ __forceinline__ float first_step(const KEYS& k) {
     hop = 0;
-    return u01(block(0u, k0, k1).w);
+    return u01(block(0u, k).w);
   }
-  __device__ __forceinline__ SpinDraws spin_draws(bool need_roul, uint32_t k0, uint32_t k1) {
+  __device__ __forceinline__ float first_step(uint32_t k0, uint32_t k1) { return first_step(SeedKeys{k0, k1}); }
+  template <class KEYS>
+  __device__ __forceinline__ SpinDraws spin_draws(bool need_roul, const KEYS& k) {
     ++hop;
-    const uint4 b = block(hop, k0, k1);
+    const uint4 b = block(hop, k);
     SpinDraws d;
     d.a = u01(b.x);
     d.b = u01(b.y);
     d.c = u01(b.z);
     d.step = u01(b.w);
     d.roul = d.c;
-    if (TT && need_roul) d.roul = u01(block(hop | 0x40000000u, k0, k1).x);
+    if (TT && need_roul) d.roul = u01(block(hop | 0x40000000u, k).x);
     return d;
   }
-  __device__ __forceinline__ float fres_u(uint32_t k0, uint32_t k1) const {
-    return u01(block(hop | 0x40000000u, k0, k1).y);
+  __device__ __forceinline__ SpinDraws spin_draws(bool need_roul, uint32_t k0, uint32_t k1) {
+    return spin_draws(need_roul, SeedKeys{k0, k1});
   }
+  template <class KEYS>
+  __device__ __forceinline__ float fres_u(const KEYS& k) const {
+    return u01(block(hop | 0x40000000u, k).y);
+  }
+  __device__ __forceinline__ float fres_u(uint32_t k0, uint32_t k1) const { return fres_u(SeedKeys{k0, k1}); }
 };
 
 // The reference's generator (helpers.metal:319-371), drawn sequentially in
@@ -196,6 +238,8 @@ struct TausRng {
     return r;
   }
   __device__ __forceinline__ float first_step(uint32_t, uint32_t) { return step_draw(); }
+  template <class KEYS>
+  __device__ __forceinline__ float first_step(const KEYS&) { return step_draw(); }
   template <bool TT>
   __device__ __forceinline__ SpinDraws spin_draws_t(bool need_roul) {
     SpinDraws d;
@@ -208,15 +252,21 @@ struct TausRng {
     return d;
   }
   __device__ __forceinline__ float fres_u(uint32_t, uint32_t) { return next(); }
+  template <class KEYS>
+  __device__ __forceinline__ float fres_u(const KEYS&) { return next(); }
 };
 
 // Uniform access to the two generators from the kernels.
-template <bool TT, class RNG>
-__device__ __forceinline__ SpinDraws spin_draws(RNG& rng, bool need_roul, uint32_t k0, uint32_t k1) {
+template <bool TT, class RNG, class KEYS>
+__device__ __forceinline__ SpinDraws spin_draws(RNG& rng, bool need_roul, const KEYS& k) {
   if constexpr (std::is_same<RNG, TausRng>::value)
     return rng.template spin_draws_t<TT>(need_roul);
   else
-    return rng.spin_draws(need_roul, k0, k1);
+    return rng.spin_draws(need_roul, k);
+}
+template <bool TT, class RNG>
+__device__ __forceinline__ SpinDraws spin_draws(RNG& rng, bool need_roul, uint32_t k0, uint32_t k1) {
+  return spin_draws<TT>(rng, need_roul, SeedKeys{k0, k1});
 }
 
 // ---------------------------------------------------------------- optics
@@ -438,6 +488,7 @@ struct DevSums {
 struct RngParams {
   uint32_t kind;  // NMC_RNG_*
   uint32_t k0, k1;
+  uint32_t rk[20];  // Philox round keys of (k0, k1) (philox_round_keys)
   uint32_t tt_replay;
   uint64_t batch;  // photons_per_dispatch (Taus run/index mapping)
 };

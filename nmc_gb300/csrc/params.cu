@@ -86,6 +86,7 @@ RngParams rng_params(const nmc_ext& e, int sim) {
   r.kind = e.rng;
   r.k0 = (uint32_t)e.seed;
   r.k1 = (uint32_t)(e.seed >> 32);
+  philox_round_keys(r.k0, r.k1, r.rk);
   r.tt_replay = (sim == NMC_SIM_MCXYZ_TT && (e.flags & NMC_FLAG_TT_REPLAY_RUN1)) ? 1u : 0u;
   r.batch = e.photons_per_dispatch;
   return r;
