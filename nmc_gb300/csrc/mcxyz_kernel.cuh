@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
         const float su = s * uz;
         const bool cross = (P.det_state == NMC_DET_REFLECTANCE && su <= rel && uz < 0.f) ||
                            (P.det_state == NMC_DET_TRANSMITTANCE && su >= rel && uz > 0.f);
-        if (cross) {
+        if (__builtin_expect(cross, 0)) {
           const float dl_b = rel / uz;
           if (back) {
             if (sv)
@@ -573,8 +573,8 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
         // (one unsigned compare per axis: a negative offset has the sign bit
         // set and compares above d; -0 and NaN enter, and norm_axis leaves
         // them as they are)
-        if ((__float_as_uint(fx) >= __float_as_uint(P.dx)) | (__float_as_uint(fy) >= __float_as_uint(P.dy)) |
-            (__float_as_uint(fz) >= __float_as_uint(P.dz))) {
+        if (__builtin_expect((__float_as_uint(fx) >= __float_as_uint(P.dx)) | (__float_as_uint(fy) >= __float_as_uint(P.dy)) |
+            (__float_as_uint(fz) >= __float_as_uint(P.dz)), 0)) {
           norm_axis(kx, fx, P.dx, P.dxmax);
           norm_axis(ky, fy, P.dy, P.dymax);
           norm_axis(kz, fz, P.dz, P.dzmax);
@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
       int iz = kz;
       const bool inside = (unsigned)ix < (unsigned)P.Nx && (unsigned)iy < (unsigned)P.Ny &&
                           (unsigned)iz < (unsigned)P.Nz;
-      if (!inside) {  // C truncation toward zero outside the grid
+      if (__builtin_expect(!inside, 0)) {  // C truncation toward zero outside the grid
         ix = lookup_index(kx, fx, P.hx, P.ox, P.hdx);
         iy = lookup_index(ky, fy, P.hy, P.oy, P.hdy);
         iz = lookup_index(kz, fz, 0, 0, 0.f);
@@ -612,7 +612,7 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
         }
         st |= kBflag;
       }
-      if (!inside) {  // boundary modes (:646-672)
+      if (__builtin_expect(!inside, 0)) {  // boundary modes (:646-672)
         const bool xo = (unsigned)ix >= (unsigned)P.Nx, yo = (unsigned)iy >= (unsigned)P.Ny;
         const bool zlo = iz < 0, zhi = iz >= P.Nz;
         ix = min(max(ix, 0), P.Nx - 1);
@@ -635,7 +635,7 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
       if (!VOX) tiss = idx_ok(i, nvox, &P.sums->flags) ? __ldg(P.V + i) : 0;
       if (ADJ && GF) gf_i = idx_ok(i, nvox, &P.sums->flags) ? __ldg(GF + i) : 0.f;
     }
-    if (nsub >= P.step_cap) {  // device-side cap: not a reference behaviour
+    if (__builtin_expect(nsub >= P.step_cap, 0)) {  // device-side cap: not a reference behaviour
       kill(NMC_FATE_STEPCAP);
       atomicOr(&P.sums->flags, (unsigned int)NMC_DEVFLAG_STEPCAP);
       continue;
@@ -663,13 +663,13 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
     }
     spin<FAST>(costheta, TT ? d.c : d.b, ux, uy, uz);
     ++nsc;
-    if (need_roul) {
+    if (__builtin_expect(need_roul, 0)) {
       if (d.roul <= kCHANCE)
         W /= kCHANCE;
       else
         kill(NMC_FATE_ROULETTE);
     }
-    if (hard_kill && (W < kMIN_VALUE || (int)nsc > kMAX_SCATT))
+    if (__builtin_expect(hard_kill && (W < kMIN_VALUE || (int)nsc > kMAX_SCATT), 0))
       kill(W < kMIN_VALUE ? NMC_FATE_MINWEIGHT : NMC_FATE_MAXSCATT);
     if (TRACE && nev < P.trace.k_events) {
       if (idx_ok(pidx, P.n, &P.sums->flags)) P.trace.events[pidx * P.trace.k_events + nev] =

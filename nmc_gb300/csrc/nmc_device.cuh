@@ -359,12 +359,14 @@ struct Math {
   }
 };
 
+// The general form is evaluated for every mode and the isotropic and
+// straight-ahead modes select over it (for g = 0 it is NaN, 0 x inf), so a
+// warp whose lanes sit in tissues of different modes takes no branch.
 template <bool FAST>
 __device__ __forceinline__ float hg_sample(const PhaseConst& p, float u) {
-  if (p.hg_mode == 1) return 2.f * u - 1.f;
-  if (p.hg_mode == 2) return 1.f;
   const float t = Math<FAST>::div(p.hg_a, fmaf(p.hg_c, u, p.hg_b));
-  return fmaf(-t, t, p.hg_d) * p.hg_e;
+  const float c = fmaf(-t, t, p.hg_d) * p.hg_e;
+  return p.hg_mode == 1 ? 2.f * u - 1.f : (p.hg_mode == 2 ? 1.f : c);
 }
 
 // Two-term sample from the branch choice and the sample uniform.
@@ -394,11 +396,11 @@ __device__ __forceinline__ void spin(float costheta, float upsi, float& ux, floa
   float sinpsi, cospsi;
   Math<FAST>::sincos2pi(upsi, &sinpsi, &cospsi);
   const float auz = fabsf(uz);
-  if (auz >= 1.f) {  // 1 - |uz| <= 1e-12 in FP32
+  if (__builtin_expect(auz >= 1.f, 0)) {  // 1 - |uz| <= 1e-12 in FP32
     ux = sintheta * cospsi;
     uy = sintheta * sinpsi;
     uz = uz >= 0.f ? costheta : -costheta;
-  } else if (1.f - auz < 1e-5f) {
+  } else if (__builtin_expect(1.f - auz < 1e-5f, 0)) {
     const double dz = uz, temp = sqrt(1.0 - dz * dz);
     const double st = sintheta, ct = costheta, cp = cospsi, sp = sinpsi;
     double nx = st * (ux * dz * cp - uy * sp) / temp + ux * ct;
