@@ -63,13 +63,13 @@ MUFU_PER_EF_SCATTER = 14.0
 # Warp instructions the transport kernel issues per voxel sub-step
 # (smsp__inst_executed.sum / sub-steps of the 1e7-photon ncu capture of this
 # workload), and the SM's issue rate (4 warp instructions per clock).
-WARP_INSTR_PER_SUBSTEP = 359_269_215_517 / 2.5574e10
+WARP_INSTR_PER_SUBSTEP = 326_699_125_741 / 2.5583e10
 ISSUE_PER_SM_CLOCK = 4.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 1e8-photon
 # launch of the transport kernel: the 1e7-photon capture's bytes times 10
 # (the tally write-back grows with the launch: 2e6 photons wrote 0.57 GB,
-# 1e7 2.86 GB, and a full-size 1e8 capture of the previous build 28.6 GB).
-TRAFFIC_BYTES_1E8 = (71_999_488 + 2_863_494_912) * 10
+# 1e7 2.86 GB, and a full-size 1e8 capture of an earlier build 28.6 GB).
+TRAFFIC_BYTES_1E8 = (72_335_360 + 2_862_277_376) * 10
 HBM_PEAK_FALLBACK_GBS = 6800.0
 
 

@@ -80,6 +80,7 @@ struct LayParams {
   double* sums;  // NMC_LAY_FIELDS
   unsigned long long first, n;
   uint32_t k0, k1;
+  uint32_t rk[20];  // Philox round keys of (k0, k1)
   unsigned long long* work;
   unsigned int* flags;
   uint32_t step_cap;
@@ -133,7 +134,7 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
       tr.init_photon(pid, P.batch, false, false);
       tr.next();  // the launch draw (radius 0: the beam stays on the axis)
     } else {
-      r = philox4x32_10(make_uint4(c0, c1, 0u, kLayTag), P.k0, P.k1);
+      r = philox4x32_10(make_uint4(c0, c1, 0u, kLayTag), RoundKeys{P.rk});
     }
     while (alive) {
       const LayDev& Ly = s_lay[L];
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
         float uzt = 0.f;
         const float R = rfresnel(Ly.n, nt, fabsf(uz), &uzt);
         const float uf =
-            REF ? tr.next() : u01(philox4x32_10(make_uint4(c0, c1, ev | 0x80000000u, kLayTag), P.k0, P.k1).x);
+            REF ? tr.next() : u01(philox4x32_10(make_uint4(c0, c1, ev | 0x80000000u, kLayTag), RoundKeys{P.rk}).x);
         ++ev;
         if (uf <= R) {
           uz = -uz;  // reflected
@@ -225,7 +226,7 @@ __global__ void __launch_bounds__(256) layered_kernel(const LayParams P) {
         atomicOr(P.flags, (unsigned int)NMC_DEVFLAG_STEPCAP);
         alive = false;
       }
-      if (!REF) r = philox4x32_10(make_uint4(c0, c1, hop, kLayTag), P.k0, P.k1);
+      if (!REF) r = philox4x32_10(make_uint4(c0, c1, hop, kLayTag), RoundKeys{P.rk});
     }
     if (dep_w > 0.f && idx_ok(dep_l, (unsigned)P.nl, P.flags)) atomicAdd(s_al + dep_l, to_fix(dep_w));
     atomicAdd(&s_sum[NMC_LAY_PHOTONS], 1.0);
@@ -367,6 +368,7 @@ nmc_status layered_impl(int32_t device, const nmc_layered_config* cfg, const nmc
   P.n = photons;
   P.k0 = (uint32_t)c.seed;
   P.k1 = (uint32_t)(c.seed >> 32);
+  philox_round_keys(P.k0, P.k1, P.rk);
   P.work = dwork;
   P.flags = (unsigned int*)(dwork + 1);
   P.step_cap = 20000000u;
