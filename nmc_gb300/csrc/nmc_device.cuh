@@ -396,20 +396,23 @@ __device__ __forceinline__ void spin(float costheta, float upsi, float& ux, floa
   float sinpsi, cospsi;
   Math<FAST>::sincos2pi(upsi, &sinpsi, &cospsi);
   const float auz = fabsf(uz);
-  if (__builtin_expect(auz >= 1.f, 0)) {  // 1 - |uz| <= 1e-12 in FP32
-    ux = sintheta * cospsi;
-    uy = sintheta * sinpsi;
-    uz = uz >= 0.f ? costheta : -costheta;
-  } else if (__builtin_expect(1.f - auz < 1e-5f, 0)) {
-    const double dz = uz, temp = sqrt(1.0 - dz * dz);
-    const double st = sintheta, ct = costheta, cp = cospsi, sp = sinpsi;
-    double nx = st * (ux * dz * cp - uy * sp) / temp + ux * ct;
-    double ny = st * (uy * dz * cp + ux * sp) / temp + uy * ct;
-    double nz = -st * cp * temp + dz * ct;
-    const double inv = 1.0 / sqrt(nx * nx + ny * ny + nz * nz);
-    ux = (float)(nx * inv);
-    uy = (float)(ny * inv);
-    uz = (float)(nz * inv);
+  // one test on the common path; the two near-vertical cases behind it
+  if (__builtin_expect(1.f - auz < 1e-5f, 0)) {
+    if (auz >= 1.f) {  // 1 - |uz| <= 1e-12 in FP32
+      ux = sintheta * cospsi;
+      uy = sintheta * sinpsi;
+      uz = uz >= 0.f ? costheta : -costheta;
+    } else {
+      const double dz = uz, temp = sqrt(1.0 - dz * dz);
+      const double st = sintheta, ct = costheta, cp = cospsi, sp = sinpsi;
+      double nx = st * (ux * dz * cp - uy * sp) / temp + ux * ct;
+      double ny = st * (uy * dz * cp + ux * sp) / temp + uy * ct;
+      double nz = -st * cp * temp + dz * ct;
+      const double inv = 1.0 / sqrt(nx * nx + ny * ny + nz * nz);
+      ux = (float)(nx * inv);
+      uy = (float)(ny * inv);
+      uz = (float)(nz * inv);
+    }
   } else {
     const float temp2 = fmaf(-uz, uz, 1.f);
     const float itemp = rsqrtf(temp2);
