@@ -473,7 +473,6 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
       }
     }
     sleft = sv ? 0.f : sleft - s * c.y;
-    if (sleft <= kLS) sleft = 0.f;
     {
       bool moved = false;
       if (!TT && !sv) {  // surface detection (:556-637)
@@ -490,7 +489,6 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
               st |= kFixed;  // the rest of this hop is a fixed length
           }
           sleft = (s - dl_b) * c.y;
-          if (sleft <= kLS) sleft = 0.f;
           fx = fmaf(dl_b, ux, fx);
           fy = fmaf(dl_b, uy, fy);
           norm_axis(kx, fx, P.dx, P.dxmax);
@@ -640,7 +638,10 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
       atomicOr(&P.sums->flags, (unsigned int)NMC_DEVFLAG_STEPCAP);
       continue;
     }
-    if (nsub < hop_end && sleft > 0.f) continue;  // at most RAY_DEPTH crossings per hop (:685)
+    // the hop goes on while more than ls of it is left (the reference
+    // zeroes sleft <= ls, :554, :571, and loops while sleft > 0, :685),
+    // at most RAY_DEPTH crossings
+    if (nsub < hop_end && sleft > kLS) continue;
 
     // ---- SPIN (:688-731 / :1046-1097), ROULETTE (:733-748), next HOP (:501)
     const bool need_roul = W < kTHRESHOLD;
@@ -663,14 +664,17 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
     }
     spin<FAST>(costheta, TT ? d.c : d.b, ux, uy, uz);
     ++nsc;
-    if (__builtin_expect(need_roul, 0)) {
-      if (d.roul <= kCHANCE)
-        W /= kCHANCE;
-      else
-        kill(NMC_FATE_ROULETTE);
+    // W < MIN_VALUE implies W < THRESHOLD: one rare test covers both kills
+    if (__builtin_expect(need_roul || (hard_kill && (int)nsc > kMAX_SCATT), 0)) {
+      if (need_roul) {
+        if (d.roul <= kCHANCE)
+          W /= kCHANCE;
+        else
+          kill(NMC_FATE_ROULETTE);
+      }
+      if (hard_kill && (W < kMIN_VALUE || (int)nsc > kMAX_SCATT))
+        kill(W < kMIN_VALUE ? NMC_FATE_MINWEIGHT : NMC_FATE_MAXSCATT);
     }
-    if (__builtin_expect(hard_kill && (W < kMIN_VALUE || (int)nsc > kMAX_SCATT), 0))
-      kill(W < kMIN_VALUE ? NMC_FATE_MINWEIGHT : NMC_FATE_MAXSCATT);
     if (TRACE && nev < P.trace.k_events) {
       if (idx_ok(pidx, P.n, &P.sums->flags)) P.trace.events[pidx * P.trace.k_events + nev] =
           make_float4((float)kx * P.dx + fx, (float)ky * P.dy + fy, (float)kz * P.dz + fz, W);
