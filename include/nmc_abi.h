@@ -162,7 +162,18 @@ enum {
   NMC_FLAG_LAYERED_REF_STREAMS = 1u << 5,
   /* Layered runs: isotropic scattering, which is what MCSubKernel samples
    * (kernels.metal:252 overwrites its Henyey-Greenstein cos theta). */
-  NMC_FLAG_LAYERED_ISOTROPIC = 1u << 6
+  NMC_FLAG_LAYERED_ISOTROPIC = 1u << 6,
+  /* Voxel handles: leave the L2 cache's persisting set-aside alone.  By
+   * default nmc_prepare marks the handle's u64 fluence tally (8 bytes per
+   * voxel) as persisting in L2 on the handle's stream, and raises the
+   * device's persisting set-aside (cudaLimitPersistingL2CacheSize, a setting
+   * of this process's context) to that size, capped by the device, while
+   * the handle lives; nmc_destroy puts the previous value back.  Without it
+   * the L2 writes the tally's lines back to DRAM under the transport's
+   * atomics (about 29 GB per 1e8 photons on a 200^3 grid); with it the
+   * transport's DRAM traffic is the map plus one touch of the tally.  Pass
+   * this flag when the application manages L2 persistence itself. */
+  NMC_FLAG_NO_L2_PERSIST = 1u << 7
 };
 
 typedef struct nmc_ext {

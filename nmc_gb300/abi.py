@@ -44,6 +44,7 @@ FLAG_SKIP_FLUENCE = 1 << 3
 FLAG_GLOBAL_TALLIES = 1 << 4
 FLAG_LAYERED_REF_STREAMS = 1 << 5
 FLAG_LAYERED_ISOTROPIC = 1 << 6
+FLAG_NO_L2_PERSIST = 1 << 7
 
 FATE_ALIVE, FATE_ESCAPED, FATE_ROULETTE, FATE_MINWEIGHT, FATE_MAXSCATT, FATE_BOUNDARY, FATE_STEPCAP = range(7)
 

@@ -64,6 +64,9 @@ struct nmc_handle {
   unsigned long long* d_J = nullptr;
   unsigned long long* d_F = nullptr;
   size_t nvox = 0, n2d = 0, nslots = 0, nJ = 0, nF = 0;
+  // the persisting L2 set-aside this handle raised, and the value it found
+  bool l2_raised = false;
+  size_t l2_prev = 0;
   // Fixed-point tallies are folded into FP64 carries before they could wrap:
   // a photon adds at most about one weight unit (2^32 fixed-point units) to a
   // bin, so 2^31 photons between folds keep every u64 word below 2^63 and
@@ -136,7 +139,53 @@ void dfree(T*& p) {
   p = nullptr;
 }
 
+// Marks [base, base + bytes) as persisting in L2 for the handle's stream and
+// raises the context's persisting set-aside to cover it (capped by the
+// device); the u64 fluence tally then stays in L2 under the atomics instead
+// of being written back and re-fetched.  A hint only: a device or driver
+// that refuses it leaves the run as it was.
+void keep_in_l2(nmc_handle* h, void* base, size_t bytes) {
+  if (h->ext.flags & NMC_FLAG_NO_L2_PERSIST) return;
+  int max_persist = 0, max_window = 0;
+  if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, h->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, h->device) != cudaSuccess ||
+      max_persist <= 0 || max_window <= 0) {
+    cudaGetLastError();
+    return;
+  }
+  const size_t window = std::min(bytes, (size_t)max_window);
+  const size_t want = std::min(window, (size_t)max_persist);
+  size_t cur = 0;
+  if (cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  if (cur < want && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) == cudaSuccess) {
+    if (!h->l2_raised) h->l2_prev = cur;
+    h->l2_raised = true;
+    cur = want;
+  }
+  cudaStreamAttrValue a{};
+  a.accessPolicyWindow.base_ptr = base;
+  a.accessPolicyWindow.num_bytes = window;
+  a.accessPolicyWindow.hitRatio = std::min(1.0f, (float)cur / (float)window);
+  a.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+  a.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+  cudaStreamSetAttribute(h->stream, cudaStreamAttributeAccessPolicyWindow, &a);
+  cudaGetLastError();
+}
+
+// Clears the stream's window (before the tally it covers is freed).
+void release_l2_window(nmc_handle* h) {
+  if (!h->stream) return;
+  cudaStreamAttrValue a{};
+  a.accessPolicyWindow.num_bytes = 0;
+  cudaStreamSetAttribute(h->stream, cudaStreamAttributeAccessPolicyWindow, &a);
+  cudaGetLastError();
+}
+
 void free_buffers(nmc_handle* h) {
+  release_l2_window(h);
   dfree(h->d_V);
   dfree(h->d_F3D);
   dfree(h->d_Rd2D);
@@ -674,6 +723,7 @@ nmc_status nmc_prepare(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue
     NMC_CUDA(h, cudaMalloc((void**)&h->d_V, h->nvox));
     NMC_CUDA(h, cudaMemcpyAsync(h->d_V, v, h->nvox, cudaMemcpyHostToDevice, h->stream));
     NMC_CUDA(h, cudaMalloc((void**)&h->d_F3D, h->nvox * 8));
+    keep_in_l2(h, h->d_F3D, h->nvox * 8);
     NMC_CUDA(h, cudaMalloc((void**)&h->d_Rd2D, h->n2d * 8));
     NMC_CUDA(h, cudaMalloc((void**)&h->d_Det, h->n2d * 4));
     NMC_CUDA(h, cudaMalloc((void**)&h->d_slots, h->nslots * 8));
@@ -1501,6 +1551,7 @@ void nmc_destroy(nmc_handle* h) {
     cudaEventDestroy(p.b);
   }
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->l2_raised) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, h->l2_prev);
   delete h;
 }
 

@@ -188,3 +188,20 @@ def test_current_device_is_kept(gpu):
     for f in ("photons", "substeps", "S", "A", "E", "rd_sum"):
         assert a[0][f] == b[0][f], f
     np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_l2_persisting_window_keeps_results(gpu):
+    # the fluence tally kept in L2 (the default) or left to the normal policy
+    # (NMC_FLAG_NO_L2_PERSIST) is a cache hint only: every tally is equal
+    rp, tp, v, ext = cases.skin_vessel_case(N=64)
+    out = []
+    for flags in (ext.flags, ext.flags | abi.FLAG_NO_L2_PERSIST):
+        ext.flags = flags
+        with gpu.Engine(abi.SIM_MCXYZ, 0, ext) as e:
+            e.prepare_data(rp, tp, v)
+            e.run(3, 40_000)
+            out.append((_tallies(e, (abi.TALLY_F3D, abi.TALLY_RD2D, abi.TALLY_DETPHOT2D)), e.summary()))
+    for w in (abi.TALLY_F3D, abi.TALLY_RD2D, abi.TALLY_DETPHOT2D):
+        np.testing.assert_array_equal(out[0][0][w], out[1][0][w])
+    for k in ("photons", "substeps", "scatters", "rd_sum"):
+        assert out[0][1][k] == out[1][1][k], k
