@@ -63,13 +63,14 @@ MUFU_PER_EF_SCATTER = 14.0
 # Warp instructions the transport kernel issues per voxel sub-step
 # (smsp__inst_executed.sum / sub-steps of the 1e7-photon ncu capture of this
 # workload), and the SM's issue rate (4 warp instructions per clock).
-WARP_INSTR_PER_SUBSTEP = 326_699_125_741 / 2.5583e10
+WARP_INSTR_PER_SUBSTEP = 319_371_341_306 / 2.5583e10
 ISSUE_PER_SM_CLOCK = 4.0
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 1e8-photon
-# launch of the transport kernel: the 1e7-photon capture's bytes times 10
-# (the tally write-back grows with the launch: 2e6 photons wrote 0.57 GB,
-# 1e7 2.86 GB, and a full-size 1e8 capture of an earlier build 28.6 GB).
-TRAFFIC_BYTES_1E8 = (72_335_360 + 2_862_277_376) * 10
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the transport kernel on this workload.  With the fluence tally persisting in
+# L2 they are the first touch of the 8 MB map and the 64 MB tally, whatever
+# the photon count (1e7 photons: 72.2 MB read, 17 KB written); before it, the
+# L2 wrote tally lines back under the atomics, ~2.86 GB per 1e7 photons.
+TRAFFIC_BYTES_PER_LAUNCH = 72_228_864 + 16_896
 HBM_PEAK_FALLBACK_GBS = 6800.0
 
 
@@ -296,7 +297,7 @@ def run_ours(args) -> dict:
     kernel_s = kernel_ms * 1e-3
     achieved = substeps * OPS_PER_SUBSTEP / kernel_s / 1e12 if kernel_s > 0 else None
     peak = ffma / 1e12
-    traffic = TRAFFIC_BYTES_1E8 * P / 1e8  # per launch; writes grow with the launch's duration
+    traffic = TRAFFIC_BYTES_PER_LAUNCH  # per launch: first touches of the map and the L2-resident tally
     try:
         hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
         hbm_src = "measured"
