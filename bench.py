@@ -65,12 +65,13 @@ MUFU_PER_EF_SCATTER = 14.0
 # workload), and the SM's issue rate (4 warp instructions per clock).
 WARP_INSTR_PER_SUBSTEP = 319_371_341_306 / 2.5583e10
 ISSUE_PER_SM_CLOCK = 4.0
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
-# the transport kernel on this workload.  With the fluence tally persisting in
-# L2 they are the first touch of the 8 MB map and the 64 MB tally, whatever
-# the photon count (1e7 photons: 72.2 MB read, 17 KB written); before it, the
-# L2 wrote tally lines back under the atomics, ~2.86 GB per 1e7 photons.
-TRAFFIC_BYTES_PER_LAUNCH = 72_228_864 + 16_896
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 1e8-photon
+# launch of the transport kernel on this workload, captured on that launch
+# (one ncu pass): 72.10 MB read, 121 KB written.  With the fluence tally
+# persisting in L2 they are the first touch of the 8 MB map and the 64 MB
+# tally; before it, the L2 wrote tally lines back under the atomics, about
+# 29 GB per launch.
+TRAFFIC_BYTES_PER_LAUNCH = 72_100_000 + 121_340
 HBM_PEAK_FALLBACK_GBS = 6800.0
 
 
