@@ -205,3 +205,52 @@ def test_l2_persisting_window_keeps_results(gpu):
         np.testing.assert_array_equal(out[0][0][w], out[1][0][w])
     for k in ("photons", "substeps", "scatters", "rd_sum"):
         assert out[0][1][k] == out[1][1][k], k
+
+
+def _cudart():
+    """The CUDA runtime library, through ctypes, to read the context's limits
+    from outside the engine (the engine links its own copy; both use the
+    device's primary context)."""
+    import ctypes
+    import glob
+    import os
+
+    home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    for path in sorted(glob.glob(os.path.join(home, "lib64", "libcudart.so*"))) + ["libcudart.so"]:
+        try:
+            return ctypes.CDLL(path)
+        except OSError:
+            continue
+    return None
+
+
+def test_l2_set_aside_restored_on_destroy(gpu):
+    # the handle raises the context's persisting-L2 set-aside while it lives
+    # and puts back the value it found when it is destroyed
+    import ctypes
+
+    rt = _cudart()
+    if rt is None:
+        pytest.skip("no CUDA runtime library to read the limit with")
+    persisting_l2 = 0x06  # cudaLimitPersistingL2CacheSize
+
+    def limit():
+        v = ctypes.c_size_t(0)
+        assert rt.cudaDeviceGetLimit(ctypes.byref(v), persisting_l2) == 0
+        return v.value
+
+    # a 160^3 grid: its 33 MB tally is above the set-aside a context starts
+    # with on GB300 (24 MB), so the handle has to raise it
+    rp, tp, v, ext = cases.skin_vessel_case(N=160)
+    before = limit()
+    with gpu.Engine(abi.SIM_MCXYZ, 0, ext) as e:
+        e.prepare_data(rp, tp, v)
+        during = limit()
+        e.run(0, 10_000)
+    after = limit()
+    maxp = ctypes.c_int(0)
+    assert rt.cudaDeviceGetAttribute(ctypes.byref(maxp), 108, 0) == 0  # cudaDevAttrMaxPersistingL2CacheSize
+    needed = min(160 ** 3 * 8, maxp.value)  # the u64 fluence tally of the grid, capped by the device
+    print("persisting L2 set-aside before / during / after:", before, during, after, "needed", needed)
+    assert during >= max(before, needed)  # the driver may round the set-aside up
+    assert after == before
