@@ -232,6 +232,13 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
   constexpr bool VOX = MODE == kVoxel || MODE == kAdjoint || MODE == kRecord || MODE == kScore;
   constexpr bool ADJ = MODE == kAdjoint || MODE == kScore;  // replays
   constexpr bool REC = MODE == kRecord;
+  // Tissue-map kernels of the one-term model flush the merged deposit where
+  // a crossing changes the voxel index, instead of testing the index at every
+  // deposit: their boundary flag, once cleared, stays cleared, so the next
+  // deposit after such a crossing always goes to the new index and the
+  // deposits merge into the same groups (same u64 sums).  The two-term
+  // kernel sets the flag again at every crossing and keeps the test.
+  constexpr bool DEPX = MODE == kTissue && !TT;
   __shared__ float4 s_core[NMC_NTISS];
   __shared__ PhaseConst s_ph[NMC_NTISS];
   __shared__ unsigned long long s_tot[5];  // photons, substeps, scatters, A, rd
@@ -409,7 +416,7 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
         ndet = nev = 0;
       }
       st = kAlive | kBflag | kSurf | kHave;
-      dep.idx = 0xFFFFFFFFu;
+      dep.idx = DEPX ? i : 0xFFFFFFFFu;
       dep.acc = 0.f;
       adj.idx = 0xFFFFFFFFu;
     }
@@ -467,6 +474,8 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
           D -= e_dep;
           Dabs += fabsf(e_dep);
         }
+      } else if (DEPX) {
+        if (st & kBflag) dep.acc += absorb;
       } else if (!SW && (st & kBflag)) {
         if (REC && i != dep.idx) dl_deposit();
         dep.add(P.F3D, i, absorb, nvox, &P.sums->flags);
@@ -630,6 +639,10 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
         }
       }
       i = (unsigned int)(iz * NyNx + ix * P.Ny + iy);  // :675-679
+      if (DEPX && i != dep.idx) {
+        dep.flush(P.F3D, nvox, &P.sums->flags);
+        dep.idx = i;
+      }
       if (!VOX) tiss = idx_ok(i, nvox, &P.sums->flags) ? __ldg(P.V + i) : 0;
       if (ADJ && GF) gf_i = idx_ok(i, nvox, &P.sums->flags) ? __ldg(GF + i) : 0.f;
     }
