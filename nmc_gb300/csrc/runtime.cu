@@ -184,16 +184,10 @@ void release_l2_window(nmc_handle* h) {
   cudaGetLastError();
 }
 
-void free_buffers(nmc_handle* h) {
-  release_l2_window(h);
-  dfree(h->d_V);
-  dfree(h->d_F3D);
-  dfree(h->d_Rd2D);
-  dfree(h->d_Det);
-  dfree(h->d_slots);
-  dfree(h->d_J);
-  dfree(h->d_F);
-  dfree(h->d_stage);
+// Everything a prepared handle may have grown beyond its map, its tallies
+// and their staging: per-voxel properties, the radial tally, the adjoint's
+// lists, FP64 carries, scratch and the captured reduction graphs.
+void free_extras(nmc_handle* h) {
   dfree(h->d_vox);
   dfree(h->d_rdr);
   dfree(h->d_ev);
@@ -215,13 +209,26 @@ void free_buffers(nmc_handle* h) {
   h->since_fold = 0;
   for (ReduceGraph& g : h->graphs) cudaGraphExecDestroy(g.exec);
   h->graphs.clear();
-  if (h->h_stage) cudaFreeHost(h->h_stage);
-  h->h_stage = nullptr;
-  h->nvox = h->n2d = h->nslots = h->nJ = h->nF = h->stage_elems = 0;
   h->voxel_mode = false;
   h->rd_bins = 0;
   h->ev_cap = 0;
   h->adj_ready = false;
+}
+
+void free_buffers(nmc_handle* h) {
+  release_l2_window(h);
+  free_extras(h);
+  dfree(h->d_V);
+  dfree(h->d_F3D);
+  dfree(h->d_Rd2D);
+  dfree(h->d_Det);
+  dfree(h->d_slots);
+  dfree(h->d_J);
+  dfree(h->d_F);
+  dfree(h->d_stage);
+  if (h->h_stage) cudaFreeHost(h->h_stage);
+  h->h_stage = nullptr;
+  h->nvox = h->n2d = h->nslots = h->nJ = h->nF = h->stage_elems = 0;
 }
 
 bool finite_nonneg(float v) { return std::isfinite(v) && v >= 0.f; }
@@ -707,6 +714,21 @@ nmc_status nmc_prepare(nmc_handle* h, const nmc_run_params* rp, const nmc_tissue
   if (st != NMC_OK) return st;
   st = sync_all(h);
   if (st != NMC_OK && st != NMC_ESTEPCAP) return st;
+  // A voxel handle prepared again for a grid of the same size keeps its map,
+  // tally and staging buffers (no cudaFree, which waits for the whole
+  // device, and no pinned re-allocation); the rest is released as below.
+  if (h->prepared && h->sim != NMC_SIM_MCSUB && h->nvox == (size_t)rp->Nx * rp->Ny * rp->Nz &&
+      h->n2d == (size_t)rp->Nx * rp->Ny && h->nslots == h->ext.photons_per_dispatch) {
+    free_extras(h);
+    h->prepared = false;
+    h->rp = *rp;
+    h->tp = *tp;
+    NMC_CUDA(h, cudaMemcpyAsync(h->d_V, v, h->nvox, cudaMemcpyHostToDevice, h->stream));
+    h->prepared = true;
+    st = nmc_reset(h);
+    if (st != NMC_OK) return st;
+    return build_xyz(h);
+  }
   free_buffers(h);
   h->prepared = false;
   h->rp = *rp;

@@ -254,3 +254,31 @@ def test_l2_set_aside_restored_on_destroy(gpu):
     print("persisting L2 set-aside before / during / after:", before, during, after, "needed", needed)
     assert during >= max(before, needed)  # the driver may round the set-aside up
     assert after == before
+
+
+def test_prepare_again_for_a_same_size_grid_equals_a_fresh_handle(gpu):
+    # a voxel handle prepared again for a grid of the same size keeps its
+    # buffers; its results are a fresh handle's, and what the first
+    # preparation grew (per-voxel properties, a radial tally) is gone
+    rp, tp, v, ext = cases.skin_vessel_case(N=48)
+    v2 = np.ascontiguousarray(v.reshape(48, 48, 48)[::-1, :, :].reshape(-1))  # the map upside down
+    which = (abi.TALLY_F3D, abi.TALLY_RD2D, abi.TALLY_DETPHOT2D, abi.TALLY_RD_SLOTS)
+    with gpu.Engine(abi.SIM_MCXYZ, 0, ext) as e:
+        e.prepare_data(rp, tp, v)
+        e.set_radial_tally(32, 0.01)
+        e.set_voxel_props(np.full(v.size, 1.0, np.float32), np.full(v.size, 90.0, np.float32),
+                          np.full(v.size, 0.9, np.float32))
+        e.run(0, 20_000)
+        e.prepare_data(rp, tp, v2)
+        e.run(5, 30_000)
+        again = (_tallies(e, which), e.summary())
+        with pytest.raises(Exception):
+            e.tally(abi.TALLY_RD_R)  # the radial tally went with the first preparation
+    with gpu.Engine(abi.SIM_MCXYZ, 0, ext) as e:
+        e.prepare_data(rp, tp, v2)
+        e.run(5, 30_000)
+        fresh = (_tallies(e, which), e.summary())
+    for w in which:
+        np.testing.assert_array_equal(again[0][w], fresh[0][w])
+    for k in ("photons", "substeps", "scatters", "rd_sum"):
+        assert again[1][k] == fresh[1][k], k
