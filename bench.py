@@ -983,6 +983,23 @@ def run_notebook_workload(args) -> dict:
                        "timing": f"best of {max(args.steps, 1)} runs of the nmc program"}}
 
 
+def run_mcsub_workload(args) -> dict:
+    """C1 alone: the semi-infinite mcsub medium, ten 1e6-photon transport
+    launches device-timed (the measurement the default line carries as its
+    `mcsub_c1` extra), with the FP32 CPU restatement unless --no-cpu."""
+    import torch
+
+    from nmc_gb300 import build, engine
+
+    build.build()
+    torch.cuda.set_device(0)
+    ffma, _ = engine.probe_issue_peaks(0)
+    out = mcsub_extra(ffma, cpu=not args.no_cpu)
+    workload = out.pop("workload")
+    return {"metric": "photons/s, mcsub semi-infinite medium", **out, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload}}
+
+
 def run_speckle_workload(args) -> dict:
     """CBS speckle mutual-interference post-processing (MetalMC.m:628-742):
     a 256 x 256 exit map with 64 speckle records per pixel (seeded synthetic
@@ -1056,7 +1073,7 @@ def main():
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the warm-up and timed transport launches (for ncu)")
     ap.add_argument("--workload", default="skinvessel", choices=["skinvessel", "sweep", "sweep_mcsub", "adjoint", "cbs", "layered", "speckle",
-                             "notebook0", "notebook2"])
+                             "mcsub", "notebook0", "notebook2"])
     args = ap.parse_args()
     if args.workload == "sweep":
         out = run_sweep_workload(args)
@@ -1070,6 +1087,8 @@ def main():
         out = run_layered_workload(args)
     elif args.workload == "speckle":
         out = run_speckle_workload(args)
+    elif args.workload == "mcsub":
+        out = run_mcsub_workload(args)
     elif args.workload in ("notebook0", "notebook2"):
         out = run_notebook_workload(args)
     else:
