@@ -484,11 +484,12 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
     sleft = sv ? 0.f : sleft - s * c.y;
     {
       bool moved = false;
-      if (!TT && !sv) {  // surface detection (:556-637)
+      if (!TT) {  // surface detection (:556-637), on steps that leave the cell
+        // (tested by every lane: the predicate costs less than a branch on sv)
         const float rel = (float)(P.ksurf - kz) * P.dz + (P.fsurf - fz);  // zsurf - z
         const float su = s * uz;
-        const bool cross = (P.det_state == NMC_DET_REFLECTANCE && su <= rel && uz < 0.f) ||
-                           (P.det_state == NMC_DET_TRANSMITTANCE && su >= rel && uz > 0.f);
+        const bool cross = !sv && ((P.det_state == NMC_DET_REFLECTANCE && su <= rel && uz < 0.f) ||
+                                   (P.det_state == NMC_DET_TRANSMITTANCE && su >= rel && uz > 0.f));
         if (__builtin_expect(cross, 0)) {
           const float dl_b = rel / uz;
           if (back) {
