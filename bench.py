@@ -63,7 +63,7 @@ MUFU_PER_EF_SCATTER = 14.0
 # Warp instructions the transport kernel issues per voxel sub-step
 # (smsp__inst_executed.sum / sub-steps of the 1e7-photon ncu capture of this
 # workload), and the SM's issue rate (4 warp instructions per clock).
-WARP_INSTR_PER_SUBSTEP = 317_851_629_259 / 2.5583e10
+WARP_INSTR_PER_SUBSTEP = 317_868_610_037 / 2.5583e10
 ISSUE_PER_SM_CLOCK = 4.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 1e8-photon
 # launch of the transport kernel on this workload, captured on that launch
