@@ -252,7 +252,7 @@ def test_l2_set_aside_restored_on_destroy(gpu):
     assert rt.cudaDeviceGetAttribute(ctypes.byref(maxp), 108, 0) == 0  # cudaDevAttrMaxPersistingL2CacheSize
     needed = min(160 ** 3 * 8, maxp.value)  # the u64 fluence tally of the grid, capped by the device
     print("persisting L2 set-aside before / during / after:", before, during, after, "needed", needed)
-    assert during >= max(before, needed)  # the driver may round the set-aside up
+    assert during >= max(before, needed)  # the CUDA driver may round the set-aside up
     assert after == before
 
 
