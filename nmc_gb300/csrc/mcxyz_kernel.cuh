@@ -22,13 +22,11 @@
 //   Q_v += D * dln p_HG(cos; g_v)/dg  for every scattering in voxel v,
 // from which dScore/dmua_v = -L_v (pathwise: the weight is exp(-sum mua s)),
 // dScore/dmus_v = M_v and dScore/dg_v = Q_v (likelihood ratio).  s' = s
-// except at the detection plane, where the reference relocates the photon
-// to the plane after charging the whole step: when the hop would have ended
-// in the voxel, s' = the distance to the plane (the rest of the hop is
-// consumed afterwards, memorylessly); when the step ran to the voxel face,
-// the rest of the hop becomes a fixed length (kernels.metal:571-573), so
-// s' = s and neither the rest nor the scattering that ends it depend on
-// the exponential draw.
+// everywhere.  Only a step to a voxel face reaches the detection plane
+// (kernels.metal:534-637).  There the reference relocates the photon to the
+// plane after charging the whole step, and the rest of the hop becomes a
+// fixed length (:571-573), so neither that rest nor the scattering that
+// ends it depends on the exponential draw.
 //
 // Design:
 //  * persistent threads: the grid fills the GPU once; a thread that retires a
@@ -452,7 +450,6 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
     const float sy = (!VOX && dyf == 0.f) ? P.dy * ry : ty;
     const bool sv = s <= fminf(sx, fminf(sy, tz));
     if (!sv) s = kLS + fminf(tx, fminf(ty, tz));
-    float s_mus = s;  // adjoint: the hop length whose probability depends on mus
     const float D_in = D;
     const bool fixed_before = (st & kFixed) != 0;
     float e_dep = 0.f;  // adjoint: score of this sub-step's deposit
@@ -492,12 +489,7 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
                                    (P.det_state == NMC_DET_TRANSMITTANCE && su >= rel && uz > 0.f));
         if (__builtin_expect(cross, 0)) {
           const float dl_b = rel / uz;
-          if (back) {
-            if (sv)
-              s_mus = dl_b;
-            else
-              st |= kFixed;  // the rest of this hop is a fixed length
-          }
+          if (back) st |= kFixed;  // the rest of this hop is a fixed length
           sleft = (s - dl_b) * c.y;
           fx = fmaf(dl_b, ux, fx);
           fy = fmaf(dl_b, uy, fy);
@@ -589,7 +581,8 @@ __global__ void __launch_bounds__(256, 4) mcxyz_kernel(const XyzParams P) {
         }
       }
     }
-    if (back && !fixed_before) adj.M = fmaf(-D_in, s_mus, adj.M);
+    // the step length s is the hop length whose probability depends on mus
+    if (back && !fixed_before) adj.M = fmaf(-D_in, s, adj.M);
     if (!sv) {
       // voxel index (:641-643): inside the grid this is the cell plus N/2
       int ix = P.hx + kx + (int)(fx >= hdx_e);
